@@ -1,0 +1,243 @@
+/*
+ * spray_gpu.h -- C ABI of the GB300 (sm_103a) speculative domain-parallel
+ * ray tracer.
+ *
+ * The reference has no plugin or FFI boundary: its tracer is a compile-time
+ * template argument of the renderer, SprayRenderer<TracerT>
+ * (src/render/spray_renderer.h:45-78), which calls
+ *   tracer_.init(cfg, camera_, &scene_, &image_)   (src/render/spray_renderer.inl:58)
+ *   tracer_.trace()                                 (src/render/spray_renderer.inl:364)
+ * on an ooc::Tracer<ShaderAo|ShaderPt<Scene<InfiniteCache|LruCache>>>
+ * (src/apps/spray_ooc.cc:56-104, src/ooc/ooc_tracer.h:52-103).
+ * The entry points below are what a binding of that tracer concept needs:
+ * create/configure (Config + Tracer::init), scene upload (Scene::init and the
+ * domain cache), camera (Camera::init), trace one frame into an HdrImage
+ * buffer (Tracer::trace), destroy.  Test hooks expose the intermediate queues
+ * and hits of the first wavefront for comparison with a CPU oracle.
+ *
+ * Conventions: every function returns 0 on success or a SPRAY_GPU_E* code;
+ * spray_gpu_last_error() returns a message for the calling thread's last
+ * failure.  No C++ exception crosses this boundary.  A tracer is used by one
+ * thread at a time; calls block until the GPU work they issue has finished
+ * unless stated otherwise.  The library copies all caller data it keeps.
+ */
+#ifndef SPRAY_GPU_H_
+#define SPRAY_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPRAY_GPU_OK 0
+#define SPRAY_GPU_EINVAL 1    /* bad argument or configuration */
+#define SPRAY_GPU_ECUDA 2     /* CUDA runtime error or no usable GPU */
+#define SPRAY_GPU_EIO 3       /* scene or PLY file could not be read */
+#define SPRAY_GPU_ESTATE 4    /* call out of order (e.g. trace before scene) */
+#define SPRAY_GPU_EOVERFLOW 5 /* a ray overlapped more domains than the list holds */
+#define SPRAY_GPU_ENOMEM 6    /* device or pinned host allocation failed */
+#define SPRAY_GPU_ETIMEOUT 7  /* a bounded device-side wait gave up */
+
+typedef struct spray_gpu_tracer spray_gpu_tracer;
+typedef struct spray_scene spray_scene;
+
+/* Run parameters.  Mirrors spray::Config (src/render/config.h:34-95) with the
+ * defaults of Config::Config() (src/render/config.cc:33-73); fields after
+ * `nthreads` are extensions that are off (0) in reference-exact mode. */
+typedef struct spray_gpu_config {
+  int32_t image_w;              /* --width (400) */
+  int32_t image_h;              /* --height (400) */
+  int32_t ao_mode;              /* --ao-mode: 1 = ShaderAo, 0 = ShaderPt (0) */
+  int32_t ao_samples;           /* --ao-samples (8); area-light samples in PT */
+  int32_t pixel_samples;        /* --pixel-samples (4) */
+  int32_t bounces;              /* --bounces (1) */
+  float ks[3];                  /* --blinn ks (unset in the reference without --blinn; 0 here) */
+  float shininess;              /* --blinn shininess (0) */
+  float fov;                    /* --fov, vertical, degrees (90) */
+  int32_t cache_size;           /* --cache-size: <0 every domain resident, else LRU capacity in domains (-1) */
+  int32_t max_samples_per_rank; /* --max-samples-per-rank (1048576) */
+  int32_t list_size;            /* SPRAY_RAY_DOMAIN_LIST_SIZE (16) */
+  int32_t history_size;         /* SPRAY_SPECU_HISTORY_SIZE (4) */
+  int32_t nthreads;             /* --nthreads; not used by the GPU path (1) */
+  int32_t num_ranks;            /* image-space ranks (mpi::worldSize) sharing the frame (1) */
+  int32_t rank;                 /* this rank: renders vertical stripe `rank` (mpi::worldRank) (0) */
+  /* ---- extensions ---- */
+  int32_t ao_light_shadow;      /* AO: one extra shadow ray toward light 0 (0) */
+  float ao_max_distance;        /* AO rays end at this distance; 0 = unbounded (0) */
+  int32_t rr_depth;             /* Russian roulette on bounce rays from this depth; 0 = off (0) */
+  int32_t cull;                 /* skip (ray, domain) pairs entered beyond the closest hit found so far (1) */
+  int64_t cache_bytes;          /* device domain-cache cap in bytes; 0 = use cache_size (0) */
+  int64_t wave_samples;         /* samples traced per wavefront; 0 = library default (0) */
+  int32_t debug_capture;        /* keep the first wavefront's stage buffers for the debug hooks (0) */
+  int32_t device;               /* CUDA device ordinal (0) */
+} spray_gpu_config;
+
+/* One domain: a triangle mesh in world space (transform already applied, as
+ * TriMeshBuffer::load does, src/render/trimesh_buffer.cc:117-169) and the
+ * world AABB the scheduler tests rays against (Domain::world_aabb,
+ * src/render/domain.h:30-40).  Vertex normals are computed by the library in
+ * face order (TriMeshBuffer::computeNormals, trimesh_buffer.cc:267-326). */
+typedef struct spray_gpu_domain {
+  const float* vertices;    /* 3 * num_vertices floats */
+  const uint32_t* faces;    /* 3 * num_faces vertex indices */
+  const uint32_t* colors;   /* num_vertices packed 0x00RRGGBB, or NULL (black) */
+  int64_t num_vertices;
+  int64_t num_faces;
+  float world_bounds[6];    /* min x y z, max x y z */
+  int32_t bsdf_type;        /* 0 diffuse, 1 mirror, 2 glass, 3 transmission */
+  float bsdf_params[3];     /* albedo / reflectance, or eta_exterior, eta_interior */
+} spray_gpu_domain;
+
+/* A light (src/render/light.h:41-89): point (position, radiance), diffuse
+ * hemisphere (radiance), or -- extension -- an emissive quad (position =
+ * corner, edge1, edge2, radiance). */
+typedef struct spray_gpu_light {
+  int32_t type;             /* 0 point, 1 diffuse hemisphere, 2 quad */
+  float position[3];
+  float radiance[3];
+  float edge1[3];
+  float edge2[3];
+} spray_gpu_light;
+
+/* Per-frame counters.  A "ray" is one logical ray counted once, whatever the
+ * number of domains it visits; a "visit" is one (ray, domain) pair traced. */
+typedef struct spray_gpu_stats {
+  int64_t rays_primary;
+  int64_t rays_shadow;      /* AO and light-shadow rays */
+  int64_t rays_bounce;
+  int64_t visits_radiance;
+  int64_t visits_shadow;
+  int64_t visits_culled;    /* pairs skipped by entry-distance culling */
+  int64_t domain_loads;     /* domain-cache misses (host-to-device domain copies) */
+  int64_t h2d_bytes;        /* bytes copied host-to-device during the frame */
+  int64_t d2h_bytes;
+  int64_t kernel_launches;  /* kernels this library launched during the frame */
+  int64_t list_overflows;   /* rays whose domain list exceeded list_size */
+  double frame_ms;          /* device time of the frame (CUDA events) */
+  double trace_ms;          /* device time inside the closest-hit kernel */
+  double occlude_ms;        /* device time inside the occlusion kernel */
+  double schedule_ms;       /* device time inside the scheduling kernels */
+  int64_t trace_launches;
+  int64_t occlude_launches;
+} spray_gpu_stats;
+
+/* ---------------------------------------------------------------- setup */
+void spray_gpu_config_defaults(spray_gpu_config* cfg);
+const char* spray_gpu_last_error(void);
+
+/* Tracer::init (src/ooc/ooc_tracer.inl:28-82) without the scene/camera. */
+int spray_gpu_create(const spray_gpu_config* cfg, spray_gpu_tracer** out);
+int spray_gpu_destroy(spray_gpu_tracer* t);
+
+/* Scene::init + domain cache warm-up (src/render/scene.inl:30-100).  Builds
+ * each domain's BVH and uploads every domain when the cache holds them all. */
+int spray_gpu_set_scene(spray_gpu_tracer* t, const spray_gpu_domain* domains, int32_t num_domains,
+                        const spray_gpu_light* lights, int32_t num_lights);
+
+/* Camera::init (src/render/camera.h:128-166); vfov in degrees. */
+int spray_gpu_set_camera(spray_gpu_tracer* t, const float pos[3], const float lookat[3],
+                         const float up[3], float vfov);
+
+/* Tracer::trace (src/ooc/ooc_tracer.inl:184-234): renders one frame and
+ * writes W*H RGBA floats to rgba_out (host memory) with HdrImage semantics:
+ * the buffer is cleared, then every unoccluded, history-consistent shadow ray
+ * adds w / pixel_samples to its pixel (src/ooc/ooc_tcontext.inl:123-135). */
+int spray_gpu_trace(spray_gpu_tracer* t, float* rgba_out, spray_gpu_stats* stats);
+
+/* Same frame, result left in device memory (W*H*4 floats at rgba_dev), for
+ * callers that keep the image on the GPU.  No host copy. */
+int spray_gpu_trace_device(spray_gpu_tracer* t, float* rgba_dev, spray_gpu_stats* stats);
+
+/* ---------------------------------------------------------------- host scene
+ * SceneLoader::load + PlyLoader (src/io/scene_loader.cc:315-358,
+ * src/io/ply_loader.cc:179-324): parse a .spray file and load every domain's
+ * PLY with its transform applied.  The loaded scene can be handed to
+ * spray_gpu_set_scene through spray_scene_domains/lights. */
+int spray_scene_load(const char* spray_file, const char* ply_path, spray_scene** out);
+int spray_scene_free(spray_scene* s);
+int spray_scene_counts(const spray_scene* s, int32_t* num_domains, int32_t* num_lights);
+/* Fills caller arrays; the domain pointers stay valid until spray_scene_free. */
+int spray_scene_domains(const spray_scene* s, spray_gpu_domain* out, int32_t capacity);
+int spray_scene_lights(const spray_scene* s, spray_gpu_light* out, int32_t capacity);
+
+/* Writes a binary little endian PLY (float xyz, uchar rgb, int faces). */
+int spray_write_ply(const char* path, const float* vertices, int64_t num_vertices,
+                    const uint32_t* colors, const uint32_t* faces, int64_t num_faces);
+
+/* Wavelet isosurface of f = 255 exp(-(x^2+y^2+z^2)/(2*0.5^2)) + 10 sin(60x+p0)
+ * + 18 sin(30y+p1) + 5 cos(40z+p2) on [-1,1]^3 sampled on samples^3 points.
+ * The caller provides the output capacities; counts are returned even when the
+ * arrays are too small (then SPRAY_GPU_EOVERFLOW). */
+int spray_generate_wavelet(int32_t samples, double iso, const double phase[3], float* vertices,
+                           int64_t vertex_capacity, uint32_t* faces, int64_t face_capacity,
+                           int64_t* num_vertices, int64_t* num_faces);
+
+/* ---------------------------------------------------------------- test hooks
+ * With cfg.debug_capture set, the first wavefront of the last traced frame is
+ * kept; these copy its stage buffers out.  `bounce` selects the radiance depth.
+ * Record layouts are the spray_gpu_dbg_* structs below; count is in records. */
+#define SPRAY_DBG_RAYS 0        /* spray_gpu_dbg_ray, radiance rays entering the bounce */
+#define SPRAY_DBG_RQUEUES 1     /* spray_gpu_dbg_entry, radiance queue entries */
+#define SPRAY_DBG_HITS 2        /* spray_gpu_dbg_hit, resolved closest hits */
+#define SPRAY_DBG_SHADOWS 3     /* spray_gpu_dbg_shadow, shadow rays and their occlusion */
+#define SPRAY_DBG_SQUEUES 4     /* spray_gpu_dbg_entry, shadow queue entries */
+#define SPRAY_DBG_SCORES 5      /* spray_gpu_dbg_score, domain scores and schedule order */
+
+typedef struct spray_gpu_dbg_ray {
+  uint32_t sample;   /* index of the sample in the wavefront */
+  int32_t pixid;
+  int32_t samid;
+  float org[3];
+  float dir[3];
+  float w[3];
+} spray_gpu_dbg_ray;
+
+/* One (ray, domain) queue entry: RayData{ray, tdom, dom_depth} pushed to the
+ * queue of `domain` (src/ooc/ooc_isector.h:126-174).  Entries are grouped by
+ * domain; within a domain they are in ray order.  origin = 1 marks the test of
+ * a shadow ray in the domain that spawned it (TContext::procShads2,
+ * src/ooc/ooc_tcontext.inl:73-91). */
+typedef struct spray_gpu_dbg_entry {
+  int32_t domain;
+  uint32_t ray;      /* radiance: sample index; shadow: sample * slots + slot */
+  float tdom;
+  int32_t depth;
+  int32_t origin;
+} spray_gpu_dbg_entry;
+
+typedef struct spray_gpu_dbg_hit {
+  uint32_t sample;
+  int32_t hit;
+  float t;
+  int32_t domain;
+  int32_t prim;
+  uint32_t color;
+  float ns[3];
+} spray_gpu_dbg_hit;
+
+typedef struct spray_gpu_dbg_shadow {
+  uint32_t sample;
+  int32_t slot;
+  float org[3];
+  float dir[3];
+  float w[3];
+  float tmax;
+  int32_t occluded;
+} spray_gpu_dbg_shadow;
+
+typedef struct spray_gpu_dbg_score {
+  int32_t domain;
+  int64_t score;
+  int32_t order;     /* position of the domain in the processing schedule */
+} spray_gpu_dbg_score;
+
+int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int64_t* count);
+int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void* out,
+                         int64_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPRAY_GPU_H_ */

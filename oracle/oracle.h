@@ -1,0 +1,123 @@
+/*
+ * CPU oracle for the speculative domain-parallel ray-tracing loop of SpRay.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library restates, in plain C++, the
+ * reference's CPU algorithm for the hot path so the CUDA path can be checked
+ * against it.  Only tests, the smoke check and bench.py's CPU-baseline leg
+ * call it.  It shares no code with the product.
+ *
+ * Parity is unpinned against the reference binary: the reference needs
+ * Embree 2.17, glm, glog and MPI, none of which are available, and it ships no
+ * golden vectors.  The oracle substitutes its own BVH and the published
+ * watertight triangle test (Woop, Benthin, Wald, JCGT 2013) for Embree, and
+ * its own vector math for glm.
+ *
+ * Two modes:
+ *   A  orc_render_speculative: the reference's loop itself -- per-thread
+ *      queues, DomainStats score order, VBuf speculation history, pending
+ *      queue, LRU/infinite domain cache, OpenMP threads with the same barriers.
+ *   B  stage functions (eye rays, scheduling, closest hit, shading, occlusion)
+ *      and orc_render_wavefront, which applies them bounce by bounce.
+ */
+#ifndef SPRAY_ORACLE_H_
+#define SPRAY_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_config {
+  int32_t image_w, image_h;
+  int32_t ao_mode, ao_samples, pixel_samples, bounces;
+  float ks[3];
+  float shininess;
+  float fov;
+  int32_t cache_size;          /* <0 infinite cache, else LRU capacity in domains */
+  int32_t max_samples_per_rank;
+  int32_t list_size;           /* SPRAY_RAY_DOMAIN_LIST_SIZE */
+  int32_t history_size;        /* SPRAY_SPECU_HISTORY_SIZE (<= 8) */
+  int32_t num_ranks, rank;
+  /* extensions (0 = reference behaviour) */
+  int32_t ao_light_shadow;
+  float ao_max_distance;
+  int32_t rr_depth;
+} orc_config;
+
+typedef struct orc_stats {
+  int64_t rays_primary, rays_shadow, rays_bounce;
+  int64_t visits_radiance, visits_shadow;
+  int64_t domain_loads;
+  int64_t rounds;
+} orc_stats;
+
+void* orc_create(const orc_config* cfg, int32_t num_domains);
+void orc_destroy(void* o);
+/* world-space mesh of domain d (copied); bounds = world AABB min xyz, max xyz */
+int orc_set_domain(void* o, int32_t d, const float* vertices, int64_t nv, const uint32_t* faces,
+                   int64_t nf, const uint32_t* colors, const float bounds[6], int32_t bsdf,
+                   const float params[3]);
+/* lights: 13 floats each: type, position[3], radiance[3], edge1[3], edge2[3] */
+int orc_set_lights(void* o, int32_t nl, const float* lights);
+int orc_build(void* o);  /* vertex normals and per-domain BVHs */
+int orc_set_camera(void* o, const float pos[3], const float lookat[3], const float up[3], float vfov);
+int orc_normals(void* o, int32_t d, float* out);  /* 3 * nv */
+
+/* blocking tiles: writes 4 ints (x, y, w, h) per tile, returns count */
+int32_t orc_tiles(void* o, int32_t* out, int32_t capacity);
+
+/* eye rays of tiles [first, first + count): org/dir 3 floats, pixid, samid */
+int64_t orc_gen_eyes(void* o, int32_t first_tile, int32_t num_tiles, float* org, float* dir,
+                     int32_t* pixid, int32_t* samid);
+
+/* Scheduling of n rays.  Radiance (origin == NULL): Isector::isectAll.
+ * Shadow (origin != NULL, tmax per ray): the test in the origin domain plus
+ * Isector::isectWithoutCurrentDomain.  Entries (5 ints each: domain, ray,
+ * tdom bits, depth, origin flag) are written queue by queue in push order;
+ * dstats [D][list_size] counts pushes per (domain, depth).  Returns the
+ * number of entries or -1 when capacity is too small. */
+int64_t orc_schedule(void* o, int64_t n, const float* org, const float* dir, const float* tmax,
+                     const int32_t* origin, int32_t* entries, int64_t capacity, int64_t* dstats);
+
+/* DomainStats::schedule on dstats: scores[D], order[D] (ties by id). */
+int orc_scores(void* o, const int64_t* dstats, int64_t* scores, int32_t* order);
+
+/* Closest hit over the AABB-overlapped domains of each ray.  Per ray: hit,
+ * t, domain, prim, u, v, colour, Ns[3]. */
+int orc_closest(void* o, int64_t n, const float* org, const float* dir, int32_t* hit, float* t,
+                int32_t* domain, int32_t* prim, float* u, float* v, uint32_t* color, float* ns);
+
+/* Occlusion of shadow rays (origin domain always tested). */
+int orc_occluded(void* o, int64_t n, const float* org, const float* dir, const float* tmax,
+                 const int32_t* origin, uint8_t* occluded);
+
+/* Shader at actual depth `depth` for n rays with hits.  Per ray input: org,
+ * dir, w (3 floats each), pixid, samid, hit t, domain, colour, Ns[3].
+ * Output per ray: `slots` shadow rays (dir[3], w[3], tmax, valid) and one
+ * bounce ray (dir[3], w[3], valid). */
+int32_t orc_slots(void* o);
+int orc_shade(void* o, int32_t depth, int64_t n, const float* org, const float* dir, const float* w,
+              const int32_t* pixid, const int32_t* samid, const float* t, const int32_t* domain,
+              const uint32_t* color, const float* ns, float* sdir, float* sw, float* stmax,
+              uint8_t* svalid, float* bdir, float* bw, uint8_t* bvalid);
+
+/* Known-answer hooks: RandomSampler stream, slab test, triangle test, LRU. */
+int orc_rng(int32_t seed, int32_t n, float* out);
+int orc_sincos(int64_t n, const float* x, float* s, float* c);
+int orc_slab(const float bounds[6], const float org[3], const float dir[3], float t0, float t1,
+             float* tmin, float* tmax);
+int orc_triangle(const float org[3], const float dir[3], const float v[9], float tnear, float tfar,
+                 float* t, float* u, float* v_out);
+/* replays domain loads through LruCache; hits[i] = 1 on a cache hit */
+int orc_lru_trace(int32_t num_domains, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits);
+
+/* Full frames: W*H*4 floats. */
+int orc_render_wavefront(void* o, float* rgba, orc_stats* stats);
+int orc_render_speculative(void* o, int32_t nthreads, float* rgba, orc_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

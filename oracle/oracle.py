@@ -1,0 +1,296 @@
+"""ctypes wrapper of the CPU oracle (oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: the CPU restatement of SpRay's speculative
+domain-parallel ray-tracing loop that the CUDA path is checked against.  Only
+tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+Parity is unpinned against the reference binary (it cannot be built here:
+Embree 2.17, glm, glog and MPI are absent and it ships no golden vectors).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "oracle.cpp"
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime,
+                                                               (HERE / "oracle.h").stat().st_mtime):
+        tmp = LIB.with_suffix(".tmp.so")
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+               "-o", str(tmp), str(SRC)]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stdout)
+        tmp.replace(LIB)
+    return LIB
+
+
+class OrcConfig(C.Structure):
+    _fields_ = [
+        ("image_w", C.c_int32), ("image_h", C.c_int32), ("ao_mode", C.c_int32),
+        ("ao_samples", C.c_int32), ("pixel_samples", C.c_int32), ("bounces", C.c_int32),
+        ("ks", C.c_float * 3), ("shininess", C.c_float), ("fov", C.c_float),
+        ("cache_size", C.c_int32), ("max_samples_per_rank", C.c_int32), ("list_size", C.c_int32),
+        ("history_size", C.c_int32), ("num_ranks", C.c_int32), ("rank", C.c_int32),
+        ("ao_light_shadow", C.c_int32), ("ao_max_distance", C.c_float), ("rr_depth", C.c_int32),
+    ]
+
+
+class OrcStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("rays_primary", "rays_shadow", "rays_bounce",
+                                         "visits_radiance", "visits_shadow", "domain_loads",
+                                         "rounds")]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P = C.c_void_p
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [C.POINTER(OrcConfig), C.c_int32]
+        L.orc_destroy.argtypes = [P]
+        L.orc_set_domain.argtypes = [P, C.c_int32, P, C.c_int64, P, C.c_int64, P, P, C.c_int32, P]
+        L.orc_set_lights.argtypes = [P, C.c_int32, P]
+        L.orc_build.argtypes = [P]
+        L.orc_set_camera.argtypes = [P, P, P, P, C.c_float]
+        L.orc_normals.argtypes = [P, C.c_int32, P]
+        L.orc_tiles.argtypes = [P, P, C.c_int32]
+        L.orc_tiles.restype = C.c_int32
+        L.orc_gen_eyes.argtypes = [P, C.c_int32, C.c_int32, P, P, P, P]
+        L.orc_gen_eyes.restype = C.c_int64
+        L.orc_schedule.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int64, P]
+        L.orc_schedule.restype = C.c_int64
+        L.orc_scores.argtypes = [P, P, P, P]
+        L.orc_closest.argtypes = [P, C.c_int64, P, P, P, P, P, P, P, P, P, P]
+        L.orc_occluded.argtypes = [P, C.c_int64, P, P, P, P, P]
+        L.orc_slots.argtypes = [P]
+        L.orc_slots.restype = C.c_int32
+        L.orc_shade.argtypes = [P, C.c_int32, C.c_int64] + [P] * 16
+        L.orc_rng.argtypes = [C.c_int32, C.c_int32, P]
+        L.orc_sincos.argtypes = [C.c_int64, P, P, P]
+        L.orc_slab.argtypes = [P, P, P, C.c_float, C.c_float, P, P]
+        L.orc_triangle.argtypes = [P, P, P, C.c_float, C.c_float, P, P, P]
+        L.orc_lru_trace.argtypes = [C.c_int32, C.c_int32, C.c_int64, P, P]
+        L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
+        L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+ORACLE_FIELDS = [f for f, _ in OrcConfig._fields_]
+
+
+def rng_floats(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    lib().orc_rng(seed, n, _p(out))
+    return out
+
+
+def sincos(x) -> tuple[np.ndarray, np.ndarray]:
+    x = _f32(x)
+    s = np.zeros_like(x)
+    c = np.zeros_like(x)
+    lib().orc_sincos(len(x), _p(x), _p(s), _p(c))
+    return s, c
+
+
+def slab(bounds, org, dir, t0=0.001, t1=np.inf):
+    tmin = np.zeros(1, np.float32)
+    tmax = np.zeros(1, np.float32)
+    hit = lib().orc_slab(_p(_f32(bounds)), _p(_f32(org)), _p(_f32(dir)), t0, t1, _p(tmin), _p(tmax))
+    return bool(hit), float(tmin[0]), float(tmax[0])
+
+
+def triangle(org, dir, verts, tnear=0.001, tfar=np.inf):
+    t = np.zeros(1, np.float32)
+    u = np.zeros(1, np.float32)
+    v = np.zeros(1, np.float32)
+    hit = lib().orc_triangle(_p(_f32(org)), _p(_f32(dir)), _p(_f32(verts).reshape(9)), tnear, tfar,
+                             _p(t), _p(u), _p(v))
+    return bool(hit), float(t[0]), float(u[0]), float(v[0])
+
+
+def lru_trace(num_domains: int, cache_size: int, ids) -> np.ndarray:
+    ids = _i32(ids)
+    hits = np.zeros(len(ids), np.uint8)
+    lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits))
+    return hits
+
+
+class Oracle:
+    """CPU oracle for one configuration and scene (see oracle.h)."""
+
+    def __init__(self, config: dict, scene):
+        c = OrcConfig()
+        for k in ORACLE_FIELDS:
+            if k == "ks":
+                c.ks = (C.c_float * 3)(*config.get("ks", (0, 0, 0)))
+            elif k in config:
+                setattr(c, k, config[k])
+        self.config = dict(config)
+        self.scene = scene
+        self.L = lib()
+        self.h = self.L.orc_create(C.byref(c), len(scene.domains))
+        if not self.h:
+            raise RuntimeError("orc_create failed")
+        for i, d in enumerate(scene.domains):
+            self.L.orc_set_domain(self.h, i, _p(d.vertices), len(d.vertices), _p(d.faces), len(d.faces),
+                                  _p(d.colors), _p(d.bounds), d.bsdf_type, _p(d.bsdf_params))
+        lf = np.zeros((max(len(scene.lights), 1), 13), np.float32)
+        for i, l in enumerate(scene.lights):
+            lf[i, 0] = l.type
+            lf[i, 1:4] = l.position
+            lf[i, 4:7] = l.radiance
+            lf[i, 7:10] = l.edge1
+            lf[i, 10:13] = l.edge2
+        self.L.orc_set_lights(self.h, len(scene.lights), _p(lf))
+        self.L.orc_build(self.h)
+        self.D = len(scene.domains)
+
+    def close(self):
+        if self.h:
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_camera(self, pos, lookat, up=(0, 1, 0), vfov=None):
+        fov = self.config.get("fov", 90.0) if vfov is None else vfov
+        self.L.orc_set_camera(self.h, _p(_f32(pos)), _p(_f32(lookat)), _p(_f32(up)), float(fov))
+
+    def normals(self, d):
+        out = np.zeros((len(self.scene.domains[d].vertices), 3), np.float32)
+        self.L.orc_normals(self.h, d, _p(out))
+        return out
+
+    def tiles(self):
+        out = np.zeros((4096, 4), np.int32)
+        n = self.L.orc_tiles(self.h, _p(out), 4096)
+        return out[:n]
+
+    def eyes(self, first_tile, num_tiles):
+        t = self.tiles()[first_tile:first_tile + num_tiles]
+        n = int((t[:, 2].astype(np.int64) * t[:, 3]).sum() * self.config["pixel_samples"])
+        org = np.zeros((n, 3), np.float32)
+        dr = np.zeros((n, 3), np.float32)
+        pix = np.zeros(n, np.int32)
+        sam = np.zeros(n, np.int32)
+        self.L.orc_gen_eyes(self.h, first_tile, num_tiles, _p(org), _p(dr), _p(pix), _p(sam))
+        return org, dr, pix, sam
+
+    def schedule(self, org, dir, tmax=None, origin=None, capacity=None):
+        org, dir = _f32(org), _f32(dir)
+        n = len(org)
+        cap = capacity or max(64, n * 40)
+        ent = np.zeros((cap, 5), np.int32)
+        L = self.config.get("list_size", 16)
+        dstats = np.zeros((self.D, L), np.int64)
+        tm = None if tmax is None else _f32(tmax)
+        og = None if origin is None else _i32(origin)
+        k = self.L.orc_schedule(self.h, n, _p(org), _p(dir), _p(tm), _p(og), _p(ent), cap, _p(dstats))
+        if k < 0:
+            raise RuntimeError("schedule capacity too small")
+        ent = ent[:k]
+        out = np.zeros(k, [("domain", "<i4"), ("ray", "<u4"), ("tdom", "<f4"), ("depth", "<i4"),
+                           ("origin", "<i4")])
+        out["domain"] = ent[:, 0]
+        out["ray"] = ent[:, 1].view(np.uint32)
+        out["tdom"] = ent[:, 2].view(np.float32)
+        out["depth"] = ent[:, 3]
+        out["origin"] = ent[:, 4]
+        return out, dstats
+
+    def scores(self, dstats):
+        sc = np.zeros(self.D, np.int64)
+        od = np.zeros(self.D, np.int32)
+        self.L.orc_scores(self.h, _p(np.ascontiguousarray(dstats, np.int64)), _p(sc), _p(od))
+        return sc, od
+
+    def closest(self, org, dir):
+        org, dir = _f32(org), _f32(dir)
+        n = len(org)
+        hit = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        dom = np.zeros(n, np.int32)
+        prim = np.zeros(n, np.int32)
+        u = np.zeros(n, np.float32)
+        v = np.zeros(n, np.float32)
+        col = np.zeros(n, np.uint32)
+        ns = np.zeros((n, 3), np.float32)
+        self.L.orc_closest(self.h, n, _p(org), _p(dir), _p(hit), _p(t), _p(dom), _p(prim), _p(u), _p(v),
+                           _p(col), _p(ns))
+        return dict(hit=hit, t=t, domain=dom, prim=prim, u=u, v=v, color=col, ns=ns)
+
+    def occluded(self, org, dir, tmax, origin):
+        org, dir = _f32(org), _f32(dir)
+        occ = np.zeros(len(org), np.uint8)
+        self.L.orc_occluded(self.h, len(org), _p(org), _p(dir), _p(_f32(tmax)), _p(_i32(origin)), _p(occ))
+        return occ
+
+    def slots(self):
+        return int(self.L.orc_slots(self.h))
+
+    def shade(self, depth, org, dir, w, pixid, samid, t, domain, color, ns):
+        n = len(org)
+        S = self.slots()
+        sdir = np.zeros((n, S, 3), np.float32)
+        sw = np.zeros((n, S, 3), np.float32)
+        stmax = np.zeros((n, S), np.float32)
+        sval = np.zeros((n, S), np.uint8)
+        bdir = np.zeros((n, 3), np.float32)
+        bw = np.zeros((n, 3), np.float32)
+        bval = np.zeros(n, np.uint8)
+        self.L.orc_shade(self.h, depth, n, _p(_f32(org)), _p(_f32(dir)), _p(_f32(w)), _p(_i32(pixid)),
+                         _p(_i32(samid)), _p(_f32(t)), _p(_i32(domain)),
+                         _p(np.ascontiguousarray(color, np.uint32)), _p(_f32(ns)), _p(sdir), _p(sw),
+                         _p(stmax), _p(sval), _p(bdir), _p(bw), _p(bval))
+        return dict(sdir=sdir, sw=sw, stmax=stmax, svalid=sval, bdir=bdir, bw=bw, bvalid=bval)
+
+    def _image(self):
+        return np.zeros((self.config["image_h"], self.config["image_w"], 4), np.float32)
+
+    def render_wavefront(self):
+        img = self._image()
+        st = OrcStats()
+        if self.L.orc_render_wavefront(self.h, _p(img), C.byref(st)) != 0:
+            raise RuntimeError("oracle wavefront render failed")
+        return img, st.asdict()
+
+    def render_speculative(self, nthreads=1):
+        img = self._image()
+        st = OrcStats()
+        if self.L.orc_render_speculative(self.h, nthreads, _p(img), C.byref(st)) != 0:
+            raise RuntimeError("oracle speculative render failed")
+        return img, st.asdict()

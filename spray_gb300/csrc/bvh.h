@@ -1,0 +1,36 @@
+// Per-domain bounding volume hierarchy: binned-SAH binary build collapsed into
+// 4-wide nodes.  Replaces the Embree triangle BVH SpRay rebuilds on every
+// domain load (src/render/trimesh_buffer.cc:104,224); here it is built once per
+// domain and kept with the domain's geometry.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace spray {
+
+// One 128-byte node: child boxes in SoA form, then the child references.
+//   child >= 0 : index of an inner node (domain-relative)
+//   child <  0 : leaf, ~child = (first_triangle << 3) | (count - 1)
+// Unused child slots carry an empty box (lo = +inf, hi = -inf).
+struct alignas(16) BvhNode4 {
+  float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
+  int32_t child[4];
+  int32_t pad[4];
+};
+static_assert(sizeof(BvhNode4) == 128, "node must be one 128-byte line");
+
+constexpr int kMaxLeafTris = 8;
+
+struct BvhBuildResult {
+  std::vector<BvhNode4> nodes;     // nodes[0] is the root
+  std::vector<uint32_t> tri_order;  // leaf order -> original face index
+  int depth = 0;                    // deepest node level (root = 1)
+};
+
+// Builds the BVH of a triangle mesh.  Boxes are exact min/max of the float
+// vertices, so traversal with a conservative box test never misses a triangle.
+void buildBvh4(const float* vertices, const uint32_t* faces, uint32_t num_faces,
+               BvhBuildResult* out);
+
+}  // namespace spray

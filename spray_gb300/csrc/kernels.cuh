@@ -1,0 +1,186 @@
+// Device data layout and kernel launchers of the wavefront tracer.
+//
+// One frame is traced as a sequence of wavefronts ("waves").  A wave holds
+// whole blocking tiles (src/render/tile.cc:317-391), so every sample keeps the
+// tile-local id SpRay seeds its random streams with.  Per bounce a wave runs:
+//   schedule  : slab test of every live ray against every domain AABB, sorted
+//               (t, id) domain list, stable partition of the (ray, domain)
+//               entries into per-domain queues        (ooc_isector.h:116-174)
+//   trace     : closest hit of each entry in its domain's BVH, folded into a
+//               per-ray packed 64-bit (t | triangle) atomicMin
+//   resolve   : the entry that owns the minimum publishes colour and normal
+//   shade     : AO / path-tracing shader spawns shadow rays and the bounce ray
+//                                                     (ooc_shader_ao.h, ooc_shader_pt.h)
+//   schedule + occlusion of the shadow rays, then retire into the image
+//                                                     (ooc_tcontext.inl:123-135)
+// Counts live in device memory so a bounce needs no host round trip.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bvh.h"
+
+namespace spray {
+
+constexpr int kMaxList = 32;       // longest per-ray domain list handled
+constexpr int kMaxEmit = kMaxList + 1;  // entries per ray: list plus a shadow ray's own domain
+constexpr int kRayIdBits = 26;     // entry word 0: ray id | depth << 26 | origin << 31
+constexpr uint32_t kRayIdMask = (1u << kRayIdBits) - 1u;
+constexpr int kMaxSlots = 64;      // shadow rays per hit
+constexpr int kSchedThreads = 256;
+constexpr int kDepthBuckets = 4;   // key = min(depth, 3) * D + domain when ordering by depth
+
+struct DomainDev {
+  float bmin[3], bmax[3];  // world AABB used by the scheduler
+  int32_t node_base;       // first BVH node of the domain (in its cache slot)
+  int32_t tri_base;        // first leaf-order triangle record
+  uint32_t gprim_base;     // global number of the domain's face 0
+  int32_t vert_base;       // first vertex (colours, normals)
+  int32_t face_base;       // first index triple (original face order)
+  int32_t bsdf;
+  float bsdf_p[3];
+  int32_t resident;        // 1 when the geometry is in device memory
+};
+
+struct SceneDev {
+  const DomainDev* domains;
+  int32_t num_domains;
+  const BvhNode4* nodes;
+  const float4* tris;       // 3 float4 per triangle, v0.w = domain-local face id
+  const uint32_t* faces;    // 3 per face
+  const uint32_t* colors;   // per vertex
+  const float* normals;     // 3 per vertex
+};
+
+struct Counters {
+  unsigned long long rays_primary;
+  unsigned long long rays_shadow;
+  unsigned long long rays_bounce;
+  unsigned long long visits_radiance;
+  unsigned long long visits_shadow;
+  unsigned long long visits_culled;
+  unsigned long long list_overflows;
+  unsigned long long arena_overflows;
+  unsigned long long entry_overflows;
+  unsigned long long error_flags;
+};
+
+// Radiance rays of a wave, indexed by sample.
+struct RayBuf {
+  float4* org;
+  float4* dir;
+  float4* wgt;
+  int32_t* pixid;
+  int32_t* samid;
+};
+
+// Shadow rays of a bounce, indexed by alive_index * slots + slot.
+struct ShadowBuf {
+  float4* dir;       // xyz, w = tmax
+  float4* wgt;       // xyz, w = 1 when the ray exists
+  float4* hitpos;    // per alive ray: hit point, w = origin domain (as float bits)
+  uint8_t* occluded;
+};
+
+struct CameraDev {
+  float pos[3];
+  float ll[3];   // lower-left corner of the image plane
+  float wv[3];   // full-width vector
+  float hv[3];   // full-height vector
+  float image_w, image_h;
+};
+
+struct TileDev {
+  int32_t x, y, w, h;
+  int64_t sample_base;  // first sample of the tile inside the wave
+};
+
+// Scheduling of one ray set into per-domain queues.
+struct SchedArgs {
+  int shadow;                 // 0 radiance, 1 shadow rays
+  const uint32_t* count;      // number of rays (device)
+  const uint32_t* list;       // ray ids (sample for radiance, shadow id for shadow)
+  RayBuf rays;                // radiance rays
+  ShadowBuf sh;               // shadow rays
+  int slots;                  // shadow slots per alive ray
+  int order_by_depth;         // key = min(depth,3)*D + domain, else domain
+  int list_size;              // SPRAY_RAY_DOMAIN_LIST_SIZE, for the domain statistics
+  uint64_t* ray_key;          // radiance: reset to kNoHit per scheduled ray
+  // outputs
+  uint2* arena;               // per-ray sorted (domain | depth << 16, tdom) lists
+  unsigned long long* arena_top;
+  unsigned long long arena_cap;
+  uint32_t* list_off;         // per scheduled ray
+  uint32_t* list_cnt;
+  uint32_t* hist;             // [nkeys][nwarps]
+  long long* dstats;          // [D][list_size] ray counts per (domain, depth)
+  uint2* entries;             // partitioned entries
+  unsigned long long entry_cap;
+  uint32_t* key_start;        // [nkeys + 1]
+  uint32_t* num_entries;      // total entries (device)
+  Counters* ctr;
+};
+
+struct TraceArgs {
+  SceneDev scene;
+  const uint2* entries;
+  const uint32_t* num_entries;
+  const uint32_t* key_start;
+  int nkeys;
+  unsigned int* work;         // work-stealing counter (zeroed before launch)
+  RayBuf rays;
+  ShadowBuf sh;
+  int slots;
+  uint64_t* ray_key;
+  uint64_t* rec_key;          // per entry
+  float4* rec_attr;           // per entry: Ns xyz, colour bits in w
+  int cull;
+  Counters* ctr;
+};
+
+struct ShadeArgs {
+  SceneDev scene;
+  const uint32_t* count;      // alive rays
+  const uint32_t* list;       // alive samples
+  RayBuf rays;                // rays of this bounce
+  RayBuf next;                // bounce rays for the next depth
+  uint8_t* next_flag;         // per sample
+  const uint64_t* ray_key;
+  float4* hit_ns;             // per sample: resolved Ns xyz, colour bits in w
+  ShadowBuf sh;
+  uint8_t* shadow_flag;       // per shadow id
+  int slots;
+  int depth;                  // actual depth of the rays being shaded
+  // shader configuration
+  int ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow;
+  float ao_max_distance;
+  float ks[3], shininess;
+  const float* lights;        // 13 floats per light: type, pos, radiance, e1, e2
+  int num_lights;
+  Counters* ctr;
+};
+
+// ---------------------------------------------------------------- launchers
+void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int ntiles,
+                      int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
+                      uint32_t* alive_count, int32_t* alive_idx, Counters* ctr);
+void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
+                    int nwarps, int nblocks, uint32_t* scan_tmp);
+void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks);
+void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks);
+void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks);
+void launchShade(cudaStream_t s, const ShadeArgs& a, int nblocks);
+// Stable compaction of flag[i] != 0 for i < n (n from *n_dev or n_host when
+// n_dev is null) into list, count and, optionally, index_of[i] (-1 if unset).
+// The element count is (*n_dev) * n_mul when n_dev is set, else n_host.
+void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
+                   uint64_t n_host, uint32_t* list, uint32_t* count, int32_t* index_of,
+                   uint32_t* block_tmp, int nblocks);
+void launchRetireImpl(cudaStream_t s, float4* image, int64_t npix, int spp, const int32_t* pixid,
+                      const int32_t* alive_idx, const ShadowBuf sh, const uint8_t* flag, int slots,
+                      double scale, int nblocks);
+void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int list_size,
+                  long long* scores, int32_t* order);
+
+}  // namespace spray

@@ -1,0 +1,430 @@
+// Primary-ray generation, the speculative scheduler (ray -> per-domain
+// queues), stable stream compaction and the domain scores.
+#include <cfloat>
+
+#include "kernels.cuh"
+#include "spray_math.cuh"
+
+namespace spray {
+
+__device__ __forceinline__ uint32_t laneMaskLt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint32_t warpExclusiveScan(uint32_t v, uint32_t* total) {
+  const int lane = threadIdx.x & 31;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  *total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
+// ---------------------------------------------------------------- primary rays
+// Eye rays of SpRay's Tracer::genSingleEyes / genMultiEyes
+// (src/ooc/ooc_tracer.inl:84-172) with Camera::generateRay
+// (src/render/camera.h:173-209): u = x / W, v = y / H, jitter drawn from a
+// sampler seeded with the tile-local sample id when pixel_samples > 1.
+__global__ void kGenPrimary(CameraDev cam, const TileDev* __restrict__ tiles, int ntiles,
+                            int64_t nsamples, int spp, int image_w, RayBuf rays,
+                            uint32_t* alive_list, uint32_t* alive_count, int32_t* alive_idx,
+                            Counters* ctr) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    *alive_count = (uint32_t)nsamples;
+    atomicAdd(&ctr->rays_primary, (unsigned long long)nsamples);
+  }
+  if (i >= nsamples) return;
+  int k = 0;
+  while (k + 1 < ntiles && tiles[k + 1].sample_base <= i) ++k;
+  const TileDev tl = tiles[k];
+  int32_t bufid = (int32_t)(i - tl.sample_base);
+  int32_t lp = spp > 1 ? bufid / spp : bufid;
+  int x = tl.x + lp % tl.w;
+  int y = tl.y + lp / tl.w;
+  float fx = (float)x, fy = (float)y;
+  if (spp > 1) {
+    uint32_t st = rngSeed(bufid);
+    fx = (float)x + rngNext(st);
+    fy = (float)y + rngNext(st);
+  }
+  float u = fx / cam.image_w;
+  float v = fy / cam.image_h;
+  V3 ll = v3(cam.ll[0], cam.ll[1], cam.ll[2]);
+  V3 wv = v3(cam.wv[0], cam.wv[1], cam.wv[2]);
+  V3 hv = v3(cam.hv[0], cam.hv[1], cam.hv[2]);
+  V3 pos = v3(cam.pos[0], cam.pos[1], cam.pos[2]);
+  V3 d = normalize(((ll + u * wv) + v * hv) - pos);
+  rays.org[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
+  rays.dir[i] = make_float4(d.x, d.y, d.z, 0.f);
+  rays.wgt[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+  rays.pixid[i] = y * image_w + x;
+  rays.samid[i] = bufid;
+  alive_list[i] = (uint32_t)i;
+  alive_idx[i] = (int32_t)i;
+}
+
+void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int ntiles,
+                      int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
+                      uint32_t* alive_count, int32_t* alive_idx, Counters* ctr) {
+  int threads = 256;
+  int64_t blocks = (nsamples + threads - 1) / threads;
+  if (blocks < 1) blocks = 1;
+  kGenPrimary<<<(unsigned)blocks, threads, 0, s>>>(cam, tiles, ntiles, nsamples, spp, image_w, rays,
+                                                   alive_list, alive_count, alive_idx, ctr);
+}
+
+// ---------------------------------------------------------------- schedule
+// Pass 1: per ray, the slab test against every domain AABB with t0 = 1e-3 and
+// t1 = the ray's end (infinity for every ray of the reference), sorted by
+// (t, id) (src/render/rays.h:71-79).  Shadow rays start with the domain that
+// spawned them, then list the other domains with their index in the full
+// sorted list as depth (ooc_isector.h:147-174).  Lists go to an arena, the
+// per-(key, warp) histogram to global memory.
+__global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
+                                                             const DomainDev* __restrict__ doms,
+                                                             int D, int nkeys, int nwarps) {
+  extern __shared__ uint32_t smem[];
+  float* sbox = reinterpret_cast<float*>(smem);
+  uint32_t* hist = smem + 6 * D;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      sbox[6 * d + c] = doms[d].bmin[c];
+      sbox[6 * d + 3 + c] = doms[d].bmax[c];
+    }
+  }
+  uint32_t* h = hist + (size_t)wib * nkeys;
+  for (int k = lane; k < nkeys; k += 32) h[k] = 0;
+  __syncthreads();
+  const uint32_t n = *a.count;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+  const uint64_t per = ((uint64_t)n + nwarps - 1) / nwarps;
+  const uint64_t r0 = min((uint64_t)n, (uint64_t)gw * per);
+  const uint64_t r1 = min((uint64_t)n, r0 + per);
+  for (uint64_t base = r0; base < r1; base += 32) {
+    const uint64_t i = base + lane;
+    const bool active = i < r1;
+    float lt[kMaxList];
+    uint32_t ld[kMaxList];
+    int cnt = 0;
+    int origin = -1;
+    bool origin_in_list = false;
+    float origin_t = 0.f;
+    if (active) {
+      uint32_t rid = a.list[i];
+      V3 org, dir;
+      float t1 = INFINITY;
+      if (!a.shadow) {
+        float4 o = a.rays.org[rid], d4 = a.rays.dir[rid];
+        org = v3(o.x, o.y, o.z);
+        dir = v3(d4.x, d4.y, d4.z);
+        a.ray_key[rid] = kNoHit;
+      } else {
+        float4 hp = a.sh.hitpos[rid / a.slots];
+        float4 d4 = a.sh.dir[rid];
+        org = v3(hp.x, hp.y, hp.z);
+        origin = __float_as_int(hp.w);
+        dir = v3(d4.x, d4.y, d4.z);
+        t1 = d4.w;
+        a.sh.occluded[rid] = 0;
+      }
+      V3 inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+      for (int d = 0; d < D; ++d) {
+        float t;
+        if (slabTest(&sbox[6 * d], &sbox[6 * d + 3], org, inv, kRayEpsilon, t1, &t)) {
+          if (cnt == kMaxList) {
+            atomicAdd(&a.ctr->list_overflows, 1ull);
+            if (lt[kMaxList - 1] <= t) continue;
+            --cnt;
+          }
+          int j = cnt;
+          while (j > 0 && lt[j - 1] > t) {
+            lt[j] = lt[j - 1];
+            ld[j] = ld[j - 1];
+            --j;
+          }
+          lt[j] = t;
+          ld[j] = (uint32_t)d;
+          ++cnt;
+        }
+      }
+      if (a.shadow) {
+        for (int j = 0; j < cnt; ++j)
+          if ((int)ld[j] == origin) {
+            origin_in_list = true;
+            origin_t = lt[j];
+          }
+      }
+    }
+    // entries this lane emits
+    uint32_t nemit = 0;
+    if (active) nemit = a.shadow ? (uint32_t)(cnt + 1 - (origin_in_list ? 1 : 0)) : (uint32_t)cnt;
+    uint32_t total;
+    uint32_t pos = warpExclusiveScan(nemit, &total);
+    unsigned long long wbase = 0;
+    if (lane == 0 && total) wbase = atomicAdd(a.arena_top, (unsigned long long)total);
+    wbase = __shfl_sync(0xffffffffu, wbase, 0);
+    bool fits = wbase + total <= a.arena_cap;
+    if (!fits && lane == 0 && total) atomicAdd(&a.ctr->arena_overflows, 1ull);
+    if (active) {
+      a.list_off[i] = (uint32_t)(wbase + pos);
+      a.list_cnt[i] = fits ? nemit : 0u;
+      if (fits) {
+        uint2* out = a.arena + wbase + pos;
+        int o = 0;
+        if (a.shadow) {
+          out[o++] = make_uint2((uint32_t)origin | (1u << 31), __float_as_uint(origin_t));
+          uint32_t key = (uint32_t)origin;
+          atomicAdd(&h[key], 1u);
+        }
+        for (int j = 0; j < cnt; ++j) {
+          uint32_t d = ld[j];
+          if (a.shadow && (int)d == origin) continue;
+          out[o++] = make_uint2(d | ((uint32_t)j << 16), __float_as_uint(lt[j]));
+          uint32_t key = a.order_by_depth ? (uint32_t)(min(j, kDepthBuckets - 1) * D) + d : d;
+          atomicAdd(&h[key], 1u);
+          if (j < a.list_size) atomicAdd((unsigned long long*)&a.dstats[(size_t)d * a.list_size + j], 1ull);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nwarps + gw] = h[k];
+}
+
+// Pass 2: exclusive scan of the (key-major) histogram in one block.
+__global__ void __launch_bounds__(1024) kScanHist(uint32_t* hist, int nkeys, int nwarps,
+                                                  uint32_t* key_start, uint32_t* num_entries,
+                                                  unsigned long long entry_cap, Counters* ctr) {
+  __shared__ uint32_t part[1024];
+  const uint64_t M = (uint64_t)nkeys * nwarps;
+  const uint64_t per = (M + blockDim.x - 1) / blockDim.x;
+  const uint64_t b0 = min(M, per * threadIdx.x), b1 = min(M, b0 + per);
+  uint32_t sum = 0;
+  for (uint64_t i = b0; i < b1; ++i) sum += hist[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - sum;
+  for (uint64_t i = b0; i < b1; ++i) {
+    uint32_t v = hist[i];
+    hist[i] = run;
+    if (i % nwarps == 0) key_start[i / nwarps] = run;
+    run += v;
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    uint32_t total = part[blockDim.x - 1];
+    key_start[nkeys] = total;
+    if (total > entry_cap) {
+      atomicAdd(&ctr->entry_overflows, 1ull);
+      total = 0;
+    }
+    *num_entries = total;
+  }
+}
+
+// Pass 3: stable scatter.  Each warp re-reads its rays in order, flattens
+// their entries into shared memory and ranks them per key with match_any, so
+// every domain's queue keeps ray order (the order a single-threaded
+// Isector::isectAll pushes them, ooc_isector.h:133-144).
+__global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nkeys, int nwarps) {
+  extern __shared__ uint32_t smem[];
+  const int wpb = blockDim.x >> 5;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t* running = smem + (size_t)wib * nkeys;
+  uint32_t* fkey = smem + (size_t)wpb * nkeys + (size_t)wib * (32 * kMaxEmit) * 3;
+  uint32_t* fw0 = fkey + 32 * kMaxEmit;
+  uint32_t* fw1 = fw0 + 32 * kMaxEmit;
+  const int gw = blockIdx.x * wpb + wib;
+  if (gw >= nwarps) return;
+  for (int k = lane; k < nkeys; k += 32) running[k] = a.hist[(size_t)k * nwarps + gw];
+  __syncwarp();
+  const uint32_t n = *a.count;
+  if (*a.num_entries == 0) return;
+  const uint64_t per = ((uint64_t)n + nwarps - 1) / nwarps;
+  const uint64_t r0 = min((uint64_t)n, (uint64_t)gw * per);
+  const uint64_t r1 = min((uint64_t)n, r0 + per);
+  const uint32_t lt = laneMaskLt();
+  for (uint64_t base = r0; base < r1; base += 32) {
+    const uint64_t i = base + lane;
+    uint32_t cnt = 0, off = 0, rid = 0;
+    if (i < r1) {
+      cnt = a.list_cnt[i];
+      off = a.list_off[i];
+      rid = a.list[i];
+    }
+    uint32_t total;
+    uint32_t pos = warpExclusiveScan(cnt, &total);
+    for (uint32_t j = 0; j < cnt; ++j) {
+      uint2 e = a.arena[off + j];
+      uint32_t d = e.x & 0xffffu;
+      uint32_t depth = (e.x >> 16) & 0x7fffu;
+      uint32_t origin = e.x >> 31;
+      uint32_t key = a.order_by_depth ? (uint32_t)(min((int)depth, kDepthBuckets - 1) * D) + d : d;
+      fkey[pos + j] = key;
+      fw0[pos + j] = (rid & kRayIdMask) | (min(depth, 31u) << kRayIdBits) | (origin << 31);
+      fw1[pos + j] = e.y;
+    }
+    __syncwarp();
+    for (uint32_t s = 0; s < total; s += 32) {
+      const uint32_t e = s + lane;
+      const bool valid = e < total;
+      const uint32_t key = valid ? fkey[e] : 0xffffffffu;
+      const uint32_t m = __match_any_sync(0xffffffffu, key);
+      uint32_t rank = 0;
+      if (valid) rank = running[key] + __popc(m & lt);
+      __syncwarp();
+      if (valid && (__ffs(m) - 1) == lane) running[key] += __popc(m);
+      __syncwarp();
+      if (valid && rank < a.entry_cap) a.entries[rank] = make_uint2(fw0[e], fw1[e]);
+    }
+    __syncwarp();
+  }
+}
+
+void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
+                    int nblocks, uint32_t* scan_tmp) {
+  (void)scan_tmp;
+  const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
+  size_t smem1 = (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
+  cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  kSchedLists<<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
+  kScanHist<<<1, 1024, 0, s>>>(a.hist, nkeys, nwarps, a.key_start, a.num_entries, a.entry_cap,
+                               a.ctr);
+  const int wpb = 4;
+  size_t smem3 = (size_t)wpb * nkeys * 4 + (size_t)wpb * 32 * kMaxEmit * 3 * 4;
+  cudaFuncSetAttribute(kSchedScatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
+  kSchedScatter<<<(nwarps + wpb - 1) / wpb, wpb * 32, smem3, s>>>(a, D, nkeys, nwarps);
+}
+
+// ---------------------------------------------------------------- compaction
+__global__ void kCompactCount(const uint8_t* __restrict__ flag, const uint32_t* n_dev,
+                              uint32_t n_mul, uint64_t n_host, uint32_t* block_tmp) {
+  __shared__ uint32_t ws[32];
+  const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
+  const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const uint64_t b0 = min(n, per * blockIdx.x), b1 = min(n, b0 + per);
+  uint32_t c = 0;
+  for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) c += flag[i] != 0;
+  for (int o = 16; o; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0u;
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) block_tmp[blockIdx.x] = v;
+  }
+}
+
+__global__ void __launch_bounds__(1024) kCompactScan(uint32_t* block_tmp, int nblocks,
+                                                     uint32_t* count) {
+  __shared__ uint32_t part[1024];
+  const int per = (nblocks + 1023) / 1024;
+  const int b0 = min(nblocks, per * (int)threadIdx.x), b1 = min(nblocks, b0 + per);
+  uint32_t sum = 0;
+  for (int i = b0; i < b1; ++i) sum += block_tmp[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - sum;
+  for (int i = b0; i < b1; ++i) {
+    uint32_t v = block_tmp[i];
+    block_tmp[i] = run;
+    run += v;
+  }
+  if (threadIdx.x == 1023) *count = part[1023];
+}
+
+__global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* n_dev,
+                              uint32_t n_mul, uint64_t n_host, const uint32_t* block_tmp,
+                              uint32_t* list, int32_t* index_of) {
+  __shared__ uint32_t ws[33];
+  const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
+  const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const uint64_t b0 = min(n, per * blockIdx.x), b1 = min(n, b0 + per);
+  uint32_t base = block_tmp[blockIdx.x];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t lt = laneMaskLt();
+  for (uint64_t s = b0; s < b1; s += blockDim.x) {
+    const uint64_t i = s + threadIdx.x;
+    const bool f = i < b1 && flag[i] != 0;
+    const uint32_t bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) ws[w] = __popc(bal);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t run = 0;
+      for (int k = 0; k < nw; ++k) {
+        uint32_t v = ws[k];
+        ws[k] = run;
+        run += v;
+      }
+      ws[32] = run;
+    }
+    __syncthreads();
+    if (i < b1) {
+      if (f) {
+        uint32_t p = base + ws[w] + __popc(bal & lt);
+        list[p] = (uint32_t)i;
+        if (index_of) index_of[i] = (int32_t)p;
+      } else if (index_of) {
+        index_of[i] = -1;
+      }
+    }
+    base += ws[32];
+    __syncthreads();
+  }
+}
+
+void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
+                   uint64_t n_host, uint32_t* list, uint32_t* count, int32_t* index_of,
+                   uint32_t* block_tmp, int nblocks) {
+  kCompactCount<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp);
+  kCompactScan<<<1, 1024, 0, s>>>(block_tmp, nblocks, count);
+  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp, list, index_of);
+}
+
+// ---------------------------------------------------------------- scores
+// DomainStats::schedule (src/ooc/ooc_domain_stats.cc:60-111):
+// score[d] = sum_k count[d][k] * (L - k), processed in descending score.  The
+// reference sorts with an unstable sort; ties are ordered by domain id here.
+__global__ void kScores(const long long* __restrict__ dstats, int D, int L, long long* scores,
+                        int32_t* order) {
+  extern __shared__ long long sc[];
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    long long v = 0;
+    for (int k = 0; k < L; ++k) v += dstats[(size_t)d * L + k] * (long long)(L - k);
+    sc[d] = v;
+    scores[d] = v;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    long long v = sc[d];
+    int rank = 0;
+    for (int e = 0; e < D; ++e) rank += (sc[e] > v) || (sc[e] == v && e < d);
+    order[rank] = d;
+  }
+}
+
+void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int list_size,
+                  long long* scores, int32_t* order) {
+  kScores<<<1, 1024, (size_t)ndomains * sizeof(long long), s>>>(dstats, ndomains, list_size, scores,
+                                                               order);
+}
+
+}  // namespace spray

@@ -1,0 +1,318 @@
+// Closest-hit and occlusion traversal of per-domain queues, and closest-hit
+// resolution across the domains a ray visited.
+//
+// Replaces Scene::intersect / Scene::occluded (src/render/scene.inl:189-209),
+// which SpRay calls once per (ray, domain) queue entry with tnear = 1e-3 and
+// tfar = infinity.  Here persistent warps pull 32 entries at a time from the
+// domain-partitioned queue; each thread walks the entry's domain BVH (4-wide
+// nodes, conservative box test) and tests triangles with the watertight test.
+// A closest hit is folded into the ray's packed (t | triangle) key with a
+// 64-bit atomicMin, so the winner does not depend on the order in which the
+// domains were visited.
+#include "kernels.cuh"
+#include "spray_math.cuh"
+
+namespace spray {
+
+namespace {
+
+// Box test slack: (1 + 2*gamma(3)) rounded up (Ize, "Robust BVH Ray
+// Traversal", JCGT 2(2), 2013), so rounding never culls a box the ray touches.
+constexpr float kBoxSlack = 1.0000004f;
+constexpr int kStack = 64;
+
+struct TravRay {
+  V3 org, dir, inv;
+  RayShear sh;
+};
+
+__device__ __forceinline__ TravRay makeTravRay(V3 org, V3 dir) {
+  TravRay r;
+  r.org = org;
+  r.dir = dir;
+  r.inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+  r.sh = makeShear(dir);
+  return r;
+}
+
+// Intersects the four children of a node; returns a mask of hit children and
+// their entry distances.
+__device__ __forceinline__ int testChildren(const BvhNode4* __restrict__ nodes, int node,
+                                            const TravRay& r, float tnear, float tfar,
+                                            float tn[4]) {
+  const float4* p = reinterpret_cast<const float4*>(nodes + node);
+  float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
+  float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
+  const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
+  const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
+  const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+  int mask = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float tx0 = (lx[c] - r.org.x) * r.inv.x, tx1 = (hx[c] - r.org.x) * r.inv.x;
+    float ty0 = (ly[c] - r.org.y) * r.inv.y, ty1 = (hy[c] - r.org.y) * r.inv.y;
+    float tz0 = (lz[c] - r.org.z) * r.inv.z, tz1 = (hz[c] - r.org.z) * r.inv.z;
+    float a0 = fminf(tx0, tx1), a1 = fmaxf(tx0, tx1);
+    float b0 = fminf(ty0, ty1), b1 = fmaxf(ty0, ty1);
+    float c0 = fminf(tz0, tz1), c1 = fmaxf(tz0, tz1);
+    float t0 = fmaxf(fmaxf(a0, b0), fmaxf(c0, tnear));
+    float t1 = fminf(fminf(a1, b1), fminf(c1, tfar)) * kBoxSlack;
+    tn[c] = t0;
+    if (t0 <= t1) mask |= 1 << c;
+  }
+  return mask;
+}
+
+__device__ __forceinline__ int4 loadChildren(const BvhNode4* __restrict__ nodes, int node) {
+  const int4* p = reinterpret_cast<const int4*>(nodes + node);
+  return __ldg(p + 6);
+}
+
+__device__ __forceinline__ int childAt(int4 c, int k) {
+  return k == 0 ? c.x : (k == 1 ? c.y : (k == 2 ? c.z : c.w));
+}
+
+// Closest hit in one domain.  best_key enters as the key to beat and leaves as
+// the best found; returns true when this domain improved it.
+__device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const TravRay& r,
+                                uint64_t& best_key, float& best_t, uint32_t& best_prim,
+                                float& best_u, float& best_v) {
+  const BvhNode4* nodes = sc.nodes + dom.node_base;
+  const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
+  uint2 stack[kStack];
+  int sp = 0;
+  int node = 0;
+  bool found = false;
+  while (true) {
+    float tn[4];
+    int mask = testChildren(nodes, node, r, kRayEpsilon, best_t, tn);
+    int4 ch = loadChildren(nodes, node);
+    // order hit children near to far
+    int ord[4], no = 0;
+    for (int c = 0; c < 4; ++c)
+      if (mask & (1 << c)) {
+        int j = no++;
+        while (j > 0 && tn[ord[j - 1]] > tn[c]) {
+          ord[j] = ord[j - 1];
+          --j;
+        }
+        ord[j] = c;
+      }
+    // leaves now, inner children onto the stack far to near
+    for (int k = 0; k < no; ++k) {
+      int c = ord[k];
+      int ref = childAt(ch, c);
+      if (ref < 0) {
+        if (tn[c] > best_t) continue;
+        uint32_t v = ~(uint32_t)ref;
+        uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+        for (uint32_t q = 0; q < cnt; ++q) {
+          const float4* tp = tris + 3 * (size_t)(first + q);
+          float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+          float t, u, vv;
+          if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z),
+                                v3(cc.x, cc.y, cc.z), kRayEpsilon, __int_as_float(0x7f800000),
+                                &t, &u, &vv)) {
+            uint32_t prim = __float_as_uint(a.w);
+            uint64_t key = packHitKey(t, dom.gprim_base + prim);
+            if (key < best_key) {
+              best_key = key;
+              best_t = t;
+              best_prim = prim;
+              best_u = u;
+              best_v = vv;
+              found = true;
+            }
+          }
+        }
+      }
+    }
+    for (int k = no - 1; k >= 0; --k) {
+      int c = ord[k];
+      int ref = childAt(ch, c);
+      if (ref >= 0 && sp < kStack) stack[sp++] = make_uint2((uint32_t)ref, __float_as_uint(tn[c]));
+    }
+    // pop the nearest pending node still in front of the best hit
+    bool next = false;
+    while (sp > 0) {
+      uint2 e = stack[--sp];
+      if (__uint_as_float(e.y) <= best_t) {
+        node = (int)e.x;
+        next = true;
+        break;
+      }
+    }
+    if (!next) break;
+  }
+  return found;
+}
+
+// Any hit in (tnear, tfar) in one domain.
+__device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar) {
+  const BvhNode4* nodes = sc.nodes + dom.node_base;
+  const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
+  int stack[kStack];
+  int sp = 0;
+  int node = 0;
+  while (true) {
+    float tn[4];
+    int mask = testChildren(nodes, node, r, kRayEpsilon, tfar, tn);
+    int4 ch = loadChildren(nodes, node);
+    for (int c = 0; c < 4; ++c) {
+      if (!(mask & (1 << c))) continue;
+      int ref = childAt(ch, c);
+      if (ref < 0) {
+        uint32_t v = ~(uint32_t)ref;
+        uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+        for (uint32_t q = 0; q < cnt; ++q) {
+          const float4* tp = tris + 3 * (size_t)(first + q);
+          float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+          float t, u, vv;
+          if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z),
+                                v3(cc.x, cc.y, cc.z), kRayEpsilon, tfar, &t, &u, &vv))
+            return true;
+        }
+      } else if (sp < kStack) {
+        stack[sp++] = ref;
+      }
+    }
+    if (sp == 0) return false;
+    node = stack[--sp];
+  }
+}
+
+__device__ __forceinline__ int findKey(const uint32_t* ks, int nkeys, uint32_t e) {
+  // last key with ks[key] <= e (segments may be empty)
+  int lo = 0, hi = nkeys - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (ks[mid] <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
+  extern __shared__ uint32_t skeys[];
+  const int D = a.scene.num_domains;
+  for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
+  __syncthreads();
+  const uint32_t E = *a.num_entries;
+  const int lane = threadIdx.x & 31;
+  unsigned long long visits = 0, culled = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(a.work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= E) break;
+    const uint32_t e = base + lane;
+    if (e >= E) continue;
+    const uint2 ent = a.entries[e];
+    const uint32_t ray = ent.x & kRayIdMask;
+    const float tdom = __uint_as_float(ent.y);
+    const int d = findKey(skeys, a.nkeys, e) % D;
+    const DomainDev dom = a.scene.domains[d];
+    uint64_t best_key = kNoHit;
+    float best_t = __int_as_float(0x7f800000);
+    if (a.cull) {
+      uint64_t cur = *((volatile uint64_t*)&a.ray_key[ray]);
+      if (cur != kNoHit) {
+        best_key = cur;
+        best_t = hitKeyT(cur);
+        if (tdom > best_t) {
+          a.rec_key[e] = kNoHit;
+          ++culled;
+          continue;
+        }
+      }
+    }
+    ++visits;
+    const float4 o = a.rays.org[ray], dd = a.rays.dir[ray];
+    TravRay r = makeTravRay(v3(o.x, o.y, o.z), v3(dd.x, dd.y, dd.z));
+    uint32_t prim = 0;
+    float u = 0.f, v = 0.f;
+    if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v)) {
+      atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
+      const uint32_t* f = a.scene.faces + 3 * ((size_t)dom.face_base + prim);
+      uint32_t i0 = dom.vert_base + f[0], i1 = dom.vert_base + f[1], i2 = dom.vert_base + f[2];
+      uint32_t col = interpolateColor(a.scene.colors[i0], a.scene.colors[i1], a.scene.colors[i2], u, v);
+      const float* nb = a.scene.normals;
+      V3 ns = interpolateNormal(v3(nb[3 * (size_t)i0], nb[3 * (size_t)i0 + 1], nb[3 * (size_t)i0 + 2]),
+                                v3(nb[3 * (size_t)i1], nb[3 * (size_t)i1 + 1], nb[3 * (size_t)i1 + 2]),
+                                v3(nb[3 * (size_t)i2], nb[3 * (size_t)i2 + 1], nb[3 * (size_t)i2 + 2]),
+                                u, v);
+      a.rec_key[e] = best_key;
+      a.rec_attr[e] = make_float4(ns.x, ns.y, ns.z, __uint_as_float(col));
+    } else {
+      a.rec_key[e] = kNoHit;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    visits += __shfl_down_sync(0xffffffffu, visits, o);
+    culled += __shfl_down_sync(0xffffffffu, culled, o);
+  }
+  if (lane == 0) {
+    if (visits) atomicAdd(&a.ctr->visits_radiance, visits);
+    if (culled) atomicAdd(&a.ctr->visits_culled, culled);
+  }
+}
+
+void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks) {
+  size_t smem = (size_t)(a.nkeys + 1) * 4;
+  kTraceClosest<<<nblocks, 256, smem, s>>>(a);
+}
+
+// The entry that holds a ray's final key publishes its colour and normal.
+__global__ void kResolve(TraceArgs a, float4* hit_ns) {
+  const uint32_t E = *a.num_entries;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t k = a.rec_key[e];
+    if (k == kNoHit) continue;
+    uint32_t ray = a.entries[e].x & kRayIdMask;
+    if (a.ray_key[ray] == k) hit_ns[ray] = a.rec_attr[e];
+  }
+}
+
+void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks) {
+  kResolve<<<nblocks, 256, 0, s>>>(a, hit_ns);
+}
+
+__global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
+  extern __shared__ uint32_t skeys[];
+  const int D = a.scene.num_domains;
+  for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
+  __syncthreads();
+  const uint32_t E = *a.num_entries;
+  const int lane = threadIdx.x & 31;
+  unsigned long long visits = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(a.work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= E) break;
+    const uint32_t e = base + lane;
+    if (e >= E) continue;
+    const uint2 ent = a.entries[e];
+    const uint32_t ray = ent.x & kRayIdMask;
+    if (*((volatile uint8_t*)&a.sh.occluded[ray])) continue;
+    const int d = findKey(skeys, a.nkeys, e) % D;
+    const DomainDev dom = a.scene.domains[d];
+    ++visits;
+    const float4 hp = a.sh.hitpos[ray / a.slots];
+    const float4 dd = a.sh.dir[ray];
+    TravRay r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
+    if (traverseAny(a.scene, dom, r, dd.w)) a.sh.occluded[ray] = 1;
+  }
+  for (int o = 16; o; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
+  if (lane == 0 && visits) atomicAdd(&a.ctr->visits_shadow, visits);
+}
+
+void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {
+  size_t smem = (size_t)(a.nkeys + 1) * 4;
+  kTraceOccluded<<<nblocks, 256, smem, s>>>(a);
+}
+
+}  // namespace spray

@@ -1,0 +1,953 @@
+// Host side of the GPU tracer: scene upload, blocking tiles, wavefront
+// orchestration on one CUDA stream, and the C ABI declared in spray_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/spray_gpu.h"
+#include "bvh.h"
+#include "kernels.cuh"
+#include "spray_math.cuh"
+#include "tracer_internal.h"
+
+namespace spray {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define CK(x)                                                                               \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_) + " at " + __FILE__ + \
+                      ":" + std::to_string(__LINE__));                                      \
+  } while (0)
+
+template <class T>
+static void devAlloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  CK(cudaMalloc((void**)p, n * sizeof(T)));
+}
+template <class T>
+static void devFree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// ---------------------------------------------------------------- tiles
+// ImageScheduleTileList::init (src/render/tile.cc:317-391) on the vertical
+// stripe of this rank (makeVerticalStripe, tile.cc:214-235).
+std::vector<HostTile> makeTiles(int W, int H, int spp, int num_ranks, int rank,
+                                int64_t max_samples) {
+  std::vector<HostTile> tiles;
+  int sw = std::max(W / num_ranks, 1);
+  int sx = rank * sw;
+  if (sx >= W) return tiles;
+  int w = ((sx + sw > W) || (rank == num_ranks - 1)) ? W - sx : sw;
+  int h = H;
+  int64_t num_samples = (int64_t)w * h * spp;
+  int64_t est = (num_samples + max_samples - 1) / max_samples;
+  if (est < 1) est = 1;
+  int tile_h = h / (int)est;
+  if (tile_h < 1) throw std::invalid_argument("max_samples_per_rank smaller than one image row");
+  for (int y = 0; y < h; y += tile_h) {
+    HostTile t;
+    t.x = sx;
+    t.y = y;
+    t.w = w;
+    t.h = std::min(tile_h, h - y);
+    tiles.push_back(t);
+  }
+  return tiles;
+}
+
+// ---------------------------------------------------------------- normals
+// TriMeshBuffer::computeNormals (src/render/trimesh_buffer.cc:267-326):
+// unnormalised sum of face cross products, faces in file order.
+void computeVertexNormals(const float* v, int64_t nv, const uint32_t* f, int64_t nf, float* n) {
+  for (int64_t i = 0; i < 3 * nv; ++i) n[i] = 0.0f;
+  for (int64_t i = 0; i < nf; ++i) {
+    size_t a = 3 * (size_t)f[3 * i], b = 3 * (size_t)f[3 * i + 1], c = 3 * (size_t)f[3 * i + 2];
+    float ux = v[b] - v[a], uy = v[b + 1] - v[a + 1], uz = v[b + 2] - v[a + 2];
+    float vx = v[c] - v[a], vy = v[c + 1] - v[a + 1], vz = v[c + 2] - v[a + 2];
+    float nx = uy * vz - uz * vy;
+    float ny = uz * vx - ux * vz;
+    float nz = ux * vy - uy * vx;
+    for (size_t k : {a, b, c}) {
+      n[k] += nx;
+      n[k + 1] += ny;
+      n[k + 2] += nz;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- camera
+// Camera::init (src/render/camera.h:128-166).
+CameraDev makeCamera(const float p[3], const float l[3], const float up[3], float vfov, int W, int H) {
+  CameraDev c;
+  float aspect = (float)W / (float)H;
+  float theta = vfov * M_PI / 180.0f;
+  float half_h = std::tan(theta / 2.0f);
+  float half_w = aspect * half_h;
+  V3 campos = v3(p[0], p[1], p[2]), lookat = v3(l[0], l[1], l[2]), upv = v3(up[0], up[1], up[2]);
+  V3 w = campos - lookat;
+  V3 u = cross(upv, w);
+  V3 v = cross(w, u);
+  w = normalize(w);
+  u = normalize(u);
+  v = normalize(v);
+  V3 center = campos - w;
+  V3 ll = (center - (half_w * u)) - (half_h * v);
+  V3 wv = (2.0f * half_w) * u;
+  V3 hv = (2.0f * half_h) * v;
+  float* dst[4] = {c.pos, c.ll, c.wv, c.hv};
+  V3 src[4] = {campos, ll, wv, hv};
+  for (int k = 0; k < 4; ++k) {
+    dst[k][0] = src[k].x;
+    dst[k][1] = src[k].y;
+    dst[k][2] = src[k].z;
+  }
+  c.image_w = (float)W;
+  c.image_h = (float)H;
+  return c;
+}
+
+// ---------------------------------------------------------------- tracer
+Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
+  if (cfg.image_w <= 0 || cfg.image_h <= 0) throw std::invalid_argument("image size must be positive");
+  if (cfg.pixel_samples <= 0) throw std::invalid_argument("pixel_samples must be positive");
+  if (cfg.bounces <= 0) throw std::invalid_argument("bounces must be positive");
+  if (cfg.ao_samples <= 0) throw std::invalid_argument("ao_samples must be positive");
+  if (cfg.list_size <= 0 || cfg.list_size > kMaxList)
+    throw std::invalid_argument("list_size must be in [1, 32]");
+  if (cfg.max_samples_per_rank <= 0) throw std::invalid_argument("max_samples_per_rank must be positive");
+  if (cfg.num_ranks <= 0 || cfg.rank < 0 || cfg.rank >= cfg.num_ranks)
+    throw std::invalid_argument("rank must be in [0, num_ranks)");
+  int ndev = 0;
+  CK(cudaGetDeviceCount(&ndev));
+  if (cfg.device < 0 || cfg.device >= ndev) throw CudaError("no CUDA device " + std::to_string(cfg.device));
+  CK(cudaSetDevice(cfg.device));
+  CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, cfg.device));
+  CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ev_start));
+  CK(cudaEventCreate(&ev_stop));
+  devAlloc(&d_ctr, 1);
+}
+
+Tracer::~Tracer() {
+  cudaSetDevice(cfg.device);
+  freeScene();
+  freeBuffers();
+  devFree(d_ctr);
+  for (auto& e : ev_pool) cudaEventDestroy(e);
+  if (ev_start) cudaEventDestroy(ev_start);
+  if (ev_stop) cudaEventDestroy(ev_stop);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void Tracer::freeScene() {
+  devFree(d_domains);
+  devFree(d_nodes);
+  devFree(d_tris);
+  devFree(d_faces);
+  devFree(d_colors);
+  devFree(d_normals);
+  devFree(d_lights);
+}
+
+void Tracer::freeBuffers() {
+  for (int k = 0; k < 2; ++k) {
+    devFree(rays[k].org);
+    devFree(rays[k].dir);
+    devFree(rays[k].wgt);
+  }
+  devFree(d_pixid);
+  devFree(d_samid);
+  devFree(d_alive_list);
+  devFree(d_alive_idx);
+  devFree(d_alive_count);
+  devFree(d_next_flag);
+  devFree(d_ray_key);
+  devFree(d_hit_ns);
+  devFree(sh.dir);
+  devFree(sh.wgt);
+  devFree(sh.hitpos);
+  devFree(sh.occluded);
+  devFree(d_shadow_flag);
+  devFree(d_shadow_list);
+  devFree(d_shadow_count);
+  devFree(d_arena);
+  devFree(d_arena_top);
+  devFree(d_list_off);
+  devFree(d_list_cnt);
+  devFree(d_hist);
+  devFree(d_dstats);
+  devFree(d_entries);
+  devFree(d_key_start);
+  devFree(d_num_entries);
+  devFree(d_rec_key);
+  devFree(d_rec_attr);
+  devFree(d_work);
+  devFree(d_block_tmp);
+  devFree(d_image);
+  devFree(d_scores);
+  devFree(d_order);
+  devFree(d_tiles);
+  cap_samples = 0;
+}
+
+int Tracer::slots() const {
+  if (cfg.ao_mode) return cfg.ao_samples + (cfg.ao_light_shadow ? 1 : 0);
+  int s = 0;
+  for (const auto& l : lights) s += (l.type == 0) ? 1 : cfg.ao_samples;
+  return s;
+}
+
+void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_light* ls, int nl) {
+  if (nd <= 0) throw std::invalid_argument("scene needs at least one domain");
+  if (nd > 65535) throw std::invalid_argument("at most 65535 domains");
+  if (!cfg.ao_mode && nl <= 0) throw std::invalid_argument("path tracing needs at least one light");
+  if (cfg.cache_size >= 0 && cfg.cache_size < nd)
+    throw std::invalid_argument("out-of-core cache (cache_size < number of domains) is not supported yet");
+  CK(cudaSetDevice(cfg.device));
+  freeScene();
+  D = nd;
+  lights.assign(ls, ls + nl);
+  if (slots() > kMaxSlots) throw std::invalid_argument("too many shadow rays per hit (max 64)");
+  std::vector<DomainPack> packs(nd);
+  std::vector<std::string> errors(nd);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int d = 0; d < nd; ++d) {
+    try {
+      const spray_gpu_domain& src = doms[d];
+      if (src.num_faces <= 0 || src.num_vertices <= 0 || !src.vertices || !src.faces)
+        throw std::invalid_argument("domain " + std::to_string(d) + " has no geometry");
+      if (src.num_faces >= (1ll << 28)) throw std::invalid_argument("domain too large");
+      for (int64_t i = 0; i < 3 * src.num_faces; ++i)
+        if ((int64_t)src.faces[i] >= src.num_vertices)
+          throw std::invalid_argument("domain " + std::to_string(d) + ": face index out of range");
+      DomainPack& p = packs[d];
+      p.nv = src.num_vertices;
+      p.nf = src.num_faces;
+      p.normals.resize(3 * (size_t)p.nv);
+      computeVertexNormals(src.vertices, p.nv, src.faces, p.nf, p.normals.data());
+      BvhBuildResult bvh;
+      buildBvh4(src.vertices, src.faces, (uint32_t)p.nf, &bvh);
+      p.nodes = std::move(bvh.nodes);
+      p.bvh_depth = bvh.depth;
+      p.tris.resize(3 * (size_t)p.nf);
+      for (size_t k = 0; k < bvh.tri_order.size(); ++k) {
+        uint32_t prim = bvh.tri_order[k];
+        const uint32_t* fi = src.faces + 3 * (size_t)prim;
+        for (int c = 0; c < 3; ++c) {
+          const float* vp = src.vertices + 3 * (size_t)fi[c];
+          float w = 0.f;
+          if (c == 0) std::memcpy(&w, &prim, 4);
+          p.tris[3 * k + c] = make_float4(vp[0], vp[1], vp[2], w);
+        }
+      }
+      p.faces.assign(src.faces, src.faces + 3 * p.nf);
+      if (src.colors) p.colors.assign(src.colors, src.colors + p.nv);
+      else p.colors.assign(p.nv, 0u);
+    } catch (const std::exception& e) {
+      errors[d] = e.what();
+    }
+  }
+  for (int d = 0; d < nd; ++d)
+    if (!errors[d].empty()) throw std::invalid_argument(errors[d]);
+  // concatenate in domain order
+  hdoms.assign(nd, DomainDev{});
+  size_t nn = 0, nt = 0, nvv = 0;
+  uint64_t gp = 0;
+  max_bvh_depth = 0;
+  for (int d = 0; d < nd; ++d) {
+    DomainDev& dd = hdoms[d];
+    for (int c = 0; c < 3; ++c) {
+      dd.bmin[c] = doms[d].world_bounds[c];
+      dd.bmax[c] = doms[d].world_bounds[3 + c];
+    }
+    dd.node_base = (int32_t)nn;
+    dd.tri_base = (int32_t)nt;
+    dd.gprim_base = (uint32_t)gp;
+    dd.vert_base = (int32_t)nvv;
+    dd.face_base = (int32_t)nt;
+    dd.bsdf = doms[d].bsdf_type;
+    for (int c = 0; c < 3; ++c) dd.bsdf_p[c] = doms[d].bsdf_params[c];
+    dd.resident = 1;
+    nn += packs[d].nodes.size();
+    nt += (size_t)packs[d].nf;
+    nvv += (size_t)packs[d].nv;
+    gp += (uint64_t)packs[d].nf;
+    max_bvh_depth = std::max(max_bvh_depth, packs[d].bvh_depth);
+    if (gp >= 0xffffffffull || nt >= (1ull << 31) || nn >= (1ull << 31))
+      throw std::invalid_argument("scene too large for 32-bit triangle numbering");
+  }
+  if (max_bvh_depth * 3 + 4 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
+  total_tris = nt;
+  devAlloc(&d_domains, nd);
+  devAlloc(&d_nodes, nn);
+  devAlloc(&d_tris, 3 * nt);
+  devAlloc(&d_faces, 3 * nt);
+  devAlloc(&d_colors, nvv);
+  devAlloc(&d_normals, 3 * nvv);
+  for (int d = 0; d < nd; ++d) {
+    const DomainPack& p = packs[d];
+    const DomainDev& dd = hdoms[d];
+    CK(cudaMemcpy(d_nodes + dd.node_base, p.nodes.data(), p.nodes.size() * sizeof(BvhNode4),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_tris + 3 * (size_t)dd.tri_base, p.tris.data(), p.tris.size() * sizeof(float4),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_faces + 3 * (size_t)dd.face_base, p.faces.data(), p.faces.size() * 4,
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_colors + dd.vert_base, p.colors.data(), p.colors.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_normals + 3 * (size_t)dd.vert_base, p.normals.data(), p.normals.size() * 4,
+                  cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(d_domains, hdoms.data(), nd * sizeof(DomainDev), cudaMemcpyHostToDevice));
+  std::vector<float> lf(13 * std::max(nl, 1), 0.f);
+  for (int l = 0; l < nl; ++l) {
+    float* q = &lf[13 * l];
+    q[0] = (float)ls[l].type;
+    for (int c = 0; c < 3; ++c) {
+      q[1 + c] = ls[l].position[c];
+      q[4 + c] = ls[l].radiance[c];
+      q[7 + c] = ls[l].edge1[c];
+      q[10 + c] = ls[l].edge2[c];
+    }
+  }
+  devAlloc(&d_lights, lf.size());
+  CK(cudaMemcpy(d_lights, lf.data(), lf.size() * 4, cudaMemcpyHostToDevice));
+  freeBuffers();  // sizes depend on the domain count and slots
+  has_scene = true;
+}
+
+void Tracer::setCamera(const float p[3], const float l[3], const float up[3], float vfov) {
+  cam = makeCamera(p, l, up, vfov, cfg.image_w, cfg.image_h);
+  has_camera = true;
+}
+
+void Tracer::planWaves() {
+  tiles = makeTiles(cfg.image_w, cfg.image_h, cfg.pixel_samples, cfg.num_ranks, cfg.rank,
+                    cfg.max_samples_per_rank);
+  const int S = std::max(slots(), 1);
+  int64_t cap = cfg.wave_samples > 0 ? cfg.wave_samples : (int64_t)16 << 20;
+  cap = std::min<int64_t>(cap, ((int64_t)1 << kRayIdBits) / S - 1);
+  waves.clear();
+  size_t k = 0;
+  while (k < tiles.size()) {
+    Wave w;
+    w.first_tile = (int)k;
+    w.num_tiles = 0;
+    w.samples = 0;
+    while (k < tiles.size()) {
+      int64_t ts = (int64_t)tiles[k].w * tiles[k].h * cfg.pixel_samples;
+      if (w.num_tiles > 0 && w.samples + ts > cap) break;
+      if (ts >= ((int64_t)1 << kRayIdBits) / S)
+        throw std::invalid_argument("a blocking tile holds more rays than one wavefront can address");
+      w.samples += ts;
+      ++w.num_tiles;
+      ++k;
+    }
+    waves.push_back(w);
+  }
+}
+
+void Tracer::ensureBuffers(int64_t nsamples) {
+  const int S = std::max(slots(), 1);
+  const int nkeys = kDepthBuckets * D;
+  sched_blocks = num_sms * 2;
+  sched_warps = sched_blocks * (kSchedThreads / 32);
+  if (nsamples <= cap_samples && cap_entries >= needed_entries) return;
+  freeBuffers();
+  int64_t N = std::max<int64_t>(nsamples, 1024);
+  int64_t NS = N * S;
+  if (needed_entries == 0) needed_entries = (uint64_t)std::max<int64_t>(4 * N, 2 * NS);
+  uint64_t E = needed_entries;
+  for (int k = 0; k < 2; ++k) {
+    devAlloc(&rays[k].org, N);
+    devAlloc(&rays[k].dir, N);
+    devAlloc(&rays[k].wgt, N);
+  }
+  devAlloc(&d_pixid, N);
+  devAlloc(&d_samid, N);
+  for (int k = 0; k < 2; ++k) {
+    rays[k].pixid = d_pixid;
+    rays[k].samid = d_samid;
+  }
+  devAlloc(&d_alive_list, N);
+  devAlloc(&d_alive_idx, N);
+  devAlloc(&d_alive_count, 1);
+  devAlloc(&d_next_flag, N);
+  devAlloc(&d_ray_key, N);
+  devAlloc(&d_hit_ns, N);
+  devAlloc(&sh.dir, NS);
+  devAlloc(&sh.wgt, NS);
+  devAlloc(&sh.hitpos, N);
+  devAlloc(&sh.occluded, NS);
+  devAlloc(&d_shadow_flag, NS);
+  devAlloc(&d_shadow_list, NS);
+  devAlloc(&d_shadow_count, 1);
+  devAlloc(&d_arena, E);
+  devAlloc(&d_arena_top, 1);
+  devAlloc(&d_list_off, NS);
+  devAlloc(&d_list_cnt, NS);
+  devAlloc(&d_hist, (size_t)nkeys * sched_warps);
+  devAlloc(&d_dstats, (size_t)D * cfg.list_size);
+  devAlloc(&d_entries, E);
+  devAlloc(&d_key_start, nkeys + 1);
+  devAlloc(&d_num_entries, 1);
+  devAlloc(&d_rec_key, E);
+  devAlloc(&d_rec_attr, E);
+  devAlloc(&d_work, 1);
+  compact_blocks = num_sms * 4;
+  devAlloc(&d_block_tmp, compact_blocks);
+  devAlloc(&d_image, (size_t)cfg.image_w * cfg.image_h);
+  devAlloc(&d_scores, D);
+  devAlloc(&d_order, D);
+  devAlloc(&d_tiles, tiles.size() + 1);
+  cap_samples = N;
+  cap_entries = E;
+}
+
+void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S) {
+  SchedArgs a{};
+  a.shadow = shadow;
+  a.count = count;
+  a.list = list;
+  a.rays = rays[cur];
+  a.sh = sh;
+  a.slots = S;
+  a.order_by_depth = order_by_depth;
+  a.list_size = cfg.list_size;
+  a.ray_key = d_ray_key;
+  a.arena = d_arena;
+  a.arena_top = d_arena_top;
+  a.arena_cap = cap_entries;
+  a.list_off = d_list_off;
+  a.list_cnt = d_list_cnt;
+  a.hist = d_hist;
+  a.dstats = d_dstats;
+  a.entries = d_entries;
+  a.entry_cap = cap_entries;
+  a.key_start = d_key_start;
+  a.num_entries = d_num_entries;
+  a.ctr = d_ctr;
+  CK(cudaMemsetAsync(d_arena_top, 0, sizeof(unsigned long long), stream));
+  launches += 1;
+  launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, nullptr);
+  launches += 3;
+}
+
+TraceArgs Tracer::traceArgs(int order_by_depth, int S) {
+  TraceArgs t{};
+  t.scene = sceneDev();
+  t.entries = d_entries;
+  t.num_entries = d_num_entries;
+  t.key_start = d_key_start;
+  t.nkeys = order_by_depth ? kDepthBuckets * D : D;
+  t.work = d_work;
+  t.rays = rays[cur];
+  t.sh = sh;
+  t.slots = S;
+  t.ray_key = d_ray_key;
+  t.rec_key = d_rec_key;
+  t.rec_attr = d_rec_attr;
+  t.cull = cfg.cull;
+  t.ctr = d_ctr;
+  return t;
+}
+
+SceneDev Tracer::sceneDev() const {
+  SceneDev s;
+  s.domains = d_domains;
+  s.num_domains = D;
+  s.nodes = d_nodes;
+  s.tris = d_tris;
+  s.faces = d_faces;
+  s.colors = d_colors;
+  s.normals = d_normals;
+  return s;
+}
+
+cudaEvent_t Tracer::poolEvent() {
+  if (ev_used == ev_pool.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    ev_pool.push_back(e);
+  }
+  return ev_pool[ev_used++];
+}
+
+void Tracer::traceWave(const Wave& w, bool capture) {
+  const int S = std::max(slots(), 1);
+  const int spp = cfg.pixel_samples;
+  std::vector<TileDev> td(w.num_tiles);
+  int64_t base = 0;
+  for (int k = 0; k < w.num_tiles; ++k) {
+    const HostTile& t = tiles[w.first_tile + k];
+    td[k] = TileDev{t.x, t.y, t.w, t.h, base};
+    base += (int64_t)t.w * t.h * spp;
+  }
+  CK(cudaMemcpyAsync(d_tiles, td.data(), td.size() * sizeof(TileDev), cudaMemcpyHostToDevice, stream));
+  h2d_bytes += td.size() * sizeof(TileDev);
+  cur = 0;
+  launchGenPrimary(stream, cam, d_tiles, w.num_tiles, w.samples, spp, cfg.image_w, rays[0],
+                   d_alive_list, d_alive_count, d_alive_idx, d_ctr);
+  launches += 1;
+  const int order_by_depth = cfg.cull ? 1 : 0;
+  const int nblk = num_sms * 4;
+  for (int b = 0; b < cfg.bounces; ++b) {
+    if (capture) captureRays(b);
+    // radiance rays -> per-domain queues
+    if (b == 0 || capture) {
+      CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
+      launches += 1;
+    }
+    cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
+    CK(cudaEventRecord(s0, stream));
+    schedule(false, order_by_depth, d_alive_count, d_alive_list, S);
+    CK(cudaEventRecord(s1, stream));
+    sched_events.push_back({s0, s1});
+    if (capture) {
+      launchScores(stream, d_dstats, D, cfg.list_size, d_scores, d_order);
+      launches += 1;
+      captureQueues(SPRAY_DBG_RQUEUES, b, order_by_depth);
+      captureScores(b);
+    }
+    CK(cudaMemsetAsync(d_work, 0, 4, stream));
+    TraceArgs ta = traceArgs(order_by_depth, S);
+    cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
+    CK(cudaEventRecord(t0, stream));
+    launchTraceClosest(stream, ta, num_sms * 8);
+    CK(cudaEventRecord(t1, stream));
+    trace_events.push_back({t0, t1});
+    launchResolve(stream, ta, d_hit_ns, nblk);
+    launches += 3;
+    if (capture) captureHits(b);
+    // shade
+    CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
+    ShadeArgs sa{};
+    sa.scene = sceneDev();
+    sa.count = d_alive_count;
+    sa.list = d_alive_list;
+    sa.rays = rays[cur];
+    sa.next = rays[cur ^ 1];
+    sa.next_flag = d_next_flag;
+    sa.ray_key = d_ray_key;
+    sa.hit_ns = d_hit_ns;
+    sa.sh = sh;
+    sa.shadow_flag = d_shadow_flag;
+    sa.slots = S;
+    sa.depth = b;
+    sa.ao_mode = cfg.ao_mode;
+    sa.ao_samples = cfg.ao_samples;
+    sa.bounces = cfg.bounces;
+    sa.rr_depth = cfg.rr_depth;
+    sa.ao_light_shadow = cfg.ao_light_shadow;
+    sa.ao_max_distance = cfg.ao_max_distance;
+    for (int c = 0; c < 3; ++c) sa.ks[c] = cfg.ks[c];
+    sa.shininess = cfg.shininess;
+    sa.lights = d_lights;
+    sa.num_lights = (int)lights.size();
+    sa.ctr = d_ctr;
+    launchShade(stream, sa, nblk);
+    launches += 2;
+    // shadow rays -> queues -> occlusion
+    launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
+                  nullptr, d_block_tmp, compact_blocks);
+    launches += 3;
+    schedule(true, 0, d_shadow_count, d_shadow_list, S);
+    if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, 0);
+    CK(cudaMemsetAsync(d_work, 0, 4, stream));
+    TraceArgs to = traceArgs(0, S);
+    cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
+    CK(cudaEventRecord(o0, stream));
+    launchTraceOccluded(stream, to, num_sms * 8);
+    CK(cudaEventRecord(o1, stream));
+    occl_events.push_back({o0, o1});
+    launches += 2;
+    if (capture) captureShadows(b, S);
+    // retire
+    int64_t npix = w.samples / spp;
+    launchRetireImpl(stream, d_image, npix, spp, d_pixid, d_alive_idx, sh, d_shadow_flag, S,
+                     1.0 / (double)spp, nblk);
+    launches += 1;
+    // next depth
+    if (b + 1 < cfg.bounces) {
+      launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count,
+                    d_alive_idx, d_block_tmp, compact_blocks);
+      launches += 3;
+      cur ^= 1;
+    }
+  }
+}
+
+void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
+  if (!has_scene) throw StateError("trace before set_scene");
+  if (!has_camera) throw StateError("trace before set_camera");
+  CK(cudaSetDevice(cfg.device));
+  planWaves();
+  int64_t maxw = 0;
+  for (auto& w : waves) maxw = std::max(maxw, w.samples);
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    ensureBuffers(maxw);
+    launches = 0;
+    h2d_bytes = 0;
+    d2h_bytes = 0;
+    ev_used = 0;
+    sched_events.clear();
+    trace_events.clear();
+    occl_events.clear();
+    dbg.clear();
+    CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
+    CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
+    launches += 2;
+    CK(cudaEventRecord(ev_start, stream));
+    for (size_t k = 0; k < waves.size(); ++k) traceWave(waves[k], cfg.debug_capture && k == 0);
+    CK(cudaEventRecord(ev_stop, stream));
+    Counters ctr;
+    CK(cudaMemcpyAsync(&ctr, d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    if (ctr.arena_overflows || ctr.entry_overflows) {
+      needed_entries = cap_entries * 2;
+      continue;  // retrace with larger queues
+    }
+    if (ctr.list_overflows) throw OverflowError("a ray overlapped more than 32 domains");
+    size_t img_bytes = (size_t)cfg.image_w * cfg.image_h * sizeof(float4);
+    if (out) {
+      if (out_is_device) {
+        CK(cudaMemcpyAsync(out, d_image, img_bytes, cudaMemcpyDeviceToDevice, stream));
+      } else {
+        CK(cudaMemcpyAsync(out, d_image, img_bytes, cudaMemcpyDeviceToHost, stream));
+        d2h_bytes += img_bytes;
+      }
+      CK(cudaStreamSynchronize(stream));
+    }
+    if (st) {
+      std::memset(st, 0, sizeof(*st));
+      st->rays_primary = (int64_t)ctr.rays_primary;
+      st->rays_shadow = (int64_t)ctr.rays_shadow;
+      st->rays_bounce = (int64_t)ctr.rays_bounce;
+      st->visits_radiance = (int64_t)ctr.visits_radiance;
+      st->visits_shadow = (int64_t)ctr.visits_shadow;
+      st->visits_culled = (int64_t)ctr.visits_culled;
+      st->domain_loads = 0;
+      st->h2d_bytes = (int64_t)h2d_bytes;
+      st->d2h_bytes = (int64_t)d2h_bytes;
+      st->kernel_launches = launches;
+      st->list_overflows = (int64_t)ctr.list_overflows;
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ev_start, ev_stop));
+      st->frame_ms = ms;
+      auto sum = [](const std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& v) {
+        double acc = 0.0;
+        for (auto& p : v) {
+          float m = 0.f;
+          if (cudaEventElapsedTime(&m, p.first, p.second) == cudaSuccess) acc += m;
+        }
+        return acc;
+      };
+      st->trace_ms = sum(trace_events);
+      st->occlude_ms = sum(occl_events);
+      st->schedule_ms = sum(sched_events);
+      st->trace_launches = (int64_t)trace_events.size();
+      st->occlude_launches = (int64_t)occl_events.size();
+    }
+    return;
+  }
+  throw std::runtime_error("queue capacity could not be grown enough");
+}
+
+// ---------------------------------------------------------------- debug
+template <class T>
+static std::vector<T> fetch(const T* d, size_t n, cudaStream_t s) {
+  std::vector<T> h(n);
+  if (n) {
+    CK(cudaMemcpyAsync(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  return h;
+}
+static uint32_t fetch1(const uint32_t* d, cudaStream_t s) { return fetch(d, 1, s)[0]; }
+
+void Tracer::captureRays(int b) {
+  uint32_t n = fetch1(d_alive_count, stream);
+  auto list = fetch(d_alive_list, n, stream);
+  auto org = fetch(rays[cur].org, cap_samples, stream);
+  auto dir = fetch(rays[cur].dir, cap_samples, stream);
+  auto wgt = fetch(rays[cur].wgt, cap_samples, stream);
+  auto pix = fetch(d_pixid, cap_samples, stream);
+  auto sam = fetch(d_samid, cap_samples, stream);
+  std::vector<char>& out = dbg[{SPRAY_DBG_RAYS, b}];
+  out.resize(n * sizeof(spray_gpu_dbg_ray));
+  auto* r = (spray_gpu_dbg_ray*)out.data();
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t s = list[i];
+    r[i].sample = s;
+    r[i].pixid = pix[s];
+    r[i].samid = sam[s];
+    float4 o = org[s], d = dir[s], w = wgt[s];
+    float ov[3] = {o.x, o.y, o.z}, dv[3] = {d.x, d.y, d.z}, wv[3] = {w.x, w.y, w.z};
+    std::memcpy(r[i].org, ov, 12);
+    std::memcpy(r[i].dir, dv, 12);
+    std::memcpy(r[i].w, wv, 12);
+  }
+}
+
+void Tracer::captureQueues(int what, int b, int order_by_depth) {
+  uint32_t E = fetch1(d_num_entries, stream);
+  const int nkeys = order_by_depth ? kDepthBuckets * D : D;
+  auto ks = fetch(d_key_start, nkeys + 1, stream);
+  auto ent = fetch(d_entries, E, stream);
+  std::vector<char>& out = dbg[{what, b}];
+  out.resize(E * sizeof(spray_gpu_dbg_entry));
+  auto* r = (spray_gpu_dbg_entry*)out.data();
+  int key = 0;
+  for (uint32_t e = 0; e < E; ++e) {
+    while (key + 1 < nkeys && ks[key + 1] <= e) ++key;
+    r[e].domain = key % D;
+    r[e].ray = ent[e].x & kRayIdMask;
+    float t;
+    std::memcpy(&t, &ent[e].y, 4);
+    r[e].tdom = t;
+    r[e].depth = (int32_t)((ent[e].x >> kRayIdBits) & 31u);
+    r[e].origin = (int32_t)(ent[e].x >> 31);
+  }
+}
+
+void Tracer::captureScores(int b) {
+  auto sc = fetch(d_scores, D, stream);
+  auto od = fetch(d_order, D, stream);
+  std::vector<char>& out = dbg[{SPRAY_DBG_SCORES, b}];
+  out.resize(D * sizeof(spray_gpu_dbg_score));
+  auto* r = (spray_gpu_dbg_score*)out.data();
+  for (int d = 0; d < D; ++d) {
+    r[d].domain = d;
+    r[d].score = sc[d];
+    r[d].order = -1;
+  }
+  for (int k = 0; k < D; ++k) r[od[k]].order = k;
+}
+
+void Tracer::captureHits(int b) {
+  uint32_t n = fetch1(d_alive_count, stream);
+  auto list = fetch(d_alive_list, n, stream);
+  auto key = fetch(d_ray_key, cap_samples, stream);
+  auto ns = fetch(d_hit_ns, cap_samples, stream);
+  std::vector<char>& out = dbg[{SPRAY_DBG_HITS, b}];
+  out.resize(n * sizeof(spray_gpu_dbg_hit));
+  auto* r = (spray_gpu_dbg_hit*)out.data();
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t s = list[i];
+    r[i].sample = s;
+    uint64_t k = key[s];
+    if (k == kNoHit) {
+      r[i].hit = 0;
+      r[i].t = INFINITY;
+      r[i].domain = -1;
+      r[i].prim = -1;
+      r[i].color = 0;
+      r[i].ns[0] = r[i].ns[1] = r[i].ns[2] = 0.f;
+      continue;
+    }
+    r[i].hit = 1;
+    r[i].t = hitKeyT(k);
+    uint32_t g = (uint32_t)k;
+    int d = 0;
+    while (d + 1 < D && hdoms[d + 1].gprim_base <= g) ++d;
+    r[i].domain = d;
+    r[i].prim = (int32_t)(g - hdoms[d].gprim_base);
+    float4 h = ns[s];
+    std::memcpy(&r[i].color, &h.w, 4);
+    r[i].ns[0] = h.x;
+    r[i].ns[1] = h.y;
+    r[i].ns[2] = h.z;
+  }
+}
+
+void Tracer::captureShadows(int b, int S) {
+  uint32_t n = fetch1(d_alive_count, stream);
+  auto list = fetch(d_alive_list, n, stream);
+  size_t ns = (size_t)n * S;
+  auto flag = fetch(d_shadow_flag, ns, stream);
+  auto dir = fetch(sh.dir, ns, stream);
+  auto wgt = fetch(sh.wgt, ns, stream);
+  auto occ = fetch(sh.occluded, ns, stream);
+  auto hp = fetch(sh.hitpos, n, stream);
+  std::vector<char>& out = dbg[{SPRAY_DBG_SHADOWS, b}];
+  out.clear();
+  for (uint32_t a = 0; a < n; ++a)
+    for (int k = 0; k < S; ++k) {
+      size_t sid = (size_t)a * S + k;
+      if (!flag[sid]) continue;
+      spray_gpu_dbg_shadow r;
+      r.sample = list[a];
+      r.slot = k;
+      r.org[0] = hp[a].x;
+      r.org[1] = hp[a].y;
+      r.org[2] = hp[a].z;
+      r.dir[0] = dir[sid].x;
+      r.dir[1] = dir[sid].y;
+      r.dir[2] = dir[sid].z;
+      r.tmax = dir[sid].w;
+      r.w[0] = wgt[sid].x;
+      r.w[1] = wgt[sid].y;
+      r.w[2] = wgt[sid].z;
+      r.occluded = occ[sid];
+      const char* p = (const char*)&r;
+      out.insert(out.end(), p, p + sizeof(r));
+    }
+}
+
+int64_t Tracer::debugCount(int what, int bounce) const {
+  auto it = dbg.find({what, bounce});
+  if (it == dbg.end()) return -1;
+  static const size_t sizes[] = {sizeof(spray_gpu_dbg_ray), sizeof(spray_gpu_dbg_entry),
+                                 sizeof(spray_gpu_dbg_hit), sizeof(spray_gpu_dbg_shadow),
+                                 sizeof(spray_gpu_dbg_entry), sizeof(spray_gpu_dbg_score)};
+  return (int64_t)(it->second.size() / sizes[what]);
+}
+
+const std::vector<char>* Tracer::debugData(int what, int bounce) const {
+  auto it = dbg.find({what, bounce});
+  return it == dbg.end() ? nullptr : &it->second;
+}
+
+}  // namespace spray
+
+// ====================================================================== C ABI
+using spray::fail;
+
+#define API_GUARD(body)                                                  \
+  try {                                                                  \
+    body                                                                 \
+  } catch (const spray::CudaError& e) {                                  \
+    return fail(SPRAY_GPU_ECUDA, e.what());                              \
+  } catch (const spray::StateError& e) {                                 \
+    return fail(SPRAY_GPU_ESTATE, e.what());                             \
+  } catch (const spray::OverflowError& e) {                              \
+    return fail(SPRAY_GPU_EOVERFLOW, e.what());                          \
+  } catch (const std::invalid_argument& e) {                             \
+    return fail(SPRAY_GPU_EINVAL, e.what());                             \
+  } catch (const std::bad_alloc&) {                                      \
+    return fail(SPRAY_GPU_ENOMEM, "host allocation failed");             \
+  } catch (const std::exception& e) {                                    \
+    return fail(SPRAY_GPU_ECUDA, e.what());                              \
+  }
+
+struct spray_gpu_tracer {
+  std::unique_ptr<spray::Tracer> impl;
+};
+
+extern "C" {
+
+void spray_gpu_config_defaults(spray_gpu_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->image_w = 400;
+  c->image_h = 400;
+  c->ao_mode = 0;
+  c->ao_samples = 8;
+  c->pixel_samples = 4;
+  c->bounces = 1;
+  c->fov = 90.0f;
+  c->cache_size = -1;
+  c->max_samples_per_rank = 1024 * 1024;
+  c->list_size = 16;
+  c->history_size = 4;
+  c->nthreads = 1;
+  c->num_ranks = 1;
+  c->rank = 0;
+  c->cull = 1;
+}
+
+const char* spray_gpu_last_error(void) { return spray::g_last_error.c_str(); }
+
+int spray_gpu_create(const spray_gpu_config* cfg, spray_gpu_tracer** out) {
+  if (!cfg || !out) return fail(SPRAY_GPU_EINVAL, "null argument");
+  *out = nullptr;
+  API_GUARD({
+    auto t = std::make_unique<spray_gpu_tracer>();
+    t->impl = std::make_unique<spray::Tracer>(*cfg);
+    *out = t.release();
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_destroy(spray_gpu_tracer* t) {
+  if (!t) return SPRAY_GPU_OK;
+  delete t;
+  return SPRAY_GPU_OK;
+}
+
+int spray_gpu_set_scene(spray_gpu_tracer* t, const spray_gpu_domain* domains, int32_t num_domains,
+                        const spray_gpu_light* lights, int32_t num_lights) {
+  if (!t || !domains || (num_lights > 0 && !lights)) return fail(SPRAY_GPU_EINVAL, "null argument");
+  API_GUARD({
+    t->impl->setScene(domains, num_domains, lights, num_lights);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_set_camera(spray_gpu_tracer* t, const float pos[3], const float lookat[3],
+                         const float up[3], float vfov) {
+  if (!t || !pos || !lookat || !up) return fail(SPRAY_GPU_EINVAL, "null argument");
+  API_GUARD({
+    t->impl->setCamera(pos, lookat, up, vfov);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_trace(spray_gpu_tracer* t, float* rgba_out, spray_gpu_stats* stats) {
+  if (!t) return fail(SPRAY_GPU_EINVAL, "null tracer");
+  API_GUARD({
+    t->impl->trace(rgba_out, false, stats);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_trace_device(spray_gpu_tracer* t, float* rgba_dev, spray_gpu_stats* stats) {
+  if (!t) return fail(SPRAY_GPU_EINVAL, "null tracer");
+  API_GUARD({
+    t->impl->trace(rgba_dev, true, stats);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int64_t* count) {
+  if (!t || !count) return fail(SPRAY_GPU_EINVAL, "null argument");
+  if (what < 0 || what > SPRAY_DBG_SCORES) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
+  int64_t n = t->impl->debugCount(what, bounce);
+  if (n < 0) return fail(SPRAY_GPU_ESTATE, "no captured buffer (set debug_capture and trace)");
+  *count = n;
+  return SPRAY_GPU_OK;
+}
+
+int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void* out, int64_t capacity) {
+  if (!t || !out) return fail(SPRAY_GPU_EINVAL, "null argument");
+  if (what < 0 || what > SPRAY_DBG_SCORES) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
+  const std::vector<char>* d = t->impl->debugData(what, bounce);
+  if (!d) return fail(SPRAY_GPU_ESTATE, "no captured buffer (set debug_capture and trace)");
+  if ((int64_t)d->size() > capacity) return fail(SPRAY_GPU_EINVAL, "output buffer too small");
+  std::memcpy(out, d->data(), d->size());
+  return SPRAY_GPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// Internal host-side tracer object behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/spray_gpu.h"
+#include "kernels.cuh"
+
+namespace spray {
+
+struct StateError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct OverflowError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+int fail(int code, const std::string& msg);
+
+struct HostTile {
+  int x, y, w, h;
+};
+
+struct Wave {
+  int first_tile;
+  int num_tiles;
+  int64_t samples;
+};
+
+// A domain prepared for the device: BVH, leaf-ordered triangles and the
+// per-vertex shading data.
+struct DomainPack {
+  int64_t nv = 0, nf = 0;
+  std::vector<BvhNode4> nodes;
+  std::vector<float4> tris;
+  std::vector<uint32_t> faces;
+  std::vector<uint32_t> colors;
+  std::vector<float> normals;
+  int bvh_depth = 0;
+};
+
+std::vector<HostTile> makeTiles(int W, int H, int spp, int num_ranks, int rank, int64_t max_samples);
+void computeVertexNormals(const float* v, int64_t nv, const uint32_t* f, int64_t nf, float* n);
+CameraDev makeCamera(const float p[3], const float l[3], const float up[3], float vfov, int W, int H);
+
+class Tracer {
+ public:
+  explicit Tracer(const spray_gpu_config& c);
+  ~Tracer();
+  void setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_light* ls, int nl);
+  void setCamera(const float p[3], const float l[3], const float up[3], float vfov);
+  void trace(float* out, bool out_is_device, spray_gpu_stats* st);
+  int64_t debugCount(int what, int bounce) const;
+  const std::vector<char>* debugData(int what, int bounce) const;
+
+ private:
+  int slots() const;
+  void planWaves();
+  void ensureBuffers(int64_t nsamples);
+  void freeScene();
+  void freeBuffers();
+  void traceWave(const Wave& w, bool capture);
+  void schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S);
+  TraceArgs traceArgs(int order_by_depth, int S);
+  SceneDev sceneDev() const;
+  cudaEvent_t poolEvent();
+  void captureRays(int b);
+  void captureQueues(int what, int b, int order_by_depth);
+  void captureScores(int b);
+  void captureHits(int b);
+  void captureShadows(int b, int S);
+
+  spray_gpu_config cfg;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sched_events, trace_events, occl_events;
+
+  // scene
+  bool has_scene = false, has_camera = false;
+  int D = 0;
+  int max_bvh_depth = 0;
+  size_t total_tris = 0;
+  std::vector<DomainDev> hdoms;
+  std::vector<spray_gpu_light> lights;
+  DomainDev* d_domains = nullptr;
+  BvhNode4* d_nodes = nullptr;
+  float4* d_tris = nullptr;
+  uint32_t* d_faces = nullptr;
+  uint32_t* d_colors = nullptr;
+  float* d_normals = nullptr;
+  float* d_lights = nullptr;
+  CameraDev cam{};
+
+  // frame plan
+  std::vector<HostTile> tiles;
+  std::vector<Wave> waves;
+
+  // wave buffers
+  int64_t cap_samples = 0;
+  uint64_t cap_entries = 0, needed_entries = 0;
+  int sched_blocks = 0, sched_warps = 0, compact_blocks = 0;
+  int cur = 0;
+  RayBuf rays[2] = {};
+  int32_t* d_pixid = nullptr;
+  int32_t* d_samid = nullptr;
+  uint32_t* d_alive_list = nullptr;
+  int32_t* d_alive_idx = nullptr;
+  uint32_t* d_alive_count = nullptr;
+  uint8_t* d_next_flag = nullptr;
+  uint64_t* d_ray_key = nullptr;
+  float4* d_hit_ns = nullptr;
+  ShadowBuf sh = {};
+  uint8_t* d_shadow_flag = nullptr;
+  uint32_t* d_shadow_list = nullptr;
+  uint32_t* d_shadow_count = nullptr;
+  uint2* d_arena = nullptr;
+  unsigned long long* d_arena_top = nullptr;
+  uint32_t* d_list_off = nullptr;
+  uint32_t* d_list_cnt = nullptr;
+  uint32_t* d_hist = nullptr;
+  long long* d_dstats = nullptr;
+  uint2* d_entries = nullptr;
+  uint32_t* d_key_start = nullptr;
+  uint32_t* d_num_entries = nullptr;
+  uint64_t* d_rec_key = nullptr;
+  float4* d_rec_attr = nullptr;
+  unsigned int* d_work = nullptr;
+  uint32_t* d_block_tmp = nullptr;
+  float4* d_image = nullptr;
+  long long* d_scores = nullptr;
+  int32_t* d_order = nullptr;
+  TileDev* d_tiles = nullptr;
+  Counters* d_ctr = nullptr;
+
+  // frame accounting
+  int64_t launches = 0;
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
+  std::map<std::pair<int, int>, std::vector<char>> dbg;
+};
+
+}  // namespace spray

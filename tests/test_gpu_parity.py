@@ -1,0 +1,302 @@
+"""CUDA path vs the CPU oracle, stage by stage and image by image.
+
+Every check calls the GPU through the C ABI (spray_gb300 -> libspray_gpu.so)
+and compares with the oracle on the same seeded inputs:
+  eye rays, per-domain queues, domain scores    bit-exact
+  closest hits (hit, domain, prim, t, colour, Ns)  bit-exact (>= 99.99% required)
+  shadow and bounce rays from the shaders       bit-exact
+  occlusion flags                               bit-exact (>= 99.99% required)
+  images vs the wavefront oracle                bit-exact (same accumulation order)
+  images vs the speculative loop (mode A)       max abs 1e-5 (float accumulation order)
+"""
+import numpy as np
+import pytest
+
+import spray_gb300 as sg
+from spray_gb300 import scenes
+from conftest import small_config
+
+pytestmark = pytest.mark.gpu
+
+HIT_AGREE = 0.9999   # required agreement on hit/miss, domain and primitive
+T_RTOL = 1e-5        # required relative agreement of hit distances
+IMG_RMSE = 1e-3      # required image agreement (RMSE on [0,1] radiance)
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def scene8():
+    return scenes.wavelet_grid(2, 24, colors="albedo", light="point+diffuse")
+
+
+@pytest.fixture(scope="module")
+def scene64():
+    return scenes.wavelet_grid(4, 32, colors="albedo", light="point")
+
+
+def run(cfg, scene, grid, oracle_mod, **gpu_kw):
+    cam = scenes.orbit_camera(grid)
+    t = sg.Tracer(cfg, debug_capture=1, **gpu_kw)
+    t.set_scene(scene)
+    t.set_camera(*cam)
+    img, st = t.trace()
+    o = oracle_mod.Oracle(cfg, scene)
+    o.set_camera(*cam)
+    return t, img, st, o
+
+
+def test_eye_rays_bit_exact(lib_built, oracle_mod, scene8):
+    for spp in (1, 4):
+        cfg = small_config(pixel_samples=spp, image_w=40, image_h=30, max_samples_per_rank=1024)
+        t, img, st, o = run(cfg, scene8, 2, oracle_mod)
+        r = t.debug(sg.DBG_RAYS, 0)
+        ntiles = len(o.tiles())
+        org, dr, pix, sam = o.eyes(0, ntiles)
+        assert len(r) == len(org) == 40 * 30 * spp
+        assert np.array_equal(r["sample"], np.arange(len(r)))
+        assert np.array_equal(bits(r["org"]), bits(org))
+        assert np.array_equal(bits(r["dir"]), bits(dr))
+        assert np.array_equal(r["pixid"], pix) and np.array_equal(r["samid"], sam)
+
+
+def _queues_by_domain(e):
+    order = np.lexsort((e["ray"], e["domain"]))
+    e = e[order]
+    return e["domain"], e["ray"], bits(e["tdom"]), e["depth"], e["origin"]
+
+
+@pytest.mark.parametrize("cull", [0, 1])
+def test_radiance_queues_bit_exact(lib_built, oracle_mod, scene64, cull):
+    cfg = small_config(image_w=80, image_h=60)
+    t, img, st, o = run(cfg, scene64, 4, oracle_mod, cull=cull)
+    rays = t.debug(sg.DBG_RAYS, 0)
+    q = t.debug(sg.DBG_RQUEUES, 0)
+    oq, dstats = o.schedule(rays["org"], rays["dir"])
+    oq["ray"] = rays["sample"][oq["ray"]]
+    assert len(q) == len(oq) > len(rays)
+    if cull == 0:
+        # domain-major order, each queue in push (ray) order: the exact sequence
+        assert np.array_equal(q["domain"], oq["domain"]) and np.array_equal(q["ray"], oq["ray"])
+        assert np.array_equal(bits(q["tdom"]), bits(oq["tdom"]))
+        assert np.array_equal(q["depth"], oq["depth"])
+    for a, b in zip(_queues_by_domain(q), _queues_by_domain(oq)):
+        assert np.array_equal(a, b)
+    # DomainStats scores and the processing order
+    sc = t.debug(sg.DBG_SCORES, 0)
+    osc, oorder = o.scores(dstats)
+    assert np.array_equal(sc["score"], osc)
+    assert np.array_equal(np.argsort(sc["order"]), oorder)
+
+
+def _hits_match(h, oh):
+    same = (h["hit"] == oh["hit"]) & (h["domain"] == oh["domain"]) & (h["prim"] == oh["prim"])
+    return same
+
+
+def test_closest_hits_bit_exact(lib_built, oracle_mod, scene64):
+    cfg = small_config(image_w=96, image_h=72, ao_mode=0, pixel_samples=2, bounces=3)
+    t, img, st, o = run(cfg, scene64, 4, oracle_mod)
+    total = 0
+    for b in range(3):
+        rays = t.debug(sg.DBG_RAYS, b)
+        h = t.debug(sg.DBG_HITS, b)
+        assert np.array_equal(h["sample"], rays["sample"])
+        oh = o.closest(rays["org"], rays["dir"])
+        same = _hits_match(h, oh)
+        assert same.mean() >= HIT_AGREE, (b, same.mean())
+        hit = (h["hit"] == 1) & same
+        assert np.allclose(h["t"][hit], oh["t"][hit], rtol=T_RTOL, atol=0)
+        # the same watertight test on both sides: identical bits
+        assert same.all(), np.nonzero(~same)[0][:10]
+        assert np.array_equal(bits(h["t"][hit]), bits(oh["t"][hit]))
+        assert np.array_equal(h["color"][hit], oh["color"][hit])
+        assert np.array_equal(bits(h["ns"][hit]), bits(oh["ns"][hit]))
+        total += hit.sum()
+    assert total > 1000
+
+
+def _shade_check(t, o, b, S):
+    rays = t.debug(sg.DBG_RAYS, b)
+    h = t.debug(sg.DBG_HITS, b)
+    sh = t.debug(sg.DBG_SHADOWS, b)
+    m = h["hit"] == 1
+    r, hh = rays[m], h[m]
+    out = o.shade(b, r["org"], r["dir"], r["w"], r["pixid"], r["samid"], hh["t"], hh["domain"],
+                  hh["color"], hh["ns"])
+    # expected shadow rays, ordered (sample, slot)
+    samp = np.repeat(r["sample"], S)
+    slot = np.tile(np.arange(S), len(r))
+    valid = out["svalid"].reshape(-1).astype(bool)
+    exp_s, exp_k = samp[valid], slot[valid]
+    assert np.array_equal(sh["sample"], exp_s) and np.array_equal(sh["slot"], exp_k)
+    assert np.array_equal(bits(sh["dir"]), bits(out["sdir"].reshape(-1, 3)[valid]))
+    assert np.array_equal(bits(sh["w"]), bits(out["sw"].reshape(-1, 3)[valid]))
+    assert np.array_equal(bits(sh["tmax"]), bits(out["stmax"].reshape(-1)[valid]))
+    # bounce rays become the rays of the next depth
+    if b + 1 < t.config["bounces"]:
+        nxt = t.debug(sg.DBG_RAYS, b + 1)
+        bv = out["bvalid"].astype(bool)
+        assert np.array_equal(nxt["sample"], r["sample"][bv])
+        assert np.array_equal(bits(nxt["dir"]), bits(out["bdir"][bv]))
+        assert np.array_equal(bits(nxt["w"]), bits(out["bw"][bv]))
+        pos = r["dir"] * hh["t"][:, None] + r["org"]
+        assert np.array_equal(bits(nxt["org"]), bits(pos[bv].astype(np.float32)))
+    return sh, h
+
+
+@pytest.mark.parametrize("mode", ["ao", "pt"])
+def test_shaders_bit_exact(lib_built, oracle_mod, scene8, mode):
+    cfg = small_config(image_w=64, image_h=48, ao_mode=int(mode == "ao"), ao_samples=3,
+                       pixel_samples=2, bounces=3, ks=[0.4, 0.4, 0.4], shininess=10.0)
+    t, img, st, o = run(cfg, scene8, 2, oracle_mod)
+    S = o.slots()
+    for b in range(3):
+        _shade_check(t, o, b, S)
+
+
+def test_occlusion_and_shadow_queues(lib_built, oracle_mod, scene64):
+    cfg = small_config(image_w=80, image_h=60, ao_mode=1, ao_samples=4, bounces=2)
+    t, img, st, o = run(cfg, scene64, 4, oracle_mod)
+    S = o.slots()
+    for b in range(2):
+        sh = t.debug(sg.DBG_SHADOWS, b)
+        h = t.debug(sg.DBG_HITS, b)
+        rays = t.debug(sg.DBG_RAYS, b)
+        dom_of = dict(zip(h["sample"].tolist(), h["domain"].tolist()))
+        origin = np.array([dom_of[s] for s in sh["sample"]], np.int32)
+        occ = o.occluded(sh["org"], sh["dir"], sh["tmax"], origin)
+        agree = (occ == sh["occluded"]).mean()
+        assert agree >= HIT_AGREE and agree == 1.0
+        # shadow queues: ray id = alive index * slots + slot
+        alive = {s: i for i, s in enumerate(rays["sample"].tolist())}
+        sid = np.array([alive[s] * S + k for s, k in zip(sh["sample"].tolist(), sh["slot"].tolist())],
+                       np.uint32)
+        q = t.debug(sg.DBG_SQUEUES, b)
+        oq, _ = o.schedule(sh["org"], sh["dir"], sh["tmax"], origin)
+        oq["ray"] = sid[oq["ray"]]
+        for a, c in zip(_queues_by_domain(q), _queues_by_domain(oq)):
+            assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("mode,spp,bounces,light", [
+    ("ao", 1, 1, "point"), ("ao", 2, 2, "point"), ("pt", 1, 1, "point"),
+    ("pt", 2, 3, "point+diffuse"), ("pt", 4, 4, "point+diffuse"), ("pt", 2, 3, "quad"),
+])
+def test_image_matches_oracles(lib_built, oracle_mod, mode, spp, bounces, light):
+    sc = scenes.wavelet_grid(2, 24, colors="albedo", light=light)
+    cfg = small_config(image_w=72, image_h=54, ao_mode=int(mode == "ao"), ao_samples=3,
+                       pixel_samples=spp, bounces=bounces, max_samples_per_rank=4096)
+    t, img, st, o = run(cfg, sc, 2, oracle_mod)
+    wb, sb = o.render_wavefront()
+    assert np.array_equal(bits(img), bits(wb))           # same order of every float add
+    assert st["rays_primary"] == sb["rays_primary"]
+    assert st["rays_shadow"] == sb["rays_shadow"] and st["rays_bounce"] == sb["rays_bounce"]
+    wa, sa = o.render_speculative(2)
+    assert np.abs(img - wa).max() <= 1e-5
+    assert np.sqrt(np.mean((img[..., :3] - wa[..., :3]) ** 2)) < IMG_RMSE
+    assert img[..., :3].max() > 0
+
+
+def test_extensions_match_wavefront_oracle(lib_built, oracle_mod):
+    sc = scenes.wavelet_grid(2, 24, colors="albedo", light="quad")
+    diag = scenes.scene_diagonal(2)
+    for cfg in (small_config(ao_mode=1, ao_samples=4, ao_max_distance=0.05 * diag, ao_light_shadow=1),
+                small_config(ao_mode=0, ao_samples=2, pixel_samples=2, bounces=5, rr_depth=3)):
+        t, img, st, o = run(cfg, sc, 2, oracle_mod)
+        wb, _ = o.render_wavefront()
+        assert np.array_equal(bits(img), bits(wb))
+
+
+def test_waves_and_culling_do_not_change_the_image(lib_built, oracle_mod, scene64):
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3,
+                       max_samples_per_rank=2048)
+    cam = scenes.orbit_camera(4)
+    imgs = []
+    for kw in (dict(cull=1), dict(cull=0), dict(cull=1, wave_samples=3000), dict(cull=0, wave_samples=2048)):
+        t = sg.Tracer(cfg, **kw)
+        t.set_scene(scene64)
+        t.set_camera(*cam)
+        img, st = t.trace()
+        imgs.append(img)
+        if kw["cull"]:
+            assert st["visits_culled"] > 0
+    for im in imgs[1:]:
+        assert np.array_equal(bits(im), bits(imgs[0]))
+
+
+def test_deterministic_frames(lib_built, scene64):
+    t = sg.Tracer(small_config(image_w=64, image_h=64, ao_mode=0, pixel_samples=2, bounces=2))
+    t.set_scene(scene64)
+    t.set_camera(*scenes.orbit_camera(4))
+    a, sa = t.trace()
+    b, sb = t.trace()
+    assert np.array_equal(bits(a), bits(b))
+    for k in ("rays_primary", "rays_shadow", "rays_bounce", "visits_radiance", "visits_shadow"):
+        assert sa[k] == sb[k]
+
+
+def test_all_rays_miss(lib_built, scene8):
+    t = sg.Tracer(small_config(image_w=32, image_h=16))
+    t.set_scene(scene8)
+    t.set_camera((0, 0, 50), (0, 0, 100), (0, 1, 0))  # looking away from the grid
+    img, st = t.trace()
+    assert not img.any() and st["rays_shadow"] == 0 and st["visits_radiance"] == 0
+
+
+def test_single_triangle_and_ragged_tiles(lib_built, oracle_mod):
+    v = np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0]], np.float32)
+    f = np.array([[0, 1, 2]], np.uint32)
+    sc = sg.Scene([sg.Domain(v, f, np.full(3, 0x80a0c0, np.uint32))], [sg.Light(0, (0, 0, 5))])
+    cfg = small_config(image_w=37, image_h=23, ao_mode=0, pixel_samples=3, max_samples_per_rank=500)
+    t = sg.Tracer(cfg)
+    t.set_scene(sc)
+    t.set_camera((0.1, 0.2, 3), (0, 0, 0), (0, 1, 0))
+    img, st = t.trace()
+    o = oracle_mod.Oracle(cfg, sc)
+    o.set_camera((0.1, 0.2, 3), (0, 0, 0), (0, 1, 0))
+    assert len(o.tiles()) > 5
+    wb, _ = o.render_wavefront()
+    assert np.array_equal(bits(img), bits(wb)) and img[..., :3].max() > 0
+
+
+def test_errors(lib_built, scene8):
+    t = sg.Tracer(small_config())
+    with pytest.raises(sg.SprayError) as e:
+        t.trace()
+    assert e.value.code == sg.ESTATE
+    t.set_scene(scene8)
+    with pytest.raises(sg.SprayError) as e:
+        t.trace()
+    assert e.value.code == sg.ESTATE  # no camera yet
+    pt = sg.Tracer(small_config(ao_mode=0))
+    with pytest.raises(sg.SprayError) as e:
+        pt.set_scene(sg.Scene(scene8.domains, []))
+    assert e.value.code == sg.EINVAL
+    with pytest.raises(sg.SprayError) as e:
+        sg.Tracer(small_config(list_size=64))
+    assert e.value.code == sg.EINVAL
+
+
+def test_domain_list_overflow_reported(lib_built):
+    # 40 unit boxes in a row: a ray along the row overlaps all of them
+    v0 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    f = np.array([[0, 1, 2]], np.uint32)
+    doms = [sg.Domain(v0 + [2 * i, 0, 0], f, bounds=[2 * i, 0, 0, 2 * i + 1, 1, 1]) for i in range(40)]
+    t = sg.Tracer(small_config(image_w=4, image_h=4))
+    t.set_scene(sg.Scene(doms, [sg.Light(0, (0, 5, 0))]))
+    t.set_camera((-5, 0.5, 0.5), (100, 0.5, 0.5), (0, 1, 0), 1.0)
+    with pytest.raises(sg.SprayError) as e:
+        t.trace()
+    assert e.value.code == sg.EOVERFLOW
+
+
+def test_scene_file_path(lib_built, oracle_mod, tmp_path):
+    p = scenes.write_wavelet_grid(tmp_path, grid=2, samples=16, colors="albedo", light="point")
+    sc = sg.Scene.load(p, p.parent)
+    cfg = small_config(ao_mode=0, pixel_samples=2, bounces=2)
+    t, img, st, o = run(cfg, sc, 2, oracle_mod)
+    wb, _ = o.render_wavefront()
+    assert np.array_equal(bits(img), bits(wb))
