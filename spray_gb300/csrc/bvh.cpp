@@ -176,14 +176,14 @@ struct Collapser {
     for (int c = 0; c < 4; ++c) {
       node.lox[c] = node.loy[c] = node.loz[c] = INFINITY;
       node.hix[c] = node.hiy[c] = node.hiz[c] = -INFINITY;
-      node.child[c] = 0;
+      node.child[c] = kEmptyChild;
       node.pad[c] = 0;
     }
     int child_ref[4];
     for (int c = 0; c < nk; ++c) {
       const BinNode& k = b.nodes[kids[c]];
       if (k.leaf()) {
-        if (k.count > (uint32_t)kMaxLeafTris || k.first >= (1u << 28))
+        if (k.count > (uint32_t)kMaxLeafTris || k.first >= (1u << 27))
           throw std::runtime_error("bvh: leaf does not fit the node encoding");
         child_ref[c] = ~(int32_t)((k.first << 3) | (k.count - 1));
       } else {
@@ -236,7 +236,7 @@ void buildBvh4(const float* vertices, const uint32_t* faces, uint32_t num_faces,
     for (int k = 0; k < 4; ++k) {
       node.lox[k] = node.loy[k] = node.loz[k] = INFINITY;
       node.hix[k] = node.hiy[k] = node.hiz[k] = -INFINITY;
-      node.child[k] = 0;
+      node.child[k] = kEmptyChild;
       node.pad[k] = 0;
     }
     const BinNode& k = b.nodes[root];

@@ -12,7 +12,7 @@ namespace spray {
 // One 128-byte node: child boxes in SoA form, then the child references.
 //   child >= 0 : index of an inner node (domain-relative)
 //   child <  0 : leaf, ~child = (first_triangle << 3) | (count - 1)
-// Unused child slots carry an empty box (lo = +inf, hi = -inf).
+//   child == kEmptyChild : unused slot, with an empty box (lo = +inf, hi = -inf)
 struct alignas(16) BvhNode4 {
   float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
   int32_t child[4];
@@ -21,6 +21,7 @@ struct alignas(16) BvhNode4 {
 static_assert(sizeof(BvhNode4) == 128, "node must be one 128-byte line");
 
 constexpr int kMaxLeafTris = 8;
+constexpr int32_t kEmptyChild = (int32_t)0x80000000;
 
 struct BvhBuildResult {
   std::vector<BvhNode4> nodes;     // nodes[0] is the root

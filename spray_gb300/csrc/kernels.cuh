@@ -41,7 +41,14 @@ struct DomainDev {
   int32_t bsdf;
   float bsdf_p[3];
   int32_t resident;        // 1 when the geometry is in device memory
+  int32_t num_nodes;       // BVH nodes of the domain
+  int32_t num_tris;        // triangles of the domain
 };
+
+// Bits of Counters::error_flags.
+constexpr unsigned long long kErrGlassBothLobes = 1ull;  // glass hit needing two rays
+constexpr unsigned long long kErrBadNode = 2ull;         // node or leaf index out of range
+constexpr unsigned long long kErrTraversalBound = 4ull;  // traversal exceeded its step bound
 
 struct SceneDev {
   const DomainDev* domains;

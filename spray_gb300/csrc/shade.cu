@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
               else {
                 // the reference aborts on a glass hit with both lobes; keep reflection
                 reflect = 1;
-                atomicOr((unsigned long long*)&a.ctr->error_flags, 1ull);
+                atomicOr((unsigned long long*)&a.ctr->error_flags, kErrGlassBothLobes);
               }
             } else {  // transmission
               float sin2ThetaI = fmax_ref(0.0f, 1.0f - (cos_theta_i * cos_theta_i));

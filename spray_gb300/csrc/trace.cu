@@ -23,6 +23,7 @@ constexpr int kStack = 64;
 
 struct TravRay {
   V3 org, dir, inv;
+  int sx, sy, sz;  // 1 when the direction component is negative
   RayShear sh;
 };
 
@@ -31,32 +32,36 @@ __device__ __forceinline__ TravRay makeTravRay(V3 org, V3 dir) {
   r.org = org;
   r.dir = dir;
   r.inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+  r.sx = r.inv.x < 0.0f;
+  r.sy = r.inv.y < 0.0f;
+  r.sz = r.inv.z < 0.0f;
   r.sh = makeShear(dir);
   return r;
 }
 
 // Intersects the four children of a node; returns a mask of hit children and
-// their entry distances.
+// their entry distances.  Near and far planes are picked by the direction's
+// sign, so an empty slot (lo = +inf, hi = -inf) can never be entered.
 __device__ __forceinline__ int testChildren(const BvhNode4* __restrict__ nodes, int node,
                                             const TravRay& r, float tnear, float tfar,
                                             float tn[4]) {
   const float4* p = reinterpret_cast<const float4*>(nodes + node);
-  float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
-  float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
-  const float lx[4] = {lox.x, lox.y, lox.z, lox.w}, hx[4] = {hix.x, hix.y, hix.z, hix.w};
-  const float ly[4] = {loy.x, loy.y, loy.z, loy.w}, hy[4] = {hiy.x, hiy.y, hiy.z, hiy.w};
-  const float lz[4] = {loz.x, loz.y, loz.z, loz.w}, hz[4] = {hiz.x, hiz.y, hiz.z, hiz.w};
+  const float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
+  const float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
+  const float4 nx = r.sx ? hix : lox, fx = r.sx ? lox : hix;
+  const float4 ny = r.sy ? hiy : loy, fy = r.sy ? loy : hiy;
+  const float4 nz = r.sz ? hiz : loz, fz = r.sz ? loz : hiz;
+  const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
+  const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
+  const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
   int mask = 0;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    float tx0 = (lx[c] - r.org.x) * r.inv.x, tx1 = (hx[c] - r.org.x) * r.inv.x;
-    float ty0 = (ly[c] - r.org.y) * r.inv.y, ty1 = (hy[c] - r.org.y) * r.inv.y;
-    float tz0 = (lz[c] - r.org.z) * r.inv.z, tz1 = (hz[c] - r.org.z) * r.inv.z;
-    float a0 = fminf(tx0, tx1), a1 = fmaxf(tx0, tx1);
-    float b0 = fminf(ty0, ty1), b1 = fmaxf(ty0, ty1);
-    float c0 = fminf(tz0, tz1), c1 = fmaxf(tz0, tz1);
-    float t0 = fmaxf(fmaxf(a0, b0), fmaxf(c0, tnear));
-    float t1 = fminf(fminf(a1, b1), fminf(c1, tfar)) * kBoxSlack;
+    float t0 = fmaxf(fmaxf((nxa[c] - r.org.x) * r.inv.x, (nya[c] - r.org.y) * r.inv.y),
+                     fmaxf((nza[c] - r.org.z) * r.inv.z, tnear));
+    float t1 = fminf(fminf((fxa[c] - r.org.x) * r.inv.x, (fya[c] - r.org.y) * r.inv.y),
+                     fminf((fza[c] - r.org.z) * r.inv.z, tfar)) *
+               kBoxSlack;
     tn[c] = t0;
     if (t0 <= t1) mask |= 1 << c;
   }
@@ -72,25 +77,41 @@ __device__ __forceinline__ int childAt(int4 c, int k) {
   return k == 0 ? c.x : (k == 1 ? c.y : (k == 2 ? c.z : c.w));
 }
 
+// Upper bound on node visits of one traversal; reaching it means a corrupt
+// hierarchy, which is reported through Counters::error_flags.
+constexpr int kMaxSteps = 1 << 20;
+
+__device__ __forceinline__ void raise(Counters* ctr, unsigned long long bit) {
+  atomicOr(&ctr->error_flags, bit);
+}
+
 // Closest hit in one domain.  best_key enters as the key to beat and leaves as
 // the best found; returns true when this domain improved it.
 __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const TravRay& r,
                                 uint64_t& best_key, float& best_t, uint32_t& best_prim,
-                                float& best_u, float& best_v) {
+                                float& best_u, float& best_v, Counters* ctr) {
   const BvhNode4* nodes = sc.nodes + dom.node_base;
   const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
   uint2 stack[kStack];
   int sp = 0;
   int node = 0;
   bool found = false;
-  while (true) {
+  for (int steps = 0;; ++steps) {
+    if (steps >= kMaxSteps) {
+      raise(ctr, kErrTraversalBound);
+      break;
+    }
+    if ((unsigned)node >= (unsigned)dom.num_nodes) {
+      raise(ctr, kErrBadNode);
+      break;
+    }
     float tn[4];
     int mask = testChildren(nodes, node, r, kRayEpsilon, best_t, tn);
     int4 ch = loadChildren(nodes, node);
     // order hit children near to far
     int ord[4], no = 0;
     for (int c = 0; c < 4; ++c)
-      if (mask & (1 << c)) {
+      if ((mask & (1 << c)) && childAt(ch, c) != kEmptyChild) {
         int j = no++;
         while (j > 0 && tn[ord[j - 1]] > tn[c]) {
           ord[j] = ord[j - 1];
@@ -106,6 +127,10 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
         if (tn[c] > best_t) continue;
         uint32_t v = ~(uint32_t)ref;
         uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+        if (first + cnt > (uint32_t)dom.num_tris) {
+          raise(ctr, kErrBadNode);
+          continue;
+        }
         for (uint32_t q = 0; q < cnt; ++q) {
           const float4* tp = tris + 3 * (size_t)(first + q);
           float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
@@ -148,22 +173,36 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
 }
 
 // Any hit in (tnear, tfar) in one domain.
-__device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar) {
+__device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar,
+                            Counters* ctr) {
   const BvhNode4* nodes = sc.nodes + dom.node_base;
   const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
   int stack[kStack];
   int sp = 0;
   int node = 0;
-  while (true) {
+  for (int steps = 0;; ++steps) {
+    if (steps >= kMaxSteps) {
+      raise(ctr, kErrTraversalBound);
+      return false;
+    }
+    if ((unsigned)node >= (unsigned)dom.num_nodes) {
+      raise(ctr, kErrBadNode);
+      return false;
+    }
     float tn[4];
     int mask = testChildren(nodes, node, r, kRayEpsilon, tfar, tn);
     int4 ch = loadChildren(nodes, node);
     for (int c = 0; c < 4; ++c) {
       if (!(mask & (1 << c))) continue;
       int ref = childAt(ch, c);
+      if (ref == kEmptyChild) continue;
       if (ref < 0) {
         uint32_t v = ~(uint32_t)ref;
         uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+        if (first + cnt > (uint32_t)dom.num_tris) {
+          raise(ctr, kErrBadNode);
+          continue;
+        }
         for (uint32_t q = 0; q < cnt; ++q) {
           const float4* tp = tris + 3 * (size_t)(first + q);
           float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
@@ -233,7 +272,7 @@ __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
     TravRay r = makeTravRay(v3(o.x, o.y, o.z), v3(dd.x, dd.y, dd.z));
     uint32_t prim = 0;
     float u = 0.f, v = 0.f;
-    if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v)) {
+    if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v, a.ctr)) {
       atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
       const uint32_t* f = a.scene.faces + 3 * ((size_t)dom.face_base + prim);
       uint32_t i0 = dom.vert_base + f[0], i1 = dom.vert_base + f[1], i2 = dom.vert_base + f[2];
@@ -304,7 +343,7 @@ __global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
     const float4 hp = a.sh.hitpos[ray / a.slots];
     const float4 dd = a.sh.dir[ray];
     TravRay r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
-    if (traverseAny(a.scene, dom, r, dd.w)) a.sh.occluded[ray] = 1;
+    if (traverseAny(a.scene, dom, r, dd.w, a.ctr)) a.sh.occluded[ray] = 1;
   }
   for (int o = 16; o; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
   if (lane == 0 && visits) atomicAdd(&a.ctr->visits_shadow, visits);

@@ -290,6 +290,8 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
     dd.bsdf = doms[d].bsdf_type;
     for (int c = 0; c < 3; ++c) dd.bsdf_p[c] = doms[d].bsdf_params[c];
     dd.resident = 1;
+    dd.num_nodes = (int32_t)packs[d].nodes.size();
+    dd.num_tris = (int32_t)packs[d].nf;
     nn += packs[d].nodes.size();
     nt += (size_t)packs[d].nf;
     nvv += (size_t)packs[d].nv;
@@ -630,6 +632,8 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       continue;  // retrace with larger queues
     }
     if (ctr.list_overflows) throw OverflowError("a ray overlapped more than 32 domains");
+    if (ctr.error_flags & (kErrBadNode | kErrTraversalBound))
+      throw std::runtime_error("BVH traversal left its bounds (corrupt hierarchy)");
     size_t img_bytes = (size_t)cfg.image_w * cfg.image_h * sizeof(float4);
     if (out) {
       if (out_is_device) {
