@@ -1,0 +1,332 @@
+"""Benchmark of the speculative domain-parallel tracer (one frame = one step).
+
+Default workload (the configuration the headline metric is quoted on): the
+64-domain wavelet grid (4x4x4 cells, 64^3 isosurfaces), path tracing,
+1920x1080, 16 spp, 5 bounces with Russian roulette from bounce 3, per-domain
+albedo, one emissive quad light, seeded orbit camera.  Prints one JSON line.
+
+  value      Mrays/s of all logical rays (primary + shadow + bounce), frames
+             timed with CUDA events on the tracer's stream, scene resident
+  e2e        the same metric through spray_gpu_trace with the image copied to
+             pinned host memory every frame (wall clock around the C ABI call)
+  roofline   closest-hit traversal kernel: algorithmic bytes / kernel time
+  cpu_baseline  the CPU restatement of the reference loop (speculative queues,
+             DomainStats order, VBuf history) on a downscaled frame, all cores
+
+--impl reference times that CPU restatement alone on the same workload (the
+reference binary itself needs Embree 2.17, glm, glog and MPI, which are not
+available), rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s at <=1e-3 image RMSE, learned vs plain scheduler; domain loads/frame"
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
+
+
+def workload(name: str):
+    from spray_gb300 import scenes
+    spec = scenes.CONFIGS[name]
+    cfg = dict(spec["cfg"])
+    ext = dict(spec["ext"])
+    diag = scenes.scene_diagonal(spec["grid"])
+    if "ao_max_distance_frac" in ext:
+        cfg["ao_max_distance"] = ext.pop("ao_max_distance_frac") * diag
+    cfg.update({k: v for k, v in ext.items() if k != "cache_bytes"})
+    return spec, cfg
+
+
+def describe(name: str, spec: dict, cfg: dict) -> str:
+    g = spec["grid"]
+    mode = "AO" if cfg.get("ao_mode") else "path tracing"
+    return (f"{name}: {g}x{g}x{g} wavelet domains ({spec['samples']}^3 isosurfaces), {mode}, "
+            f"{cfg['image_w']}x{cfg['image_h']}, {cfg['pixel_samples']} spp, {cfg['bounces']} bounces")
+
+
+def clock_sampler(out: Path):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(out, "w")
+        return subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                 "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL), f
+    except Exception:
+        return None, None
+
+
+def clock_summary(path: Path, device: int) -> dict | None:
+    try:
+        rows = [l.split(",") for l in path.read_text().splitlines() if l.strip()]
+    except Exception:
+        return None
+    rows = [[c.strip() for c in r] for r in rows if len(r) >= 9 and r[0].strip() == str(device)]
+    if not rows:
+        return None
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons, "samples": len(rows)}
+
+
+def hbm_peak():
+    try:
+        d = json.loads(MEASURED_PEAKS.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def load_profile_traffic(name: str):
+    """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / f"trace_closest_{name}.json"
+    try:
+        d = json.loads(p.read_text())
+        return d
+    except Exception:
+        return None
+
+
+def cpu_speculative(name, spec, cfg, threads: int, scale: int, frame: int = 0):
+    """The reference loop restated on the CPU, on a frame downscaled by `scale`."""
+    from oracle import oracle as O
+    from spray_gb300 import scenes
+    import spray_gb300 as sg
+    path, _ = scenes.benchmark_scene(name)
+    scene = sg.Scene.load(path, path.parent)
+    c = dict(cfg)
+    c["image_w"] = max(8, cfg["image_w"] // scale)
+    c["image_h"] = max(8, cfg["image_h"] // scale)
+    c.setdefault("history_size", 4)
+    c.setdefault("list_size", 16)
+    c.setdefault("cache_size", -1)
+    c.setdefault("max_samples_per_rank", 1 << 20)
+    c.setdefault("num_ranks", 1)
+    c.setdefault("rank", 0)
+    o = O.Oracle(c, scene)
+    o.set_camera(*scenes.orbit_camera(spec["grid"], frame=frame))
+    t0 = time.perf_counter()
+    img, st = o.render_speculative(threads)
+    dt = time.perf_counter() - t0
+    rays = st["rays_primary"] + st["rays_shadow"] + st["rays_bounce"]
+    return rays, dt, c, st
+
+
+def run_reference(args, spec, cfg, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    scale = args.cpu_scale
+    for _ in range(args.warmup):
+        cpu_speculative(args.config, spec, cfg, threads, scale)
+    rays_t, secs = 0, 0.0
+    st_last = None
+    for k in range(args.steps):
+        rays, dt, c, st = cpu_speculative(args.config, spec, cfg, threads, scale)
+        rays_t += rays
+        secs += dt
+        st_last = st
+    v = rays_t / secs / 1e6
+    sample = (f"{c['image_w']}x{c['image_h']} frame of the same scene, camera, spp and bounces "
+              f"(1/{scale} of each image dimension), speculative loop with {threads} OpenMP threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": describe(args.config, spec, cfg)},
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "domain_loads_per_frame": st_last["domain_loads"] if st_last else None,
+        "note": "reference binary unbuildable here (Embree 2.17, glm, glog, MPI absent); "
+                "timed the CPU restatement of its speculative loop",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--cpu-scale", type=int, default=2, help="CPU baseline frame downscale per axis")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-flush", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    spec, cfg = workload(args.config)
+
+    if args.impl == "reference":
+        run_reference(args, spec, cfg, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    import spray_gb300 as sg
+    from spray_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def allmax(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def allsum(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    if rank == 0:
+        scenes.benchmark_scene(args.config)
+    barrier()
+    path, _ = scenes.benchmark_scene(args.config)
+    scene = sg.Scene.load(path, path.parent)
+    tracer = sg.Tracer(cfg, device=local)
+    tracer.set_scene(scene)
+    # weak scaling: each rank renders its own seeded view of the scene
+    tracer.set_camera(*scenes.orbit_camera(spec["grid"], frame=rank))
+    W, H = cfg["image_w"], cfg["image_h"]
+    img_dev = torch.empty(H * W * 4, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MiB > 129 MB L2
+
+    def frame_device():
+        if not args.no_flush:
+            flush.fill_(1)
+            torch.cuda.synchronize()
+        return tracer.trace_device(img_dev.data_ptr())
+
+    for _ in range(args.warmup):
+        frame_device()
+
+    clk_path = ROOT / "gpurun_out" / f"clocks_rank{rank}.csv"
+    clk_path.parent.mkdir(exist_ok=True)
+    proc, fh = clock_sampler(clk_path)
+    barrier()
+    torch.cuda.synchronize()
+    stats = [frame_device() for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+
+    rays = sum(s["rays_primary"] + s["rays_shadow"] + s["rays_bounce"] for s in stats)
+    dev_ms = sum(s["frame_ms"] for s in stats)
+    t_max = allmax(dev_ms)
+    rays_all = allsum(rays)
+    value = rays_all / (t_max * 1e-3) / 1e6
+
+    # end to end through the C ABI: image to pinned host memory every frame
+    host = torch.empty(H * W * 4, dtype=torch.float32, pin_memory=True)
+    host_np = host.numpy().reshape(H, W, 4)
+    e2e_rays, e2e_s, h2d, d2h = 0, 0.0, 0, 0
+    barrier()
+    for _ in range(args.steps):
+        if not args.no_flush:
+            flush.fill_(1)
+            torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, st = tracer.trace(host_np)
+        e2e_s += time.perf_counter() - t0
+        e2e_rays += st["rays_primary"] + st["rays_shadow"] + st["rays_bounce"]
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+    barrier()
+    e2e_value = allsum(e2e_rays) / allmax(e2e_s) / 1e6
+    if proc is not None:
+        proc.terminate()
+        proc.wait()
+        fh.close()
+    clocks = clock_summary(clk_path, local)
+
+    s0 = stats[-1]
+    peak, peak_kind = hbm_peak()
+    trace_bytes = (s0["visits_radiance"] * (RAY_BYTES + ENTRY_BYTES + HIT_BYTES)
+                   + s0["nodes_radiance"] * NODE_BYTES + s0["tris_radiance"] * TRI_BYTES)
+    occl_bytes = (s0["visits_shadow"] * (RAY_BYTES + ENTRY_BYTES)
+                  + s0["nodes_shadow"] * NODE_BYTES + s0["tris_shadow"] * TRI_BYTES)
+    if s0["trace_ms"] >= s0["occlude_ms"]:
+        kname, kbytes, kms, klaunch = "closest-hit traversal", trace_bytes, s0["trace_ms"], s0["trace_launches"]
+    else:
+        kname, kbytes, kms, klaunch = "occlusion traversal", occl_bytes, s0["occlude_ms"], s0["occlude_launches"]
+    achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
+    prof = load_profile_traffic(args.config)
+    traffic = None
+    if prof and prof.get("kernel") == kname:
+        traffic = prof.get("dram_bytes_per_frame")
+
+    nrays = s0["rays_primary"] + s0["rays_shadow"] + s0["rays_bounce"]
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": allmax(dev_ms / args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded wavelet isosurface scene, seeded orbit camera)",
+        "config": {"workload": describe(args.config, spec, cfg), "scheduler": "plain speculative",
+                   "domains": len(scene.domains), "triangles": s0["scene_triangles"],
+                   "image": [W, H], "spp": cfg["pixel_samples"], "bounces": cfg["bounces"],
+                   "l2": "256 MiB buffer written before every timed frame; ray state > L2",
+                   "parallelism": f"replicas x{world} (one view per GPU)"},
+        "rays_per_frame": {"primary": s0["rays_primary"], "shadow": s0["rays_shadow"],
+                           "bounce": s0["rays_bounce"]},
+        "mrays_per_s_by_class": {k: s0[f"rays_{k}"] / (s0["frame_ms"] * 1e-3) / 1e6
+                                 for k in ("primary", "shadow", "bounce")},
+        "visits_per_ray": (s0["visits_radiance"] + s0["visits_shadow"]) / max(nrays, 1),
+        "visits_culled": s0["visits_culled"],
+        "domain_loads_per_frame": s0["domain_loads"],
+        "h2d_bytes_per_frame": s0["h2d_bytes"],
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_frame": kbytes,
+                     "launches_per_frame": klaunch, "kernel_ms_per_frame": kms},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r, dt, c, _ = cpu_speculative(args.config, spec, cfg, threads, args.cpu_scale)
+        out["cpu_baseline"] = {
+            "value": r / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{c['image_w']}x{c['image_h']} frame (1/{args.cpu_scale} per axis), same scene, "
+                      f"camera, spp and bounces; speculative loop, {threads} OpenMP threads"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

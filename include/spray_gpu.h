@@ -120,6 +120,12 @@ typedef struct spray_gpu_stats {
   double schedule_ms;       /* device time inside the scheduling kernels */
   int64_t trace_launches;
   int64_t occlude_launches;
+  int64_t nodes_radiance;   /* BVH nodes fetched by closest-hit traversal */
+  int64_t tris_radiance;    /* triangles tested by closest-hit traversal */
+  int64_t nodes_shadow;     /* BVH nodes fetched by occlusion traversal */
+  int64_t tris_shadow;      /* triangles tested by occlusion traversal */
+  int64_t scene_triangles;  /* triangles in the scene */
+  int64_t scene_bytes;      /* device bytes of BVH nodes, triangles and shading data */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

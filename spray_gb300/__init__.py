@@ -62,6 +62,8 @@ class StatsC(C.Structure):
         ("kernel_launches", C.c_int64), ("list_overflows", C.c_int64), ("frame_ms", C.c_double),
         ("trace_ms", C.c_double), ("occlude_ms", C.c_double), ("schedule_ms", C.c_double),
         ("trace_launches", C.c_int64), ("occlude_launches", C.c_int64),
+        ("nodes_radiance", C.c_int64), ("tris_radiance", C.c_int64), ("nodes_shadow", C.c_int64),
+        ("tris_shadow", C.c_int64), ("scene_triangles", C.c_int64), ("scene_bytes", C.c_int64),
     ]
 
     def asdict(self) -> dict:

@@ -71,6 +71,10 @@ struct Counters {
   unsigned long long arena_overflows;
   unsigned long long entry_overflows;
   unsigned long long error_flags;
+  unsigned long long nodes_radiance;  // BVH nodes fetched by closest-hit traversal
+  unsigned long long tris_radiance;   // triangles tested by closest-hit traversal
+  unsigned long long nodes_shadow;
+  unsigned long long tris_shadow;
 };
 
 // Radiance rays of a wave, indexed by sample.
@@ -136,6 +140,7 @@ struct TraceArgs {
   const uint32_t* key_start;
   int nkeys;
   unsigned int* work;         // work-stealing counter (zeroed before launch)
+  int bucket;                 // depth bucket to trace (-1 = every entry)
   RayBuf rays;
   ShadowBuf sh;
   int slots;

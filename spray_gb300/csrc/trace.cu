@@ -89,7 +89,8 @@ __device__ __forceinline__ void raise(Counters* ctr, unsigned long long bit) {
 // the best found; returns true when this domain improved it.
 __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const TravRay& r,
                                 uint64_t& best_key, float& best_t, uint32_t& best_prim,
-                                float& best_u, float& best_v, Counters* ctr) {
+                                float& best_u, float& best_v, Counters* ctr,
+                                unsigned long long& nnodes, unsigned long long& ntris) {
   const BvhNode4* nodes = sc.nodes + dom.node_base;
   const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
   uint2 stack[kStack];
@@ -106,6 +107,7 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
       break;
     }
     float tn[4];
+    ++nnodes;
     int mask = testChildren(nodes, node, r, kRayEpsilon, best_t, tn);
     int4 ch = loadChildren(nodes, node);
     // order hit children near to far
@@ -131,6 +133,7 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
           raise(ctr, kErrBadNode);
           continue;
         }
+        ntris += cnt;
         for (uint32_t q = 0; q < cnt; ++q) {
           const float4* tp = tris + 3 * (size_t)(first + q);
           float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
@@ -174,7 +177,7 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
 
 // Any hit in (tnear, tfar) in one domain.
 __device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar,
-                            Counters* ctr) {
+                            Counters* ctr, unsigned long long& nnodes, unsigned long long& ntris) {
   const BvhNode4* nodes = sc.nodes + dom.node_base;
   const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
   int stack[kStack];
@@ -190,6 +193,7 @@ __device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const Trav
       return false;
     }
     float tn[4];
+    ++nnodes;
     int mask = testChildren(nodes, node, r, kRayEpsilon, tfar, tn);
     int4 ch = loadChildren(nodes, node);
     for (int c = 0; c < 4; ++c) {
@@ -203,6 +207,7 @@ __device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const Trav
           raise(ctr, kErrBadNode);
           continue;
         }
+        ntris += cnt;
         for (uint32_t q = 0; q < cnt; ++q) {
           const float4* tp = tris + 3 * (size_t)(first + q);
           float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
@@ -238,12 +243,16 @@ __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
   const int D = a.scene.num_domains;
   for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
   __syncthreads();
-  const uint32_t E = *a.num_entries;
+  uint32_t E0 = 0, E = *a.num_entries;
+  if (a.bucket >= 0 && E > 0) {
+    E0 = skeys[a.bucket * D];
+    E = a.bucket + 1 < kDepthBuckets ? skeys[(a.bucket + 1) * D] : skeys[a.nkeys];
+  }
   const int lane = threadIdx.x & 31;
-  unsigned long long visits = 0, culled = 0;
+  unsigned long long visits = 0, culled = 0, nnodes = 0, ntris = 0;
   while (true) {
     uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(a.work, 32u);
+    if (lane == 0) base = E0 + atomicAdd(a.work, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= E) break;
     const uint32_t e = base + lane;
@@ -272,7 +281,7 @@ __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
     TravRay r = makeTravRay(v3(o.x, o.y, o.z), v3(dd.x, dd.y, dd.z));
     uint32_t prim = 0;
     float u = 0.f, v = 0.f;
-    if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v, a.ctr)) {
+    if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v, a.ctr, nnodes, ntris)) {
       atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
       const uint32_t* f = a.scene.faces + 3 * ((size_t)dom.face_base + prim);
       uint32_t i0 = dom.vert_base + f[0], i1 = dom.vert_base + f[1], i2 = dom.vert_base + f[2];
@@ -291,10 +300,14 @@ __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
   for (int o = 16; o; o >>= 1) {
     visits += __shfl_down_sync(0xffffffffu, visits, o);
     culled += __shfl_down_sync(0xffffffffu, culled, o);
+    nnodes += __shfl_down_sync(0xffffffffu, nnodes, o);
+    ntris += __shfl_down_sync(0xffffffffu, ntris, o);
   }
   if (lane == 0) {
     if (visits) atomicAdd(&a.ctr->visits_radiance, visits);
     if (culled) atomicAdd(&a.ctr->visits_culled, culled);
+    if (nnodes) atomicAdd(&a.ctr->nodes_radiance, nnodes);
+    if (ntris) atomicAdd(&a.ctr->tris_radiance, ntris);
   }
 }
 
@@ -326,7 +339,7 @@ __global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
   __syncthreads();
   const uint32_t E = *a.num_entries;
   const int lane = threadIdx.x & 31;
-  unsigned long long visits = 0;
+  unsigned long long visits = 0, nnodes = 0, ntris = 0;
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(a.work, 32u);
@@ -343,10 +356,18 @@ __global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
     const float4 hp = a.sh.hitpos[ray / a.slots];
     const float4 dd = a.sh.dir[ray];
     TravRay r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
-    if (traverseAny(a.scene, dom, r, dd.w, a.ctr)) a.sh.occluded[ray] = 1;
+    if (traverseAny(a.scene, dom, r, dd.w, a.ctr, nnodes, ntris)) a.sh.occluded[ray] = 1;
   }
-  for (int o = 16; o; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
-  if (lane == 0 && visits) atomicAdd(&a.ctr->visits_shadow, visits);
+  for (int o = 16; o; o >>= 1) {
+    visits += __shfl_down_sync(0xffffffffu, visits, o);
+    nnodes += __shfl_down_sync(0xffffffffu, nnodes, o);
+    ntris += __shfl_down_sync(0xffffffffu, ntris, o);
+  }
+  if (lane == 0) {
+    if (visits) atomicAdd(&a.ctr->visits_shadow, visits);
+    if (nnodes) atomicAdd(&a.ctr->nodes_shadow, nnodes);
+    if (ntris) atomicAdd(&a.ctr->tris_shadow, ntris);
+  }
 }
 
 void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {

@@ -302,6 +302,7 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   }
   if (max_bvh_depth * 3 + 4 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
   total_tris = nt;
+  scene_bytes = nn * sizeof(BvhNode4) + 3 * nt * sizeof(float4) + 3 * nt * 4 + nvv * 4 + 3 * nvv * 4;
   devAlloc(&d_domains, nd);
   devAlloc(&d_nodes, nn);
   devAlloc(&d_tris, 3 * nt);
@@ -416,7 +417,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_num_entries, 1);
   devAlloc(&d_rec_key, E);
   devAlloc(&d_rec_attr, E);
-  devAlloc(&d_work, 1);
+  devAlloc(&d_work, kDepthBuckets);
   compact_blocks = num_sms * 4;
   devAlloc(&d_block_tmp, compact_blocks);
   devAlloc(&d_image, (size_t)cfg.image_w * cfg.image_h);
@@ -464,6 +465,7 @@ TraceArgs Tracer::traceArgs(int order_by_depth, int S) {
   t.key_start = d_key_start;
   t.nkeys = order_by_depth ? kDepthBuckets * D : D;
   t.work = d_work;
+  t.bucket = -1;
   t.rays = rays[cur];
   t.sh = sh;
   t.slots = S;
@@ -532,15 +534,22 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       captureQueues(SPRAY_DBG_RQUEUES, b, order_by_depth);
       captureScores(b);
     }
-    CK(cudaMemsetAsync(d_work, 0, 4, stream));
+    // closest hits; with culling, one launch per depth bucket so that every
+    // entry sees the hits of all nearer domain lists (front-to-back waves)
+    CK(cudaMemsetAsync(d_work, 0, 4 * kDepthBuckets, stream));
     TraceArgs ta = traceArgs(order_by_depth, S);
-    cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
-    CK(cudaEventRecord(t0, stream));
-    launchTraceClosest(stream, ta, num_sms * 8);
-    CK(cudaEventRecord(t1, stream));
-    trace_events.push_back({t0, t1});
+    const int nb = order_by_depth ? kDepthBuckets : 1;
+    for (int k = 0; k < nb; ++k) {
+      ta.bucket = order_by_depth ? k : -1;
+      ta.work = d_work + k;
+      cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
+      CK(cudaEventRecord(t0, stream));
+      launchTraceClosest(stream, ta, num_sms * 8);
+      CK(cudaEventRecord(t1, stream));
+      trace_events.push_back({t0, t1});
+    }
     launchResolve(stream, ta, d_hit_ns, nblk);
-    launches += 3;
+    launches += 2 + nb;
     if (capture) captureHits(b);
     // shade
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
@@ -673,6 +682,12 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->schedule_ms = sum(sched_events);
       st->trace_launches = (int64_t)trace_events.size();
       st->occlude_launches = (int64_t)occl_events.size();
+      st->nodes_radiance = (int64_t)ctr.nodes_radiance;
+      st->tris_radiance = (int64_t)ctr.tris_radiance;
+      st->nodes_shadow = (int64_t)ctr.nodes_shadow;
+      st->tris_shadow = (int64_t)ctr.tris_shadow;
+      st->scene_triangles = (int64_t)total_tris;
+      st->scene_bytes = (int64_t)scene_bytes;
     }
     return;
   }

@@ -89,6 +89,7 @@ class Tracer {
   int D = 0;
   int max_bvh_depth = 0;
   size_t total_tris = 0;
+  size_t scene_bytes = 0;
   std::vector<DomainDev> hdoms;
   std::vector<spray_gpu_light> lights;
   DomainDev* d_domains = nullptr;

