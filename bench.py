@@ -40,14 +40,14 @@ FALLBACK_HBM_GBS = 6800.0
 NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
 
 
-def workload(name: str):
+def workload(name: str, scene=None):
     from spray_gb300 import scenes
     spec = scenes.CONFIGS[name]
     cfg = dict(spec["cfg"])
     ext = dict(spec["ext"])
-    diag = scenes.scene_diagonal(spec["grid"])
-    if "ao_max_distance_frac" in ext:
-        cfg["ao_max_distance"] = ext.pop("ao_max_distance_frac") * diag
+    frac = ext.pop("ao_max_distance_frac", None)
+    if frac is not None and scene is not None:
+        cfg["ao_max_distance"] = frac * scenes.scene_diagonal(scene)
     cfg.update({k: v for k, v in ext.items() if k != "cache_bytes"})
     return spec, cfg
 
@@ -122,7 +122,7 @@ def cpu_speculative(name, spec, cfg, threads: int, scale: int, frame: int = 0):
     c.setdefault("num_ranks", 1)
     c.setdefault("rank", 0)
     o = O.Oracle(c, scene)
-    o.set_camera(*scenes.orbit_camera(spec["grid"], frame=frame))
+    o.set_camera(*scenes.orbit_camera(scene, frame=frame))
     t0 = time.perf_counter()
     img, st = o.render_speculative(threads)
     dt = time.perf_counter() - t0
@@ -179,10 +179,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    spec, cfg = workload(args.config)
 
     if args.impl == "reference":
-        run_reference(args, spec, cfg, rank)
+        if rank == 0:
+            import spray_gb300 as sg
+            from spray_gb300 import scenes
+            path, _ = scenes.benchmark_scene(args.config)
+            spec, cfg = workload(args.config, sg.Scene.load(path, path.parent))
+            run_reference(args, spec, cfg, rank)
         return
 
     import torch
@@ -217,10 +221,11 @@ def main():
     barrier()
     path, _ = scenes.benchmark_scene(args.config)
     scene = sg.Scene.load(path, path.parent)
+    spec, cfg = workload(args.config, scene)
     tracer = sg.Tracer(cfg, device=local)
     tracer.set_scene(scene)
     # weak scaling: each rank renders its own seeded view of the scene
-    tracer.set_camera(*scenes.orbit_camera(spec["grid"], frame=rank))
+    tracer.set_camera(*scenes.orbit_camera(scene, frame=rank))
     W, H = cfg["image_w"], cfg["image_h"]
     img_dev = torch.empty(H * W * 4, dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MiB > 129 MB L2

@@ -3,9 +3,10 @@
 The benchmark scenes are grids of domains, each the wavelet isosurface
 f = 255 exp(-(x^2+y^2+z^2)/(2*0.5^2)) + 10 sin(60x+p0) + 18 sin(30y+p1)
     + 5 cos(40z+p2) = 157
-on [-1,1]^3, translated into its cell of a g^3 grid with cell size 2, as the
-reference's example scene places 64 copies of one wavelet mesh
-(examples/wavelets64/wavelets64.spray).  Domain bounds are the object-space
+on [-1,1]^3, translated into its cell of a g^3 grid whose cell size is the
+largest domain extent, as the reference's example scene packs 64 copies of one
+wavelet mesh at its bounding-box size (examples/wavelets64/wavelets64.spray:
+bound -10..10, translate steps of 20), so neighbouring domain boxes touch.  Domain bounds are the object-space
 AABB of the vertices, as ply_header_reader computes them
 (src/apps/ply_header_reader.cc:86-103).  Colours are per-vertex uchar RGB
 because the reference shades with vertex colour, not the mtl albedo
@@ -70,7 +71,7 @@ def domain_phases(n: int, seed: int | None) -> np.ndarray:
     return np.random.default_rng(seed).uniform(0.0, 2.0 * math.pi, size=(n, 3))
 
 
-def grid_translations(grid: int, cell: float = 2.0) -> np.ndarray:
+def grid_translations(grid: int, cell: float) -> np.ndarray:
     """Domain d = i + g*j + g*g*k sits at cell (i, j, k)."""
     t = []
     for k in range(grid):
@@ -80,14 +81,27 @@ def grid_translations(grid: int, cell: float = 2.0) -> np.ndarray:
     return np.asarray(t, np.float32)
 
 
-def scene_bounds(grid: int, cell: float = 2.0):
-    lo = np.array([-1.0, -1.0, -1.0])
-    hi = lo + cell * grid
-    return lo, hi
+def domain_meshes(grid: int, samples: int, phase_seed: int | None):
+    """Per-domain object-space meshes and the grid cell size (largest extent)."""
+    n = grid ** 3
+    phases = domain_phases(n, phase_seed)
+    if phase_seed is None:
+        base = generate_wavelet(samples, 157.0, (0.0, 0.0, 0.0))
+        meshes = [base] * n
+    else:
+        meshes = [generate_wavelet(samples, 157.0, tuple(phases[d])) for d in range(n)]
+    cell = max(float((v.max(0) - v.min(0)).max()) for v, _ in meshes[: (1 if phase_seed is None else n)])
+    cell = float(np.float32(cell))
+    return meshes, cell
 
 
-def make_lights(kind: str, grid: int, cell: float = 2.0) -> list[Light]:
-    lo, hi = scene_bounds(grid, cell)
+def scene_box(scene: Scene):
+    b = np.array([d.bounds for d in scene.domains], np.float64)
+    return b[:, :3].min(0), b[:, 3:].max(0)
+
+
+def make_lights(kind: str, lo, hi) -> list[Light]:
+    lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
     c = 0.5 * (lo + hi)
     ext = hi - lo
     if kind == "point":
@@ -105,9 +119,9 @@ def make_lights(kind: str, grid: int, cell: float = 2.0) -> list[Light]:
     raise ValueError(kind)
 
 
-def orbit_camera(grid: int, seed: int = CAMERA_SEED, frame: int = 0, cell: float = 2.0):
+def orbit_camera(scene: Scene, seed: int = CAMERA_SEED, frame: int = 0):
     """Pinhole on a seeded orbit around the scene centre, radius 1.2 x diagonal."""
-    lo, hi = scene_bounds(grid, cell)
+    lo, hi = scene_box(scene)
     c = 0.5 * (lo + hi)
     diag = float(np.linalg.norm(hi - lo))
     rng = np.random.default_rng(seed + 7919 * frame)
@@ -119,37 +133,33 @@ def orbit_camera(grid: int, seed: int = CAMERA_SEED, frame: int = 0, cell: float
     return pos.astype(np.float32), c.astype(np.float32), np.array([0, 1, 0], np.float32)
 
 
-def scene_diagonal(grid: int, cell: float = 2.0) -> float:
-    lo, hi = scene_bounds(grid, cell)
+def scene_diagonal(scene: Scene) -> float:
+    lo, hi = scene_box(scene)
     return float(np.linalg.norm(hi - lo))
 
 
 def wavelet_grid(grid: int = 4, samples: int = 64, colors: str = "grey", light: str = "point",
-                 phase_seed: int | None = None, cell: float = 2.0) -> Scene:
+                 phase_seed: int | None = None) -> Scene:
     """In-memory scene: the same domains the .spray writer produces."""
     n = grid ** 3
+    meshes, cell = domain_meshes(grid, samples, phase_seed)
     trans = grid_translations(grid, cell)
-    phases = domain_phases(n, phase_seed)
     alb = domain_albedo(n) if colors == "albedo" else None
-    base = None
     domains = []
     for d in range(n):
-        if phase_seed is None:
-            if base is None:
-                base = generate_wavelet(samples, 157.0, (0.0, 0.0, 0.0))
-            v, f = base
-        else:
-            v, f = generate_wavelet(samples, 157.0, tuple(phases[d]))
+        v, f = meshes[d]
         col = _color(alb[d]) if alb is not None else _color((GREY, GREY, GREY))
         obj_lo, obj_hi = v.min(0), v.max(0)
         wv = (v + trans[d]).astype(np.float32)  # one float add per coordinate, as the loader does
         bounds = np.concatenate([obj_lo + trans[d], obj_hi + trans[d]]).astype(np.float32)
         domains.append(Domain(wv, f, np.full(len(v), col, np.uint32), bounds))
-    return Scene(domains, make_lights(light, grid, cell))
+    sc = Scene(domains, [])
+    sc.lights = make_lights(light, *scene_box(sc))
+    return sc
 
 
 def write_wavelet_grid(out_dir: Path, grid: int = 4, samples: int = 64, colors: str = "grey",
-                       light: str = "point", phase_seed: int | None = None, cell: float = 2.0) -> Path:
+                       light: str = "point", phase_seed: int | None = None) -> Path:
     """Writes PLY files and a .spray scene file; returns the .spray path."""
     out_dir = Path(out_dir)
     out_dir.mkdir(parents=True, exist_ok=True)
@@ -157,11 +167,13 @@ def write_wavelet_grid(out_dir: Path, grid: int = 4, samples: int = 64, colors: 
     if spray.exists():
         return spray
     n = grid ** 3
+    meshes, cell = domain_meshes(grid, samples, phase_seed)
     trans = grid_translations(grid, cell)
-    phases = domain_phases(n, phase_seed)
     alb = domain_albedo(n) if colors == "albedo" else None
+    lo = np.min([meshes[d][0].min(0) + trans[d] for d in range(n)], axis=0)
+    hi = np.max([meshes[d][0].max(0) + trans[d] for d in range(n)], axis=0)
     lines = []
-    for l in make_lights(light, grid, cell):
+    for l in make_lights(light, lo, hi):
         if l.type == Light.POINT:
             lines.append("light point %.9g %.9g %.9g %.9g %.9g %.9g" % (*l.position, *l.radiance))
         elif l.type == Light.DIFFUSE:
@@ -169,24 +181,18 @@ def write_wavelet_grid(out_dir: Path, grid: int = 4, samples: int = 64, colors: 
         else:
             lines.append("light quad " + " ".join("%.9g" % x for x in (*l.position, *l.edge1, *l.edge2,
                                                                       *l.radiance)))
-    base = None
     written = {}
     for d in range(n):
-        if phase_seed is None:
-            if base is None:
-                base = generate_wavelet(samples, 157.0, (0.0, 0.0, 0.0))
-            v, f = base
-        else:
-            v, f = generate_wavelet(samples, 157.0, tuple(phases[d]))
+        v, f = meshes[d]
         col = _color(alb[d]) if alb is not None else _color((GREY, GREY, GREY))
         key = (d if phase_seed is not None else -1, col)
         if key not in written:
             name = f"wavelet_{d:04d}.ply"
             write_ply(out_dir / name, v, f, np.full(len(v), col, np.uint32))
             written[key] = (name, v.min(0), v.max(0), len(v), len(f))
-        name, lo, hi, nv, nf = written[key]
+        name, blo, bhi, nv, nf = written[key]
         lines += ["", f"# domain {d}", "domain", f"file {name}", "mtl diffuse 1 1 1",
-                  "bound %.9g %.9g %.9g %.9g %.9g %.9g" % (*lo, *hi), f"face {nf}", f"vertex {nv}",
+                  "bound %.9g %.9g %.9g %.9g %.9g %.9g" % (*blo, *bhi), f"face {nf}", f"vertex {nv}",
                   "translate %.9g %.9g %.9g" % tuple(trans[d])]
     tmp = spray.with_suffix(".tmp")
     tmp.write_text("\n".join(lines) + "\n")
@@ -197,7 +203,7 @@ def write_wavelet_grid(out_dir: Path, grid: int = 4, samples: int = 64, colors: 
 def benchmark_scene(name: str) -> tuple[Path, dict]:
     """Generates (once) and returns the .spray file of a benchmark workload."""
     spec = CONFIGS[name]
-    d = SCENE_CACHE / f"{name}_g{spec['grid']}_s{spec['samples']}_{spec['colors']}_{spec['light']}"
+    d = SCENE_CACHE / f"{name}_g{spec['grid']}_s{spec['samples']}_{spec['colors']}_{spec['light']}_packed"
     path = write_wavelet_grid(d, spec["grid"], spec["samples"], spec["colors"], spec["light"],
                               spec["phase_seed"])
     return path, spec

@@ -38,7 +38,7 @@ def scene64():
 
 
 def run(cfg, scene, grid, oracle_mod, **gpu_kw):
-    cam = scenes.orbit_camera(grid)
+    cam = scenes.orbit_camera(scene)
     t = sg.Tracer(cfg, debug_capture=1, **gpu_kw)
     t.set_scene(scene)
     t.set_camera(*cam)
@@ -202,7 +202,7 @@ def test_image_matches_oracles(lib_built, oracle_mod, mode, spp, bounces, light)
 
 def test_extensions_match_wavefront_oracle(lib_built, oracle_mod):
     sc = scenes.wavelet_grid(2, 24, colors="albedo", light="quad")
-    diag = scenes.scene_diagonal(2)
+    diag = scenes.scene_diagonal(sc)
     for cfg in (small_config(ao_mode=1, ao_samples=4, ao_max_distance=0.05 * diag, ao_light_shadow=1),
                 small_config(ao_mode=0, ao_samples=2, pixel_samples=2, bounces=5, rr_depth=3)):
         t, img, st, o = run(cfg, sc, 2, oracle_mod)
@@ -213,7 +213,7 @@ def test_extensions_match_wavefront_oracle(lib_built, oracle_mod):
 def test_waves_and_culling_do_not_change_the_image(lib_built, oracle_mod, scene64):
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3,
                        max_samples_per_rank=2048)
-    cam = scenes.orbit_camera(4)
+    cam = scenes.orbit_camera(scene64)
     imgs = []
     for kw in (dict(cull=1), dict(cull=0), dict(cull=1, wave_samples=3000), dict(cull=0, wave_samples=2048)):
         t = sg.Tracer(cfg, **kw)
@@ -230,7 +230,7 @@ def test_waves_and_culling_do_not_change_the_image(lib_built, oracle_mod, scene6
 def test_deterministic_frames(lib_built, scene64):
     t = sg.Tracer(small_config(image_w=64, image_h=64, ao_mode=0, pixel_samples=2, bounces=2))
     t.set_scene(scene64)
-    t.set_camera(*scenes.orbit_camera(4))
+    t.set_camera(*scenes.orbit_camera(scene64))
     a, sa = t.trace()
     b, sb = t.trace()
     assert np.array_equal(bits(a), bits(b))
