@@ -30,6 +30,7 @@ constexpr uint32_t kRayIdMask = (1u << kRayIdBits) - 1u;
 constexpr int kMaxSlots = 64;      // shadow rays per hit
 constexpr int kSchedThreads = 256;
 constexpr int kDepthBuckets = 4;   // key = min(depth, 3) * D + domain when ordering by depth
+constexpr int kMaxScanBlocks = 4096;  // blocks of the histogram scan
 
 struct DomainDev {
   float bmin[3], bmax[3];  // world AABB used by the scheduler
@@ -177,6 +178,7 @@ struct ShadeArgs {
 void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int ntiles,
                       int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
                       uint32_t* alive_count, int32_t* alive_idx, Counters* ctr);
+// scan_tmp holds kMaxScanBlocks words.  Launches 5 kernels.
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
                     int nwarps, int nblocks, uint32_t* scan_tmp);
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks);

@@ -1,5 +1,6 @@
 // Primary-ray generation, the speculative scheduler (ray -> per-domain
 // queues), stable stream compaction and the domain scores.
+#include <algorithm>
 #include <cfloat>
 
 #include "kernels.cuh"
@@ -198,39 +199,81 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
   for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nwarps + gw] = h[k];
 }
 
-// Pass 2: exclusive scan of the (key-major) histogram in one block.
-__global__ void __launch_bounds__(1024) kScanHist(uint32_t* hist, int nkeys, int nwarps,
-                                                  uint32_t* key_start, uint32_t* num_entries,
-                                                  unsigned long long entry_cap, Counters* ctr) {
-  __shared__ uint32_t part[1024];
-  const uint64_t M = (uint64_t)nkeys * nwarps;
-  const uint64_t per = (M + blockDim.x - 1) / blockDim.x;
-  const uint64_t b0 = min(M, per * threadIdx.x), b1 = min(M, b0 + per);
-  uint32_t sum = 0;
-  for (uint64_t i = b0; i < b1; ++i) sum += hist[i];
-  part[threadIdx.x] = sum;
+// Pass 2: exclusive scan of the key-major histogram, three phases over many
+// blocks: per-block sums, a scan of the block sums, then per-block scans.
+constexpr int kScanThreads = 512;
+
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t ws[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t wt;
+  uint32_t x = warpExclusiveScan(v, &wt);
+  if (lane == 31) ws[w] = wt;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+  if (w == 0) {
+    uint32_t y = lane < nw ? ws[lane] : 0u, t2;
+    uint32_t e = warpExclusiveScan(y, &t2);
+    if (lane < nw) ws[lane] = e;
+    if (lane == 0) ws[31] = t2;
+  }
+  __syncthreads();
+  uint32_t r = x + ws[w];
+  *total = ws[31];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) kScanReduce(const uint32_t* __restrict__ in, uint64_t M,
+                                                            uint64_t chunk, uint32_t* partial) {
+  const uint64_t b0 = min(M, chunk * blockIdx.x), b1 = min(M, b0 + chunk);
+  uint32_t s = 0;
+  for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += in[i];
+  uint32_t tot;
+  blockExclusiveScan(s, &tot);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) kScanPartials(uint32_t* partial, int nb) {
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    uint32_t v = i < nb ? partial[i] : 0u, tot;
+    uint32_t e = blockExclusiveScan(v, &tot);
+    if (i < nb) partial[i] = carry + e;
     __syncthreads();
-    part[threadIdx.x] += v;
+    if (threadIdx.x == 0) carry += tot;
     __syncthreads();
   }
-  uint32_t run = part[threadIdx.x] - sum;
-  for (uint64_t i = b0; i < b1; ++i) {
-    uint32_t v = hist[i];
-    hist[i] = run;
-    if (i % nwarps == 0) key_start[i / nwarps] = run;
-    run += v;
-  }
-  if (threadIdx.x == blockDim.x - 1) {
-    uint32_t total = part[blockDim.x - 1];
-    key_start[nkeys] = total;
-    if (total > entry_cap) {
-      atomicAdd(&ctr->entry_overflows, 1ull);
-      total = 0;
+}
+
+__global__ void __launch_bounds__(kScanThreads) kScanApply(uint32_t* hist, uint64_t M, uint64_t chunk,
+                                                           const uint32_t* partial, int nb, int nwarps,
+                                                           int nkeys, uint32_t* key_start,
+                                                           uint32_t* num_entries,
+                                                           unsigned long long entry_cap, Counters* ctr) {
+  const uint64_t b0 = min(M, chunk * blockIdx.x), b1 = min(M, b0 + chunk);
+  uint32_t run = partial[blockIdx.x];
+  for (uint64_t base = b0; base < b1; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const uint32_t v = i < b1 ? hist[i] : 0u;
+    uint32_t tot;
+    const uint32_t e = blockExclusiveScan(v, &tot);
+    if (i < b1) {
+      hist[i] = run + e;
+      if (i % nwarps == 0) key_start[i / nwarps] = run + e;
+      if (i == M - 1) {
+        uint32_t total = run + e + v;
+        key_start[nkeys] = total;
+        if (total > entry_cap) {
+          atomicAdd(&ctr->entry_overflows, 1ull);
+          total = 0;
+        }
+        *num_entries = total;
+      }
     }
-    *num_entries = total;
+    run += tot;
   }
 }
 
@@ -295,13 +338,17 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
 
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
                     int nblocks, uint32_t* scan_tmp) {
-  (void)scan_tmp;
   const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
   size_t smem1 = (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
   cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
   kSchedLists<<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
-  kScanHist<<<1, 1024, 0, s>>>(a.hist, nkeys, nwarps, a.key_start, a.num_entries, a.entry_cap,
-                               a.ctr);
+  const uint64_t M = (uint64_t)nkeys * nwarps;
+  const int nb = (int)std::min<uint64_t>(kMaxScanBlocks, (M + 2047) / 2048);
+  const uint64_t chunk = (M + nb - 1) / nb;
+  kScanReduce<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp);
+  kScanPartials<<<1, 1024, 0, s>>>(scan_tmp, nb);
+  kScanApply<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp, nb, nwarps, nkeys, a.key_start,
+                                          a.num_entries, a.entry_cap, a.ctr);
   const int wpb = 4;
   size_t smem3 = (size_t)wpb * nkeys * 4 + (size_t)wpb * 32 * kMaxEmit * 3 * 4;
   cudaFuncSetAttribute(kSchedScatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);

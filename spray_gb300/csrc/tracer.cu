@@ -204,6 +204,7 @@ void Tracer::freeBuffers() {
   devFree(d_rec_key);
   devFree(d_rec_attr);
   devFree(d_work);
+  devFree(d_scan_tmp);
   devFree(d_block_tmp);
   devFree(d_image);
   devFree(d_scores);
@@ -349,7 +350,7 @@ void Tracer::planWaves() {
   tiles = makeTiles(cfg.image_w, cfg.image_h, cfg.pixel_samples, cfg.num_ranks, cfg.rank,
                     cfg.max_samples_per_rank);
   const int S = std::max(slots(), 1);
-  int64_t cap = cfg.wave_samples > 0 ? cfg.wave_samples : (int64_t)16 << 20;
+  int64_t cap = cfg.wave_samples > 0 ? cfg.wave_samples : (int64_t)64 << 20;
   cap = std::min<int64_t>(cap, ((int64_t)1 << kRayIdBits) / S - 1);
   waves.clear();
   size_t k = 0;
@@ -374,7 +375,7 @@ void Tracer::planWaves() {
 void Tracer::ensureBuffers(int64_t nsamples) {
   const int S = std::max(slots(), 1);
   const int nkeys = kDepthBuckets * D;
-  sched_blocks = num_sms * 2;
+  sched_blocks = num_sms * 8;
   sched_warps = sched_blocks * (kSchedThreads / 32);
   if (nsamples <= cap_samples && cap_entries >= needed_entries) return;
   freeBuffers();
@@ -418,6 +419,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_rec_key, E);
   devAlloc(&d_rec_attr, E);
   devAlloc(&d_work, kDepthBuckets);
+  devAlloc(&d_scan_tmp, kMaxScanBlocks);
   compact_blocks = num_sms * 4;
   devAlloc(&d_block_tmp, compact_blocks);
   devAlloc(&d_image, (size_t)cfg.image_w * cfg.image_h);
@@ -453,8 +455,8 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.ctr = d_ctr;
   CK(cudaMemsetAsync(d_arena_top, 0, sizeof(unsigned long long), stream));
   launches += 1;
-  launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, nullptr);
-  launches += 3;
+  launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp);
+  launches += 5;
 }
 
 TraceArgs Tracer::traceArgs(int order_by_depth, int S) {

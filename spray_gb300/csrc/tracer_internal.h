@@ -135,6 +135,7 @@ class Tracer {
   uint64_t* d_rec_key = nullptr;
   float4* d_rec_attr = nullptr;
   unsigned int* d_work = nullptr;
+  uint32_t* d_scan_tmp = nullptr;
   uint32_t* d_block_tmp = nullptr;
   float4* d_image = nullptr;
   long long* d_scores = nullptr;
