@@ -205,6 +205,7 @@ constexpr int kScanThreads = 512;
 
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* total) {
   __shared__ uint32_t ws[32];
+  __shared__ uint32_t ws_total;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   uint32_t wt;
   uint32_t x = warpExclusiveScan(v, &wt);
@@ -214,11 +215,11 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* tot
     uint32_t y = lane < nw ? ws[lane] : 0u, t2;
     uint32_t e = warpExclusiveScan(y, &t2);
     if (lane < nw) ws[lane] = e;
-    if (lane == 0) ws[31] = t2;
+    if (lane == 0) ws_total = t2;
   }
   __syncthreads();
   uint32_t r = x + ws[w];
-  *total = ws[31];
+  *total = ws_total;
   __syncthreads();
   return r;
 }
