@@ -172,6 +172,8 @@ def main():
     ap.add_argument("--cpu-scale", type=int, default=2, help="CPU baseline frame downscale per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
+    ap.add_argument("--scale", type=int, default=1,
+                    help="divide the image size (profiling captures on a small frame only)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -222,6 +224,9 @@ def main():
     path, _ = scenes.benchmark_scene(args.config)
     scene = sg.Scene.load(path, path.parent)
     spec, cfg = workload(args.config, scene)
+    if args.scale > 1:
+        cfg["image_w"] = max(8, cfg["image_w"] // args.scale)
+        cfg["image_h"] = max(8, cfg["image_h"] // args.scale)
     tracer = sg.Tracer(cfg, device=local)
     tracer.set_scene(scene)
     # weak scaling: each rank renders its own seeded view of the scene

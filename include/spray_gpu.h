@@ -242,6 +242,33 @@ int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int
 int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void* out,
                          int64_t capacity);
 
+/* ---------------------------------------------------------------- no allocation
+ * No counterpart in the reference.  The scheduler (slab test of every ray
+ * against every domain AABB, (t, id)-sorted domain lists, stable partition
+ * into per-domain queues, as Isector::isectAll builds them) for callers that
+ * cannot allocate device memory while they run -- a fixed device budget
+ * reserved at start-up, another framework's stream capture (cudaMalloc is not
+ * capturable, cudaFree synchronises the device), a host runtime that hands
+ * out GPU memory from its own pool.  All scratch lives in one static device
+ * array (about 13 MB, kept on each device that used it until exit); this call
+ * allocates nothing.
+ *   domain_bounds  device, 6 floats per domain (min xyz, max xyz), <= 256 domains
+ *   ray_org/dir    device, 4 floats per ray (xyz + unused), 16-byte aligned,
+ *                  <= 262144 rays, tnear 1e-3, tfar infinity
+ *   entries        device output, 2 words per entry: ray | depth << 26, tdom
+ *                  bits; grouped by domain, ray order inside a domain
+ *   domain_start   device output, num_domains + 1 entry offsets
+ *   num_entries    host output
+ *   stream         cudaStream_t to run on (NULL = legacy default stream)
+ * At most 1048576 entries; larger requests fail with SPRAY_GPU_EINVAL or
+ * SPRAY_GPU_EOVERFLOW.  Blocks until the stream finished the call.  The first
+ * call on a device looks up the scratch address; make it before any stream
+ * capture.  Calls share the scratch: calls that overlap on the GPU race. */
+int spray_gpu_schedule_static(const float* domain_bounds, int32_t num_domains, const float* ray_org,
+                              const float* ray_dir, int32_t num_rays, int32_t list_size,
+                              uint32_t* entries, int64_t entry_capacity, uint32_t* domain_start,
+                              int64_t* num_entries, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,7 +92,7 @@ EXPORTED_SYMBOLS = [
     "spray_gpu_set_scene", "spray_gpu_set_camera", "spray_gpu_trace", "spray_gpu_trace_device",
     "spray_scene_load", "spray_scene_free", "spray_scene_counts", "spray_scene_domains",
     "spray_scene_lights", "spray_write_ply", "spray_generate_wavelet", "spray_gpu_debug_count",
-    "spray_gpu_debug_copy",
+    "spray_gpu_debug_copy", "spray_gpu_schedule_static",
 ]
 
 
@@ -123,6 +123,8 @@ def lib() -> C.CDLL:
         L.spray_write_ply.argtypes = [C.c_char_p, P, C.c_int64, P, P, C.c_int64]
         L.spray_generate_wavelet.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_double), P, C.c_int64,
                                              P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.spray_gpu_schedule_static.argtypes = [P, C.c_int32, P, P, C.c_int32, C.c_int32, P, C.c_int64, P,
+                                                C.POINTER(C.c_int64), P]
         _lib_handle = L
     return _lib_handle
 
@@ -303,6 +305,19 @@ class Tracer:
             _check(lib().spray_gpu_debug_copy(self._h, what, bounce, out.ctypes.data_as(C.c_void_p),
                                               out.nbytes))
         return out
+
+
+def schedule_static(domain_bounds_ptr: int, num_domains: int, org_ptr: int, dir_ptr: int, num_rays: int,
+                    list_size: int, entries_ptr: int, entry_capacity: int, domain_start_ptr: int,
+                    stream: int | None = None) -> int:
+    """spray_gpu_schedule_static on device pointers; returns the entry count."""
+    n = C.c_int64()
+    _check(lib().spray_gpu_schedule_static(C.c_void_p(domain_bounds_ptr), num_domains, C.c_void_p(org_ptr),
+                                           C.c_void_p(dir_ptr), num_rays, list_size,
+                                           C.c_void_p(entries_ptr), entry_capacity,
+                                           C.c_void_p(domain_start_ptr), C.byref(n),
+                                           C.c_void_p(stream) if stream else None))
+    return n.value
 
 
 def generate_wavelet(samples: int = 64, iso: float = 157.0, phase=(0.0, 0.0, 0.0)):

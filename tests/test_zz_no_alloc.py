@@ -1,0 +1,68 @@
+"""The allocation-free scheduling entry point against the regular one.
+
+spray_gpu_schedule_static serves callers that cannot allocate device memory
+while they run (a fixed budget reserved at start-up, another framework's
+stream capture, a runtime with its own device pool): its scratch is one static
+device array.  Its queues must equal, entry for entry, the queues the regular
+path (spray_gpu_trace, read back through spray_gpu_debug_copy) builds from the
+same rays -- on two calls in a row, since calls share and reuse the scratch.
+This file is collected last so that a failure here does not hide the others.
+"""
+import numpy as np
+import pytest
+
+import spray_gb300 as sg
+from spray_gb300 import scenes
+from conftest import small_config
+
+pytestmark = pytest.mark.gpu
+
+
+def test_static_scratch_schedule_matches_regular_path(lib_built):
+    torch = pytest.importorskip("torch")
+    scene = scenes.wavelet_grid(2, 24, colors="albedo", light="point")
+    cfg = small_config(image_w=96, image_h=64, cull=0, debug_capture=1)
+    t = sg.Tracer(cfg)
+    t.set_scene(scene)
+    t.set_camera(*scenes.orbit_camera(scene))
+    t.trace()
+    rays = t.debug(sg.DBG_RAYS, 0)
+    want = t.debug(sg.DBG_RQUEUES, 0)
+    n, D = len(rays), len(scene.domains)
+    assert np.array_equal(rays["sample"], np.arange(n)) and len(want) > 0
+
+    dev = torch.device("cuda:0")
+    org = torch.zeros((n, 4), dtype=torch.float32)
+    dr = torch.zeros((n, 4), dtype=torch.float32)
+    org[:, :3] = torch.from_numpy(np.ascontiguousarray(rays["org"]))
+    dr[:, :3] = torch.from_numpy(np.ascontiguousarray(rays["dir"]))
+    org, dr = org.to(dev), dr.to(dev)
+    bounds = torch.from_numpy(np.stack([d.bounds for d in scene.domains]).astype(np.float32)).to(dev)
+    cap = 4 * len(want) + 64
+    entries = torch.zeros((cap, 2), dtype=torch.int32, device=dev)
+    starts = torch.zeros(D + 1, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    for call in range(2):
+        entries.fill_(-1)
+        starts.fill_(-1)
+        torch.cuda.synchronize()
+        k = sg.schedule_static(bounds.data_ptr(), D, org.data_ptr(), dr.data_ptr(), n, cfg["list_size"],
+                               entries.data_ptr(), cap, starts.data_ptr())
+        assert k == len(want), (call, k, len(want))
+        e = entries[:k].cpu().numpy().view(np.uint32)
+        ks = starts.cpu().numpy().astype(np.int64)
+        assert ks[0] == 0 and ks[-1] == k and np.all(np.diff(ks) >= 0)
+        dom = np.repeat(np.arange(D), np.diff(ks))
+        assert np.array_equal(dom, want["domain"])
+        assert np.array_equal(e[:, 0] & ((1 << 26) - 1), want["ray"])
+        assert np.array_equal((e[:, 0] >> 26) & 31, want["depth"])
+        assert np.array_equal(e[:, 1], want["tdom"].view(np.uint32))
+
+
+def test_static_scratch_rejects_oversize_requests(lib_built):
+    with pytest.raises(sg.SprayError) as e:
+        sg.schedule_static(16, 257, 16, 16, 1, 16, 16, 1, 16)
+    assert e.value.code == sg.EINVAL and "num_domains" in str(e.value)
+    with pytest.raises(sg.SprayError) as e:
+        sg.schedule_static(16, 8, 16, 16, (1 << 18) + 1, 16, 16, 1, 16)
+    assert e.value.code == sg.EINVAL and "num_rays" in str(e.value)
