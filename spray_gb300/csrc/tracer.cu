@@ -454,7 +454,6 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.num_entries = d_num_entries;
   a.ctr = d_ctr;
   CK(cudaMemsetAsync(d_arena_top, 0, sizeof(unsigned long long), stream));
-  launches += 1;
   launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp);
   launches += 5;
 }
@@ -523,7 +522,6 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     // radiance rays -> per-domain queues
     if (b == 0 || capture) {
       CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
-      launches += 1;
     }
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
     CK(cudaEventRecord(s0, stream));
@@ -551,7 +549,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       trace_events.push_back({t0, t1});
     }
     launchResolve(stream, ta, d_hit_ns, nblk);
-    launches += 2 + nb;
+    launches += 1 + nb;
     if (capture) captureHits(b);
     // shade
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
@@ -580,7 +578,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     sa.num_lights = (int)lights.size();
     sa.ctr = d_ctr;
     launchShade(stream, sa, nblk);
-    launches += 2;
+    launches += 1;
     // shadow rays -> queues -> occlusion
     launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
                   nullptr, d_block_tmp, compact_blocks);
@@ -594,7 +592,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     launchTraceOccluded(stream, to, num_sms * 8);
     CK(cudaEventRecord(o1, stream));
     occl_events.push_back({o0, o1});
-    launches += 2;
+    launches += 1;
     if (capture) captureShadows(b, S);
     // retire
     int64_t npix = w.samples / spp;
@@ -630,7 +628,6 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     dbg.clear();
     CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
     CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
-    launches += 2;
     CK(cudaEventRecord(ev_start, stream));
     for (size_t k = 0; k < waves.size(); ++k) traceWave(waves[k], cfg.debug_capture && k == 0);
     CK(cudaEventRecord(ev_stop, stream));
