@@ -14,6 +14,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libspray_gpu.so"
+FILM = PKG / "spray_gpu_film"
 
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
@@ -72,6 +73,13 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout)
         os.replace(tmp, LIB)
+    film_src = CSRC / "film_main.cpp"
+    if force or not FILM.exists() or _needs(FILM, [film_src, LIB]):
+        cmd = ["g++", "-O2", "-std=c++17", "-o", str(FILM), str(film_src), "-L" + str(PKG),
+               "-lspray_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("film app link failed:\n" + r.stdout)
     return LIB
 
 

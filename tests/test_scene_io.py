@@ -116,3 +116,16 @@ def test_reference_example_scenes_parse(lib_built):
     s2 = sg.Scene.load(REF_EXAMPLES / "wavelet" / "wavelet_example.spray", REF_EXAMPLES / "wavelet")
     assert len(s2.domains) == 2 and [l.type for l in s2.lights] == [0, 1]
     assert len(s2.domains[0].faces) == 1748 and len(s2.domains[1].faces) == 1684
+
+
+def test_ppm_writer_semantics(tmp_path):
+    from spray_gb300 import image
+    img = np.zeros((2, 3, 4), np.float32)
+    img[0, 0, :3] = [0.5, 2.0, -1.0]       # bottom-left pixel
+    img[1, 2, :3] = [0.001, 0.9999, 1.0]    # top-right pixel
+    data = image.ppm_bytes(img).decode().split("\n")
+    assert data[:3] == ["P3", "3 2", "1023"]
+    # rows from y = H-1 down; clamp(v * 1023) truncated (image.h:193-200)
+    assert data[3 + 2] == "1 1022 1023"
+    assert data[3 + 3] == "511 1023 0"
+    assert np.array_equal(image.read_ppm_bytes(image.ppm_bytes(img))[0, 0], [511, 1023, 0])
