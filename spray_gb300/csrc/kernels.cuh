@@ -142,6 +142,9 @@ struct TraceArgs {
   int nkeys;
   unsigned int* work;         // work-stealing counter (zeroed before launch)
   int bucket;                 // depth bucket to trace (-1 = every entry)
+  const uint32_t* seg_begin;  // out of core: first entry of each segment to trace
+  const uint32_t* seg_prefix; // exclusive prefix of the segment lengths (nseg + 1)
+  int nseg;                   // 0 = no segment table
   RayBuf rays;
   ShadowBuf sh;
   int slots;

@@ -236,15 +236,40 @@ __device__ __forceinline__ int findKey(const uint32_t* ks, int nkeys, uint32_t e
   return lo;
 }
 
+// Key offsets and, out of core, the segment table into shared memory.
+__device__ __forceinline__ void loadTables(const TraceArgs& a, uint32_t* skeys, uint32_t* sbeg,
+                                           uint32_t* spre) {
+  for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
+  for (int k = threadIdx.x; k < a.nseg; k += blockDim.x) sbeg[k] = a.seg_begin[k];
+  for (int k = threadIdx.x; k <= a.nseg; k += blockDim.x) spre[k] = a.seg_prefix[k];
+  __syncthreads();
+}
+
+// Work index -> entry index (identity without a segment table).
+__device__ __forceinline__ uint32_t entryOf(const TraceArgs& a, const uint32_t* sbeg,
+                                            const uint32_t* spre, uint32_t w) {
+  if (a.nseg == 0) return w;
+  int lo = 0, hi = a.nseg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (spre[mid] <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  return sbeg[lo] + (w - spre[lo]);
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
-  for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
-  __syncthreads();
+  uint32_t* sbeg = skeys + a.nkeys + 1;
+  uint32_t* spre = sbeg + a.nseg;
+  loadTables(a, skeys, sbeg, spre);
   uint32_t E0 = 0, E = *a.num_entries;
-  if (a.bucket >= 0 && E > 0) {
+  if (a.nseg > 0) {
+    E = spre[a.nseg];
+  } else if (a.bucket >= 0 && E > 0) {
     E0 = skeys[a.bucket * D];
     E = a.bucket + 1 < kDepthBuckets ? skeys[(a.bucket + 1) * D] : skeys[a.nkeys];
   }
@@ -255,8 +280,9 @@ __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
     if (lane == 0) base = E0 + atomicAdd(a.work, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= E) break;
-    const uint32_t e = base + lane;
-    if (e >= E) continue;
+    const uint32_t w = base + lane;
+    if (w >= E) continue;
+    const uint32_t e = entryOf(a, sbeg, spre, w);
     const uint2 ent = a.entries[e];
     const uint32_t ray = ent.x & kRayIdMask;
     const float tdom = __uint_as_float(ent.y);
@@ -312,7 +338,7 @@ __global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
 }
 
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks) {
-  size_t smem = (size_t)(a.nkeys + 1) * 4;
+  size_t smem = (size_t)(a.nkeys + 2 + 2 * a.nseg) * 4;
   kTraceClosest<<<nblocks, 256, smem, s>>>(a);
 }
 
@@ -335,9 +361,10 @@ void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nbloc
 __global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
-  for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
-  __syncthreads();
-  const uint32_t E = *a.num_entries;
+  uint32_t* sbeg = skeys + a.nkeys + 1;
+  uint32_t* spre = sbeg + a.nseg;
+  loadTables(a, skeys, sbeg, spre);
+  const uint32_t E = a.nseg > 0 ? spre[a.nseg] : *a.num_entries;
   const int lane = threadIdx.x & 31;
   unsigned long long visits = 0, nnodes = 0, ntris = 0;
   while (true) {
@@ -345,8 +372,9 @@ __global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
     if (lane == 0) base = atomicAdd(a.work, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= E) break;
-    const uint32_t e = base + lane;
-    if (e >= E) continue;
+    const uint32_t w = base + lane;
+    if (w >= E) continue;
+    const uint32_t e = entryOf(a, sbeg, spre, w);
     const uint2 ent = a.entries[e];
     const uint32_t ray = ent.x & kRayIdMask;
     if (*((volatile uint8_t*)&a.sh.occluded[ray])) continue;
@@ -371,7 +399,7 @@ __global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
 }
 
 void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {
-  size_t smem = (size_t)(a.nkeys + 1) * 4;
+  size_t smem = (size_t)(a.nkeys + 2 + 2 * a.nseg) * 4;
   kTraceOccluded<<<nblocks, 256, smem, s>>>(a);
 }
 

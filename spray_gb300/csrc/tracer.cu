@@ -162,6 +162,12 @@ Tracer::~Tracer() {
 }
 
 void Tracer::freeScene() {
+  if (h_pinned) cudaFreeHost(h_pinned);
+  h_pinned = nullptr;
+  if (h_stage) cudaFreeHost(h_stage);
+  h_stage = nullptr;
+  ooc = false;
+  devFree(d_segs);
   devFree(d_domains);
   devFree(d_nodes);
   devFree(d_tris);
@@ -224,8 +230,7 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   if (nd <= 0) throw std::invalid_argument("scene needs at least one domain");
   if (nd > 65535) throw std::invalid_argument("at most 65535 domains");
   if (!cfg.ao_mode && nl <= 0) throw std::invalid_argument("path tracing needs at least one light");
-  if (cfg.cache_size >= 0 && cfg.cache_size < nd)
-    throw std::invalid_argument("out-of-core cache (cache_size < number of domains) is not supported yet");
+  if (cfg.cache_size == 0) throw std::invalid_argument("cache_size must not be 0");
   CK(cudaSetDevice(cfg.device));
   freeScene();
   D = nd;
@@ -272,6 +277,8 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   }
   for (int d = 0; d < nd; ++d)
     if (!errors[d].empty()) throw std::invalid_argument(errors[d]);
+  domain_verts.assign(nd, 0);
+  for (int d = 0; d < nd; ++d) domain_verts[d] = (size_t)packs[d].nv;
   // concatenate in domain order
   hdoms.assign(nd, DomainDev{});
   size_t nn = 0, nt = 0, nvv = 0;
@@ -304,6 +311,22 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   if (max_bvh_depth * 3 + 4 > 64) throw std::runtime_error("BVH deeper than the traversal stack");
   total_tris = nt;
   scene_bytes = nn * sizeof(BvhNode4) + 3 * nt * sizeof(float4) + 3 * nt * 4 + nvv * 4 + 3 * nvv * 4;
+  // out-of-core when the cache holds fewer domains than the scene has
+  size_t max_nodes = 0, max_tris = 0, max_verts = 0;
+  for (int d = 0; d < nd; ++d) {
+    max_nodes = std::max(max_nodes, packs[d].nodes.size());
+    max_tris = std::max(max_tris, (size_t)packs[d].nf);
+    max_verts = std::max(max_verts, (size_t)packs[d].nv);
+  }
+  const size_t slot_bytes = max_nodes * sizeof(BvhNode4) + max_tris * (3 * sizeof(float4) + 12) + max_verts * 16;
+  int capacity = nd;
+  if (cfg.cache_bytes > 0) capacity = (int)std::max<int64_t>(1, std::min<int64_t>(nd, cfg.cache_bytes / (int64_t)slot_bytes));
+  else if (cfg.cache_size > 0 && cfg.cache_size < nd) capacity = cfg.cache_size;
+  ooc = capacity < nd;
+  if (ooc) {
+    setupOutOfCore(packs, capacity, max_nodes, max_tris, max_verts, slot_bytes);
+    packs.clear();
+  } else {
   devAlloc(&d_domains, nd);
   devAlloc(&d_nodes, nn);
   devAlloc(&d_tris, 3 * nt);
@@ -324,6 +347,7 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
                   cudaMemcpyHostToDevice));
   }
   CK(cudaMemcpy(d_domains, hdoms.data(), nd * sizeof(DomainDev), cudaMemcpyHostToDevice));
+  }
   std::vector<float> lf(13 * std::max(nl, 1), 0.f);
   for (int l = 0; l < nl; ++l) {
     float* q = &lf[13 * l];
@@ -339,6 +363,190 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   CK(cudaMemcpy(d_lights, lf.data(), lf.size() * 4, cudaMemcpyHostToDevice));
   freeBuffers();  // sizes depend on the domain count and slots
   has_scene = true;
+}
+
+// ---------------------------------------------------------------- out of core
+// Domains stay in pinned host memory, prepared (BVH, leaf-ordered triangles,
+// shading data) once; the device holds `capacity` fixed-size slots managed by
+// an LRU with the reference's policy (LruCache::load, src/render/lru_cache.cc:
+// 65-171: promote on hit, evict the least recently used block on a miss).
+void Tracer::setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t max_nodes,
+                            size_t max_tris, size_t max_verts, size_t slot_bytes) {
+  cache_capacity = capacity;
+  slot_nodes = max_nodes;
+  slot_tris = max_tris;
+  slot_verts = max_verts;
+  cache_slot_bytes = slot_bytes;
+  // one pinned arena: per domain nodes | tris | faces | colours | normals
+  host_off.assign(D, 0);
+  size_t total = 0;
+  for (int d = 0; d < D; ++d) {
+    host_off[d] = total;
+    const DomainPack& p = packs[d];
+    total += p.nodes.size() * sizeof(BvhNode4) + p.tris.size() * sizeof(float4) + p.faces.size() * 4 +
+             p.colors.size() * 4 + p.normals.size() * 4;
+    total = (total + 255) & ~(size_t)255;
+  }
+  CK(cudaHostAlloc((void**)&h_pinned, std::max<size_t>(total, 256), cudaHostAllocDefault));
+  for (int d = 0; d < D; ++d) {
+    const DomainPack& p = packs[d];
+    char* q = h_pinned + host_off[d];
+    auto put = [&](const void* src, size_t n) {
+      std::memcpy(q, src, n);
+      q += n;
+    };
+    put(p.nodes.data(), p.nodes.size() * sizeof(BvhNode4));
+    put(p.tris.data(), p.tris.size() * sizeof(float4));
+    put(p.faces.data(), p.faces.size() * 4);
+    put(p.colors.data(), p.colors.size() * 4);
+    put(p.normals.data(), p.normals.size() * 4);
+    hdoms[d].resident = 0;
+    hdoms[d].node_base = hdoms[d].tri_base = hdoms[d].vert_base = hdoms[d].face_base = 0;
+  }
+  devAlloc(&d_domains, D);
+  devAlloc(&d_nodes, (size_t)capacity * max_nodes);
+  devAlloc(&d_tris, 3 * (size_t)capacity * max_tris);
+  devAlloc(&d_faces, 3 * (size_t)capacity * max_tris);
+  devAlloc(&d_colors, (size_t)capacity * max_verts);
+  devAlloc(&d_normals, 3 * (size_t)capacity * max_verts);
+  devAlloc(&d_segs, 2 * (size_t)D + 2);
+  CK(cudaHostAlloc((void**)&h_stage, D * sizeof(DomainDev) + (2 * (size_t)D + 2) * 4, cudaHostAllocDefault));
+  CK(cudaMemcpy(d_domains, hdoms.data(), D * sizeof(DomainDev), cudaMemcpyHostToDevice));
+  lru.init(capacity);
+}
+
+void LruSlots::init(int cap) {
+  capacity = cap;
+  blocks.clear();
+  where.clear();
+}
+
+bool LruSlots::load(int domain, int* slot, int* evicted) {
+  *evicted = -1;
+  auto it = where.find(domain);
+  if (it != where.end()) {
+    std::pair<int, int> b = *it->second;
+    blocks.erase(it->second);
+    blocks.push_back(b);
+    where[domain] = std::prev(blocks.end());
+    *slot = b.first;
+    return true;
+  }
+  int s;
+  if ((int)blocks.size() < capacity) {
+    s = (int)blocks.size();
+  } else {
+    std::pair<int, int> old = blocks.front();
+    blocks.pop_front();
+    where.erase(old.second);
+    *evicted = old.second;
+    s = old.first;
+  }
+  blocks.push_back({s, domain});
+  where[domain] = std::prev(blocks.end());
+  *slot = s;
+  return false;
+}
+
+// Copies a domain into a device slot (stream-ordered, from pinned memory).
+void Tracer::loadDomain(int d, int slot) {
+  DomainDev& dd = hdoms[d];
+  const size_t nn = (size_t)dd.num_nodes, nt = (size_t)dd.num_tris;
+  // vertex count: colours + normals follow the faces in the pinned block
+  const char* q = h_pinned + host_off[d];
+  size_t nv = domain_verts[d];
+  dd.node_base = (int32_t)(slot * slot_nodes);
+  dd.tri_base = (int32_t)(slot * slot_tris);
+  dd.face_base = (int32_t)(slot * slot_tris);
+  dd.vert_base = (int32_t)(slot * slot_verts);
+  dd.resident = 1;
+  size_t b_nodes = nn * sizeof(BvhNode4), b_tris = 3 * nt * sizeof(float4), b_faces = 3 * nt * 4;
+  CK(cudaMemcpyAsync(d_nodes + dd.node_base, q, b_nodes, cudaMemcpyHostToDevice, stream));
+  q += b_nodes;
+  CK(cudaMemcpyAsync(d_tris + 3 * (size_t)dd.tri_base, q, b_tris, cudaMemcpyHostToDevice, stream));
+  q += b_tris;
+  CK(cudaMemcpyAsync(d_faces + 3 * (size_t)dd.face_base, q, b_faces, cudaMemcpyHostToDevice, stream));
+  q += b_faces;
+  CK(cudaMemcpyAsync(d_colors + dd.vert_base, q, nv * 4, cudaMemcpyHostToDevice, stream));
+  q += nv * 4;
+  CK(cudaMemcpyAsync(d_normals + 3 * (size_t)dd.vert_base, q, 3 * nv * 4, cudaMemcpyHostToDevice, stream));
+  h2d_bytes += b_nodes + b_tris + b_faces + nv * 16;
+  ++domain_loads;
+}
+
+// Traces the queues of an out-of-core scene: domains in `order` that have
+// entries are made resident in batches of at most the cache capacity (so a
+// batch never evicts its own domains), and each batch is traced in one launch
+// over its entry segments.
+void Tracer::traceOutOfCore(bool shadow, const std::vector<int>& order, int S) {
+  std::vector<uint32_t> ks(D + 1);
+  CK(cudaMemcpyAsync(ks.data(), d_key_start, (D + 1) * 4, cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  std::vector<int> todo;
+  for (int d : order)
+    if (ks[d + 1] > ks[d]) todo.push_back(d);
+  size_t i = 0;
+  while (i < todo.size()) {
+    size_t j = std::min(todo.size(), i + (size_t)cache_capacity);
+    for (size_t k = i; k < j; ++k) {
+      int slot, evicted;
+      if (!lru.load(todo[k], &slot, &evicted)) {
+        if (evicted >= 0) hdoms[evicted].resident = 0;
+        loadDomain(todo[k], slot);
+      }
+    }
+    // stage the domain table and the segment table (begin, prefix) of this batch
+    DomainDev* sd = reinterpret_cast<DomainDev*>(h_stage);
+    std::memcpy(sd, hdoms.data(), D * sizeof(DomainDev));
+    uint32_t* seg = reinterpret_cast<uint32_t*>(h_stage + D * sizeof(DomainDev));
+    const int nseg = (int)(j - i);
+    uint32_t run = 0;
+    for (int k = 0; k < nseg; ++k) {
+      int d = todo[i + k];
+      seg[k] = ks[d];
+      seg[D + 1 + k] = run;
+      run += ks[d + 1] - ks[d];
+    }
+    seg[D + 1 + nseg] = run;
+    CK(cudaMemcpyAsync(d_domains, sd, D * sizeof(DomainDev), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_segs, seg, (2 * (size_t)D + 2) * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(d_work, 0, 4, stream));
+    TraceArgs ta = traceArgs(0, S);
+    ta.seg_begin = d_segs;
+    ta.seg_prefix = d_segs + D + 1;
+    ta.nseg = nseg;
+    cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
+    CK(cudaEventRecord(e0, stream));
+    if (shadow) launchTraceOccluded(stream, ta, num_sms * 8);
+    else launchTraceClosest(stream, ta, num_sms * 8);
+    CK(cudaEventRecord(e1, stream));
+    (shadow ? occl_events : trace_events).push_back({e0, e1});
+    launches += 1;
+    // the staging buffer is reused by the next batch
+    CK(cudaStreamSynchronize(stream));
+    i = j;
+  }
+}
+
+// Domain processing order: DomainStats::schedule on the counts of the last
+// radiance scheduling (descending score, ties by id).
+std::vector<int> Tracer::scoreOrder() {
+  std::vector<long long> st((size_t)D * cfg.list_size);
+  CK(cudaMemcpyAsync(st.data(), d_dstats, st.size() * 8, cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  std::vector<std::pair<long long, int>> sc(D);
+  const int L = cfg.list_size;
+  for (int d = 0; d < D; ++d) {
+    long long v = 0;
+    for (int k = 0; k < L; ++k) v += st[(size_t)d * L + k] * (long long)(L - k);
+    sc[d] = {v, d};
+  }
+  std::sort(sc.begin(), sc.end(), [](const std::pair<long long, int>& a, const std::pair<long long, int>& b) {
+    return a.first > b.first || (a.first == b.first && a.second < b.second);
+  });
+  std::vector<int> order(D);
+  for (int k = 0; k < D; ++k) order[k] = sc[k].second;
+  return order;
 }
 
 void Tracer::setCamera(const float p[3], const float l[3], const float up[3], float vfov) {
@@ -467,6 +675,9 @@ TraceArgs Tracer::traceArgs(int order_by_depth, int S) {
   t.nkeys = order_by_depth ? kDepthBuckets * D : D;
   t.work = d_work;
   t.bucket = -1;
+  t.seg_begin = nullptr;
+  t.seg_prefix = nullptr;
+  t.nseg = 0;
   t.rays = rays[cur];
   t.sh = sh;
   t.slots = S;
@@ -515,12 +726,12 @@ void Tracer::traceWave(const Wave& w, bool capture) {
   launchGenPrimary(stream, cam, d_tiles, w.num_tiles, w.samples, spp, cfg.image_w, rays[0],
                    d_alive_list, d_alive_count, d_alive_idx, d_ctr);
   launches += 1;
-  const int order_by_depth = cfg.cull ? 1 : 0;
+  const int order_by_depth = (cfg.cull && !ooc) ? 1 : 0;
   const int nblk = num_sms * 4;
   for (int b = 0; b < cfg.bounces; ++b) {
     if (capture) captureRays(b);
     // radiance rays -> per-domain queues
-    if (b == 0 || capture) {
+    if (b == 0 || capture || ooc) {
       CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
     }
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
@@ -536,20 +747,27 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     // closest hits; with culling, one launch per depth bucket so that every
     // entry sees the hits of all nearer domain lists (front-to-back waves)
-    CK(cudaMemsetAsync(d_work, 0, 4 * kDepthBuckets, stream));
     TraceArgs ta = traceArgs(order_by_depth, S);
-    const int nb = order_by_depth ? kDepthBuckets : 1;
-    for (int k = 0; k < nb; ++k) {
-      ta.bucket = order_by_depth ? k : -1;
-      ta.work = d_work + k;
-      cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
-      CK(cudaEventRecord(t0, stream));
-      launchTraceClosest(stream, ta, num_sms * 8);
-      CK(cudaEventRecord(t1, stream));
-      trace_events.push_back({t0, t1});
+    std::vector<int> order;
+    if (ooc) {
+      order = scoreOrder();
+      traceOutOfCore(false, order, S);
+    } else {
+      CK(cudaMemsetAsync(d_work, 0, 4 * kDepthBuckets, stream));
+      const int nb = order_by_depth ? kDepthBuckets : 1;
+      for (int k = 0; k < nb; ++k) {
+        ta.bucket = order_by_depth ? k : -1;
+        ta.work = d_work + k;
+        cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
+        CK(cudaEventRecord(t0, stream));
+        launchTraceClosest(stream, ta, num_sms * 8);
+        CK(cudaEventRecord(t1, stream));
+        trace_events.push_back({t0, t1});
+      }
+      launches += nb;
     }
     launchResolve(stream, ta, d_hit_ns, nblk);
-    launches += 1 + nb;
+    launches += 1;
     if (capture) captureHits(b);
     // shade
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
@@ -585,14 +803,25 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     launches += 3;
     schedule(true, 0, d_shadow_count, d_shadow_list, S);
     if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, 0);
-    CK(cudaMemsetAsync(d_work, 0, 4, stream));
-    TraceArgs to = traceArgs(0, S);
-    cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
-    CK(cudaEventRecord(o0, stream));
-    launchTraceOccluded(stream, to, num_sms * 8);
-    CK(cudaEventRecord(o1, stream));
-    occl_events.push_back({o0, o1});
-    launches += 1;
+    if (ooc) {
+      // resident domains first (most recently used first), then the rest in score order
+      std::vector<int> sorder;
+      for (auto it = lru.blocks.rbegin(); it != lru.blocks.rend(); ++it) sorder.push_back(it->second);
+      std::vector<char> seen(D, 0);
+      for (int d : sorder) seen[d] = 1;
+      for (int d : order)
+        if (!seen[d]) sorder.push_back(d);
+      traceOutOfCore(true, sorder, S);
+    } else {
+      CK(cudaMemsetAsync(d_work, 0, 4, stream));
+      TraceArgs to = traceArgs(0, S);
+      cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
+      CK(cudaEventRecord(o0, stream));
+      launchTraceOccluded(stream, to, num_sms * 8);
+      CK(cudaEventRecord(o1, stream));
+      occl_events.push_back({o0, o1});
+      launches += 1;
+    }
     if (capture) captureShadows(b, S);
     // retire
     int64_t npix = w.samples / spp;
@@ -621,6 +850,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     launches = 0;
     h2d_bytes = 0;
     d2h_bytes = 0;
+    domain_loads = 0;
     ev_used = 0;
     sched_events.clear();
     trace_events.clear();
@@ -660,7 +890,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->visits_radiance = (int64_t)ctr.visits_radiance;
       st->visits_shadow = (int64_t)ctr.visits_shadow;
       st->visits_culled = (int64_t)ctr.visits_culled;
-      st->domain_loads = 0;
+      st->domain_loads = domain_loads;
       st->h2d_bytes = (int64_t)h2d_bytes;
       st->d2h_bytes = (int64_t)d2h_bytes;
       st->kernel_launches = launches;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <list>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -45,6 +46,17 @@ struct DomainPack {
   int bvh_depth = 0;
 };
 
+// Device slots of the out-of-core domain cache, least recently used first.
+struct LruSlots {
+  int capacity = 0;
+  std::list<std::pair<int, int>> blocks;  // (slot, domain)
+  std::map<int, std::list<std::pair<int, int>>::iterator> where;
+  void init(int cap);
+  // Returns true on a hit; on a miss `slot` is the slot to fill and `evicted`
+  // the domain that lived there (-1 if the slot was free).
+  bool load(int domain, int* slot, int* evicted);
+};
+
 std::vector<HostTile> makeTiles(int W, int H, int spp, int num_ranks, int rank, int64_t max_samples);
 void computeVertexNormals(const float* v, int64_t nv, const uint32_t* f, int64_t nf, float* n);
 CameraDev makeCamera(const float p[3], const float l[3], const float up[3], float vfov, int W, int H);
@@ -75,6 +87,11 @@ class Tracer {
   void captureScores(int b);
   void captureHits(int b);
   void captureShadows(int b, int S);
+  void setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t max_nodes, size_t max_tris,
+                      size_t max_verts, size_t slot_bytes);
+  void loadDomain(int d, int slot);
+  void traceOutOfCore(bool shadow, const std::vector<int>& order, int S);
+  std::vector<int> scoreOrder();
 
   spray_gpu_config cfg;
   int num_sms = 0;
@@ -100,6 +117,18 @@ class Tracer {
   float* d_normals = nullptr;
   float* d_lights = nullptr;
   CameraDev cam{};
+  std::vector<size_t> domain_verts;
+
+  // out-of-core cache
+  bool ooc = false;
+  int cache_capacity = 0;
+  size_t slot_nodes = 0, slot_tris = 0, slot_verts = 0, cache_slot_bytes = 0;
+  char* h_pinned = nullptr;       // prepared domains, pinned
+  std::vector<size_t> host_off;   // per domain offset into h_pinned
+  char* h_stage = nullptr;        // pinned staging of the domain and segment tables
+  uint32_t* d_segs = nullptr;
+  LruSlots lru;
+  int64_t domain_loads = 0;
 
   // frame plan
   std::vector<HostTile> tiles;

@@ -41,11 +41,13 @@ CONFIGS = {
                         bounces=5, fov=60.0),
                ext=dict(rr_depth=3)),
     # 8x8x8 grid of phase-shifted 128^3 isosurfaces, path tracing, 2048^2,
-    # 8 spp, 4 bounces, device cache capped at 8 GiB
+    # 8 spp, 4 bounces; the device cache holds half of the domains (the
+    # 8 GiB-of-16 GiB ratio of the workload description; the generated scene
+    # is smaller, so the cap is given in domains like SpRay's --cache-size)
     "c3": dict(grid=8, samples=128, colors="albedo", light="quad", phase_seed=2024,
                cfg=dict(image_w=2048, image_h=2048, ao_mode=0, ao_samples=1, pixel_samples=8,
-                        bounces=4, fov=60.0, list_size=22),
-               ext=dict(cache_bytes=8 << 30)),
+                        bounces=4, fov=60.0, list_size=22, cache_size=256),
+               ext=dict()),
 }
 
 GREY = 200
@@ -89,7 +91,10 @@ def domain_meshes(grid: int, samples: int, phase_seed: int | None):
         base = generate_wavelet(samples, 157.0, (0.0, 0.0, 0.0))
         meshes = [base] * n
     else:
-        meshes = [generate_wavelet(samples, 157.0, tuple(phases[d])) for d in range(n)]
+        # the generator runs in C++ without the GIL: one thread per core
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            meshes = list(ex.map(lambda d: generate_wavelet(samples, 157.0, tuple(phases[d])), range(n)))
     cell = max(float((v.max(0) - v.min(0)).max()) for v, _ in meshes[: (1 if phase_seed is None else n)])
     cell = float(np.float32(cell))
     return meshes, cell
@@ -182,14 +187,22 @@ def write_wavelet_grid(out_dir: Path, grid: int = 4, samples: int = 64, colors: 
             lines.append("light quad " + " ".join("%.9g" % x for x in (*l.position, *l.edge1, *l.edge2,
                                                                       *l.radiance)))
     written = {}
+    jobs = []
     for d in range(n):
         v, f = meshes[d]
         col = _color(alb[d]) if alb is not None else _color((GREY, GREY, GREY))
         key = (d if phase_seed is not None else -1, col)
         if key not in written:
             name = f"wavelet_{d:04d}.ply"
-            write_ply(out_dir / name, v, f, np.full(len(v), col, np.uint32))
+            jobs.append((out_dir / name, v, f, np.full(len(v), col, np.uint32)))
             written[key] = (name, v.min(0), v.max(0), len(v), len(f))
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        list(ex.map(lambda j: write_ply(*j), jobs))
+    for d in range(n):
+        v, f = meshes[d]
+        col = _color(alb[d]) if alb is not None else _color((GREY, GREY, GREY))
+        key = (d if phase_seed is not None else -1, col)
         name, blo, bhi, nv, nf = written[key]
         lines += ["", f"# domain {d}", "domain", f"file {name}", "mtl diffuse 1 1 1",
                   "bound %.9g %.9g %.9g %.9g %.9g %.9g" % (*blo, *bhi), f"face {nf}", f"vertex {nv}",

@@ -300,3 +300,36 @@ def test_scene_file_path(lib_built, oracle_mod, tmp_path):
     t, img, st, o = run(cfg, sc, 2, oracle_mod)
     wb, _ = o.render_wavefront()
     assert np.array_equal(bits(img), bits(wb))
+
+
+@pytest.mark.parametrize("kw", [dict(cache_size=16), dict(cache_size=5), dict(cache_bytes=3 << 20)])
+def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
+    """Streaming domains through a small LRU cache changes loads, never the image."""
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
+    cam = scenes.orbit_camera(scene64)
+    ref = sg.Tracer(cfg)
+    ref.set_scene(scene64)
+    ref.set_camera(*cam)
+    want, st0 = ref.trace()
+    assert st0["domain_loads"] == 0
+    t = sg.Tracer(cfg, **kw)
+    t.set_scene(scene64)
+    t.set_camera(*cam)
+    got, st = t.trace()
+    assert np.array_equal(bits(got), bits(want))
+    assert st["domain_loads"] > 0 and st["h2d_bytes"] > 0
+    assert st["rays_shadow"] == st0["rays_shadow"] and st["visits_radiance"] >= st0["visits_radiance"] - st0["visits_culled"]
+    got2, st2 = t.trace()  # the cache stays warm across frames
+    assert np.array_equal(bits(got2), bits(want))
+
+
+def test_out_of_core_queues_match_oracle(lib_built, oracle_mod, scene64):
+    cfg = small_config(image_w=80, image_h=60, cache_size=8)
+    t, img, st, o = run(cfg, scene64, 4, oracle_mod)
+    rays = t.debug(sg.DBG_RAYS, 0)
+    q = t.debug(sg.DBG_RQUEUES, 0)
+    oq, _ = o.schedule(rays["org"], rays["dir"])
+    oq["ray"] = rays["sample"][oq["ray"]]
+    assert np.array_equal(q["domain"], oq["domain"]) and np.array_equal(q["ray"], oq["ray"])
+    wb, _ = o.render_wavefront()
+    assert np.array_equal(bits(img), bits(wb))
