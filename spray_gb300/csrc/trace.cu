@@ -240,8 +240,10 @@ __device__ __forceinline__ int findKey(const uint32_t* ks, int nkeys, uint32_t e
 __device__ __forceinline__ void loadTables(const TraceArgs& a, uint32_t* skeys, uint32_t* sbeg,
                                            uint32_t* spre) {
   for (int k = threadIdx.x; k <= a.nkeys; k += blockDim.x) skeys[k] = a.key_start[k];
-  for (int k = threadIdx.x; k < a.nseg; k += blockDim.x) sbeg[k] = a.seg_begin[k];
-  for (int k = threadIdx.x; k <= a.nseg; k += blockDim.x) spre[k] = a.seg_prefix[k];
+  if (a.nseg > 0) {
+    for (int k = threadIdx.x; k < a.nseg; k += blockDim.x) sbeg[k] = a.seg_begin[k];
+    for (int k = threadIdx.x; k <= a.nseg; k += blockDim.x) spre[k] = a.seg_prefix[k];
+  }
   __syncthreads();
 }
 
