@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 #include <stdexcept>
 
 namespace spray {
@@ -254,6 +255,75 @@ void buildBvh4(const float* vertices, const uint32_t* faces, uint32_t num_faces,
   }
   c.emit(root, 1);
   out->depth = c.maxdepth;
+}
+
+}  // namespace spray
+
+namespace spray {
+namespace {
+
+struct DomBuild {
+  const float* boxes;
+  std::vector<int> ids;
+  std::vector<DomNode>* out;
+
+  void bounds(int first, int count, float lo[3], float hi[3]) const {
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = INFINITY;
+      hi[k] = -INFINITY;
+    }
+    for (int i = first; i < first + count; ++i)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], boxes[6 * ids[i] + k]);
+        hi[k] = std::max(hi[k], boxes[6 * ids[i] + 3 + k]);
+      }
+    // enlarge outward by a relative 1e-6 (plus a tiny absolute term)
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = (float)((double)lo[k] - (std::fabs((double)lo[k]) + 1e-30) * 1e-6);
+      hi[k] = (float)((double)hi[k] + (std::fabs((double)hi[k]) + 1e-30) * 1e-6);
+    }
+  }
+
+  // Returns the child reference for ids[first, first + count).
+  int32_t build(int first, int count) {
+    if (count == 1) return ~(int32_t)ids[first];
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = first; i < first + count; ++i)
+      for (int k = 0; k < 3; ++k) {
+        float c = 0.5f * (boxes[6 * ids[i] + k] + boxes[6 * ids[i] + 3 + k]);
+        clo[k] = std::min(clo[k], c);
+        chi[k] = std::max(chi[k], c);
+      }
+    int axis = 0;
+    for (int k = 1; k < 3; ++k)
+      if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+    int mid = first + count / 2;
+    std::nth_element(ids.begin() + first, ids.begin() + mid, ids.begin() + first + count, [&](int a, int b) {
+      float ca = boxes[6 * a + axis] + boxes[6 * a + 3 + axis];
+      float cb = boxes[6 * b + axis] + boxes[6 * b + 3 + axis];
+      return ca < cb || (ca == cb && a < b);
+    });
+    int id = (int)out->size();
+    out->emplace_back();
+    DomNode node;
+    std::memset(&node, 0, sizeof(node));
+    bounds(first, mid - first, node.lo0, node.hi0);
+    bounds(mid, first + count - mid, node.lo1, node.hi1);
+    node.c0 = build(first, mid - first);
+    node.c1 = build(mid, first + count - mid);
+    (*out)[id] = node;
+    return id;
+  }
+};
+
+}  // namespace
+
+void buildDomainBvh(const float* boxes, int n, std::vector<DomNode>* out) {
+  out->clear();
+  if (n < 2) throw std::runtime_error("domain hierarchy needs at least two domains");
+  DomBuild b{boxes, std::vector<int>(n), out};
+  for (int i = 0; i < n; ++i) b.ids[i] = i;
+  b.build(0, n);
 }
 
 }  // namespace spray

@@ -23,6 +23,25 @@ static_assert(sizeof(BvhNode4) == 128, "node must be one 128-byte line");
 constexpr int kMaxLeafTris = 8;
 constexpr int32_t kEmptyChild = (int32_t)0x80000000;
 
+// Binary hierarchy over the domain boxes, used by the scheduler to find the
+// domains a ray may overlap before it runs SpRay's exact slab test on them.
+// Node boxes are enlarged outward so a conservative node test never rejects a
+// domain the exact test accepts.  c0/c1 >= 0: inner node; < 0: leaf ~domain.
+struct alignas(16) DomNode {
+  float lo0[3];
+  int32_t c0;
+  float hi0[3];
+  float pad0;
+  float lo1[3];
+  int32_t c1;
+  float hi1[3];
+  float pad1;
+};
+static_assert(sizeof(DomNode) == 64, "domain node must be 64 bytes");
+
+// boxes: 6 floats per domain (min xyz, max xyz); n >= 2.
+void buildDomainBvh(const float* boxes, int n, std::vector<DomNode>* out);
+
 struct BvhBuildResult {
   std::vector<BvhNode4> nodes;     // nodes[0] is the root
   std::vector<uint32_t> tri_order;  // leaf order -> original face index

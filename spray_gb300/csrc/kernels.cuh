@@ -31,6 +31,7 @@ constexpr int kMaxSlots = 64;      // shadow rays per hit
 constexpr int kSchedThreads = 256;
 constexpr int kDepthBuckets = 4;   // key = min(depth, 3) * D + domain when ordering by depth
 constexpr int kMaxScanBlocks = 4096;  // blocks of the histogram scan
+constexpr int kDomainBvhMin = 16;     // domain counts from which the scheduler descends a hierarchy
 
 struct DomainDev {
   float bmin[3], bmax[3];  // world AABB used by the scheduler
@@ -119,6 +120,8 @@ struct SchedArgs {
   int order_by_depth;         // key = min(depth,3)*D + domain, else domain
   int list_size;              // SPRAY_RAY_DOMAIN_LIST_SIZE, for the domain statistics
   uint64_t* ray_key;          // radiance: reset to kNoHit per scheduled ray
+  const DomNode* dnodes;      // hierarchy over the domain boxes (null: test every domain)
+  int dnode_count;
   // outputs
   uint2* arena;               // per-ray sorted (domain | depth << 16, tdom) lists
   unsigned long long* arena_top;

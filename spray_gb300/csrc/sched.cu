@@ -91,8 +91,10 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
                                                              const DomainDev* __restrict__ doms,
                                                              int D, int nkeys, int nwarps) {
   extern __shared__ uint32_t smem[];
-  float* sbox = reinterpret_cast<float*>(smem);
-  uint32_t* hist = smem + 6 * D;
+  const int NN = a.dnode_count;
+  float4* snode = reinterpret_cast<float4*>(smem);  // 4 float4 per hierarchy node
+  float* sbox = reinterpret_cast<float*>(smem + 16 * NN);
+  uint32_t* hist = smem + 16 * NN + 6 * D;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int d = threadIdx.x; d < D; d += blockDim.x) {
     for (int c = 0; c < 3; ++c) {
@@ -100,6 +102,8 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
       sbox[6 * d + 3 + c] = doms[d].bmax[c];
     }
   }
+  for (int k = threadIdx.x; k < 4 * NN; k += blockDim.x)
+    snode[k] = reinterpret_cast<const float4*>(a.dnodes)[k];
   uint32_t* h = hist + (size_t)wib * nkeys;
   for (int k = lane; k < nkeys; k += 32) h[k] = 0;
   __syncthreads();
@@ -136,23 +140,58 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
         a.sh.occluded[rid] = 0;
       }
       V3 inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-      for (int d = 0; d < D; ++d) {
+      // exact slab test of domain d, kept in (t, id) order
+      auto consider = [&](int d) {
         float t;
-        if (slabTest(&sbox[6 * d], &sbox[6 * d + 3], org, inv, kRayEpsilon, t1, &t)) {
-          if (cnt == kMaxList) {
-            atomicAdd(&a.ctr->list_overflows, 1ull);
-            if (lt[kMaxList - 1] <= t) continue;
-            --cnt;
+        if (!slabTest(&sbox[6 * d], &sbox[6 * d + 3], org, inv, kRayEpsilon, t1, &t)) return;
+        if (cnt == kMaxList) {
+          atomicAdd(&a.ctr->list_overflows, 1ull);
+          if (lt[kMaxList - 1] < t || (lt[kMaxList - 1] == t && (int)ld[kMaxList - 1] < d)) return;
+          --cnt;
+        }
+        int j = cnt;
+        while (j > 0 && (lt[j - 1] > t || (lt[j - 1] == t && (int)ld[j - 1] > d))) {
+          lt[j] = lt[j - 1];
+          ld[j] = ld[j - 1];
+          --j;
+        }
+        lt[j] = t;
+        ld[j] = (uint32_t)d;
+        ++cnt;
+      };
+      if (NN == 0) {
+        for (int d = 0; d < D; ++d) consider(d);
+      } else {
+        // conservative descent of the domain hierarchy, exact test at the leaves
+        const int sx = inv.x < 0.0f, sy = inv.y < 0.0f, sz = inv.z < 0.0f;
+        const float tfar = t1 * 1.0000004f;
+        int stack[40];
+        int sp = 0;
+        int node = 0;
+        for (int steps = 0; steps < 4 * NN + 4; ++steps) {
+          const float4 l0 = snode[4 * node], h0 = snode[4 * node + 1];
+          const float4 l1 = snode[4 * node + 2], h1 = snode[4 * node + 3];
+          int next = -1;
+          for (int c = 0; c < 2; ++c) {
+            const float4 lo = c ? l1 : l0, hi = c ? h1 : h0;
+            const float nx = sx ? hi.x : lo.x, fx = sx ? lo.x : hi.x;
+            const float ny = sy ? hi.y : lo.y, fy = sy ? lo.y : hi.y;
+            const float nz = sz ? hi.z : lo.z, fz = sz ? lo.z : hi.z;
+            const float t0 = fmaxf(fmaxf((nx - org.x) * inv.x, (ny - org.y) * inv.y),
+                                   fmaxf((nz - org.z) * inv.z, kRayEpsilon));
+            const float tt = fminf(fminf((fx - org.x) * inv.x, (fy - org.y) * inv.y),
+                                   fminf((fz - org.z) * inv.z, tfar)) * 1.0000004f;
+            if (!(t0 <= tt)) continue;
+            const int ref = __float_as_int(lo.w);
+            if (ref < 0) consider(~ref);
+            else if (next < 0) next = ref;
+            else if (sp < 40) stack[sp++] = ref;
           }
-          int j = cnt;
-          while (j > 0 && lt[j - 1] > t) {
-            lt[j] = lt[j - 1];
-            ld[j] = ld[j - 1];
-            --j;
+          if (next < 0) {
+            if (sp == 0) break;
+            next = stack[--sp];
           }
-          lt[j] = t;
-          ld[j] = (uint32_t)d;
-          ++cnt;
+          node = next;
         }
       }
       if (a.shadow) {
@@ -340,7 +379,7 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
                     int nblocks, uint32_t* scan_tmp) {
   const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
-  size_t smem1 = (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
+  size_t smem1 = (size_t)a.dnode_count * 64 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
   cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
   kSchedLists<<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
   const uint64_t M = (uint64_t)nkeys * nwarps;

@@ -168,6 +168,8 @@ void Tracer::freeScene() {
   h_stage = nullptr;
   ooc = false;
   devFree(d_segs);
+  devFree(d_dnodes);
+  dnode_count = 0;
   devFree(d_domains);
   devFree(d_nodes);
   devFree(d_tris);
@@ -347,6 +349,22 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
                   cudaMemcpyHostToDevice));
   }
   CK(cudaMemcpy(d_domains, hdoms.data(), nd * sizeof(DomainDev), cudaMemcpyHostToDevice));
+  }
+  // hierarchy over the domain boxes for the scheduler (all domains are tested
+  // directly when there are few)
+  dnode_count = 0;
+  if (nd >= kDomainBvhMin) {
+    std::vector<float> boxes(6 * (size_t)nd);
+    for (int d = 0; d < nd; ++d)
+      for (int c = 0; c < 3; ++c) {
+        boxes[6 * d + c] = hdoms[d].bmin[c];
+        boxes[6 * d + 3 + c] = hdoms[d].bmax[c];
+      }
+    std::vector<DomNode> dn;
+    buildDomainBvh(boxes.data(), nd, &dn);
+    dnode_count = (int)dn.size();
+    devAlloc(&d_dnodes, dn.size());
+    CK(cudaMemcpy(d_dnodes, dn.data(), dn.size() * sizeof(DomNode), cudaMemcpyHostToDevice));
   }
   std::vector<float> lf(13 * std::max(nl, 1), 0.f);
   for (int l = 0; l < nl; ++l) {
@@ -649,6 +667,8 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.order_by_depth = order_by_depth;
   a.list_size = cfg.list_size;
   a.ray_key = d_ray_key;
+  a.dnodes = d_dnodes;
+  a.dnode_count = dnode_count;
   a.arena = d_arena;
   a.arena_top = d_arena_top;
   a.arena_cap = cap_entries;

@@ -127,6 +127,8 @@ class Tracer {
   std::vector<size_t> host_off;   // per domain offset into h_pinned
   char* h_stage = nullptr;        // pinned staging of the domain and segment tables
   uint32_t* d_segs = nullptr;
+  DomNode* d_dnodes = nullptr;   // hierarchy over the domain boxes
+  int dnode_count = 0;
   LruSlots lru;
   int64_t domain_loads = 0;
 
