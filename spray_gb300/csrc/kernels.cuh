@@ -187,6 +187,8 @@ void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int n
 // scan_tmp holds kMaxScanBlocks words.  Launches 5 kernels.
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
                     int nwarps, int nblocks, uint32_t* scan_tmp);
+// Resident blocks per SM of the scheduling kernel for this shared-memory use.
+int schedBlocksPerSm(int D, int nkeys, int dnode_count);
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks);
 void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks);
 void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks);

@@ -376,6 +376,16 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
   }
 }
 
+int schedBlocksPerSm(int D, int nkeys, int dnode_count) {
+  size_t smem = (size_t)dnode_count * 64 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
+  cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kSchedLists, kSchedThreads, smem) != cudaSuccess ||
+      bps < 1)
+    bps = 1;
+  return bps;
+}
+
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
                     int nblocks, uint32_t* scan_tmp) {
   const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;

@@ -262,7 +262,7 @@ __device__ __forceinline__ uint32_t entryOf(const TraceArgs& a, const uint32_t* 
 
 }  // namespace
 
-__global__ void __launch_bounds__(256) kTraceClosest(TraceArgs a) {
+__global__ void __launch_bounds__(256, 4) kTraceClosest(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
   uint32_t* sbeg = skeys + a.nkeys + 1;
@@ -360,7 +360,7 @@ void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nbloc
   kResolve<<<nblocks, 256, 0, s>>>(a, hit_ns);
 }
 
-__global__ void __launch_bounds__(256) kTraceOccluded(TraceArgs a) {
+__global__ void __launch_bounds__(256, 4) kTraceOccluded(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
   uint32_t* sbeg = skeys + a.nkeys + 1;

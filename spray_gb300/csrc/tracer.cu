@@ -535,8 +535,8 @@ void Tracer::traceOutOfCore(bool shadow, const std::vector<int>& order, int S) {
     ta.nseg = nseg;
     cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
     CK(cudaEventRecord(e0, stream));
-    if (shadow) launchTraceOccluded(stream, ta, num_sms * 8);
-    else launchTraceClosest(stream, ta, num_sms * 8);
+    if (shadow) launchTraceOccluded(stream, ta, num_sms * 4);
+    else launchTraceClosest(stream, ta, num_sms * 4);
     CK(cudaEventRecord(e1, stream));
     (shadow ? occl_events : trace_events).push_back({e0, e1});
     launches += 1;
@@ -601,7 +601,8 @@ void Tracer::planWaves() {
 void Tracer::ensureBuffers(int64_t nsamples) {
   const int S = std::max(slots(), 1);
   const int nkeys = kDepthBuckets * D;
-  sched_blocks = num_sms * 8;
+  // one resident wave: each warp owns a contiguous chunk of rays
+  sched_blocks = num_sms * schedBlocksPerSm(D, kDepthBuckets * D, dnode_count);
   sched_warps = sched_blocks * (kSchedThreads / 32);
   if (nsamples <= cap_samples && cap_entries >= needed_entries) return;
   freeBuffers();
@@ -780,7 +781,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
         ta.work = d_work + k;
         cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
         CK(cudaEventRecord(t0, stream));
-        launchTraceClosest(stream, ta, num_sms * 8);
+        launchTraceClosest(stream, ta, num_sms * 4);
         CK(cudaEventRecord(t1, stream));
         trace_events.push_back({t0, t1});
       }
@@ -837,7 +838,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       TraceArgs to = traceArgs(0, S);
       cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
       CK(cudaEventRecord(o0, stream));
-      launchTraceOccluded(stream, to, num_sms * 8);
+      launchTraceOccluded(stream, to, num_sms * 4);
       CK(cudaEventRecord(o1, stream));
       occl_events.push_back({o0, o1});
       launches += 1;
