@@ -71,6 +71,8 @@ typedef struct spray_gpu_config {
   int64_t wave_samples;         /* samples traced per wavefront; 0 = library default (0) */
   int32_t debug_capture;        /* keep the first wavefront's stage buffers for the debug hooks (0) */
   int32_t device;               /* CUDA device ordinal (0) */
+  int32_t schedule_policy;      /* out-of-core domain order: 0 DomainStats score order (the
+                                   reference's), 1 resident domains first (0) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as

@@ -38,6 +38,7 @@ class ConfigC(C.Structure):
         ("rank", C.c_int32), ("ao_light_shadow", C.c_int32), ("ao_max_distance", C.c_float),
         ("rr_depth", C.c_int32), ("cull", C.c_int32), ("cache_bytes", C.c_int64),
         ("wave_samples", C.c_int64), ("debug_capture", C.c_int32), ("device", C.c_int32),
+        ("schedule_policy", C.c_int32),
     ]
 
 

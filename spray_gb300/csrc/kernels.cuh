@@ -122,6 +122,10 @@ struct SchedArgs {
   uint64_t* ray_key;          // radiance: reset to kNoHit per scheduled ray
   const DomNode* dnodes;      // hierarchy over the domain boxes (null: test every domain)
   int dnode_count;
+  // primary rays: candidate domains per screen bin (null: not primary rays)
+  const uint32_t* bin_start;  // [bins_x * bins_y + 1]
+  const uint16_t* bin_ids;
+  int bins_x, bin_shift, image_w;
   // outputs
   uint2* arena;               // per-ray sorted (domain | depth << 16, tdom) lists
   unsigned long long* arena_top;

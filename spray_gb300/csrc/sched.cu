@@ -159,7 +159,14 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
         ld[j] = (uint32_t)d;
         ++cnt;
       };
-      if (NN == 0) {
+      if (a.bin_start) {
+        // primary rays: the domains whose projected box covers this pixel's bin
+        const int pid = a.rays.pixid[rid];
+        const int bx = (pid % a.image_w) >> a.bin_shift, by = (pid / a.image_w) >> a.bin_shift;
+        const int bin = by * a.bins_x + bx;
+        const uint32_t c0 = a.bin_start[bin], c1 = a.bin_start[bin + 1];
+        for (uint32_t c = c0; c < c1; ++c) consider((int)a.bin_ids[c]);
+      } else if (NN == 0) {
         for (int d = 0; d < D; ++d) consider(d);
       } else {
         // conservative descent of the domain hierarchy, exact test at the leaves

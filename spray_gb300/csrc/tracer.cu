@@ -170,6 +170,9 @@ void Tracer::freeScene() {
   devFree(d_segs);
   devFree(d_dnodes);
   dnode_count = 0;
+  devFree(d_bin_start);
+  devFree(d_bin_ids);
+  bin_start_cap = bin_ids_cap = 0;
   devFree(d_domains);
   devFree(d_nodes);
   devFree(d_tris);
@@ -657,7 +660,8 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   cap_entries = E;
 }
 
-void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S) {
+void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S,
+                      bool primary) {
   SchedArgs a{};
   a.shadow = shadow;
   a.count = count;
@@ -670,6 +674,13 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.ray_key = d_ray_key;
   a.dnodes = d_dnodes;
   a.dnode_count = dnode_count;
+  if (primary && use_bins) {
+    a.bin_start = d_bin_start;
+    a.bin_ids = d_bin_ids;
+    a.bins_x = bins_x;
+    a.bin_shift = kBinShift;
+    a.image_w = cfg.image_w;
+  }
   a.arena = d_arena;
   a.arena_top = d_arena_top;
   a.arena_cap = cap_entries;
@@ -757,7 +768,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
     CK(cudaEventRecord(s0, stream));
-    schedule(false, order_by_depth, d_alive_count, d_alive_list, S);
+    schedule(false, order_by_depth, d_alive_count, d_alive_list, S, b == 0);
     CK(cudaEventRecord(s1, stream));
     sched_events.push_back({s0, s1});
     if (capture) {
@@ -772,7 +783,20 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     std::vector<int> order;
     if (ooc) {
       order = scoreOrder();
-      traceOutOfCore(false, order, S);
+      if (cfg.schedule_policy == 1) {
+        // resident domains first (most recently used first), then score order
+        std::vector<int> ro;
+        std::vector<char> seen(D, 0);
+        for (auto it = lru.blocks.rbegin(); it != lru.blocks.rend(); ++it) {
+          ro.push_back(it->second);
+          seen[it->second] = 1;
+        }
+        for (int d : order)
+          if (!seen[d]) ro.push_back(d);
+        traceOutOfCore(false, ro, S);
+      } else {
+        traceOutOfCore(false, order, S);
+      }
     } else {
       CK(cudaMemsetAsync(d_work, 0, 4 * kDepthBuckets, stream));
       const int nb = order_by_depth ? kDepthBuckets : 1;
@@ -824,7 +848,9 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     launches += 3;
     schedule(true, 0, d_shadow_count, d_shadow_list, S);
     if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, 0);
-    if (ooc) {
+    if (ooc && cfg.schedule_policy == 0) {
+      traceOutOfCore(true, order, S);
+    } else if (ooc) {
       // resident domains first (most recently used first), then the rest in score order
       std::vector<int> sorder;
       for (auto it = lru.blocks.rbegin(); it != lru.blocks.rend(); ++it) sorder.push_back(it->second);
@@ -859,6 +885,82 @@ void Tracer::traceWave(const Wave& w, bool capture) {
   }
 }
 
+// Screen bins of the primary rays.  Each domain box is projected through the
+// camera onto the image plane; the pixel rectangle of its 8 corners, widened
+// by two pixels, lists the domain in every bin it touches.  A box with a
+// corner at or behind the camera plane is listed everywhere.  A ray can only
+// pass the exact slab test of a box whose projection contains its pixel, so
+// the per-bin lists are supersets of what the full test would find.
+void Tracer::buildScreenBins() {
+  const int W = cfg.image_w, H = cfg.image_h;
+  bins_x = (W + kBinSize - 1) / kBinSize;
+  bins_y = (H + kBinSize - 1) / kBinSize;
+  const int nb = bins_x * bins_y;
+  std::vector<std::vector<uint16_t>> lists(nb);
+  // camera frame in double: P(u, v) = ll + u wv + v hv, viewing along -w
+  double pos[3], ll[3], wv[3], hv[3], fw[3];
+  for (int k = 0; k < 3; ++k) {
+    pos[k] = cam.pos[k];
+    ll[k] = cam.ll[k];
+    wv[k] = cam.wv[k];
+    hv[k] = cam.hv[k];
+  }
+  // forward = (centre of the image plane) - pos
+  for (int k = 0; k < 3; ++k) fw[k] = (ll[k] + 0.5 * wv[k] + 0.5 * hv[k]) - pos[k];
+  auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+  const double fw2 = dot(fw, fw), wv2 = dot(wv, wv), hv2 = dot(hv, hv);
+  for (int d = 0; d < D; ++d) {
+    const DomainDev& dd = hdoms[d];
+    double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
+    bool everywhere = false;
+    for (int c = 0; c < 8 && !everywhere; ++c) {
+      double q[3] = {((c & 1) ? dd.bmax[0] : dd.bmin[0]) - pos[0], ((c & 2) ? dd.bmax[1] : dd.bmin[1]) - pos[1],
+                     ((c & 4) ? dd.bmax[2] : dd.bmin[2]) - pos[2]};
+      double depth = dot(q, fw) / fw2;  // 1 on the image plane
+      if (!(depth > 1e-6)) {
+        everywhere = true;
+        break;
+      }
+      double p[3];
+      for (int k = 0; k < 3; ++k) p[k] = pos[k] + q[k] / depth - ll[k];
+      double u = dot(p, wv) / wv2, v = dot(p, hv) / hv2;
+      umin = std::min(umin, u);
+      umax = std::max(umax, u);
+      vmin = std::min(vmin, v);
+      vmax = std::max(vmax, v);
+    }
+    int x0 = 0, x1 = W - 1, y0 = 0, y1 = H - 1;
+    if (!everywhere) {
+      double fx0 = umin * W - 2.0, fx1 = umax * W + 2.0, fy0 = vmin * H - 2.0, fy1 = vmax * H + 2.0;
+      if (fx1 < 0.0 || fy1 < 0.0 || fx0 > W || fy0 > H) continue;
+      x0 = (int)std::max(0.0, std::floor(fx0));
+      x1 = (int)std::min((double)(W - 1), std::ceil(fx1));
+      y0 = (int)std::max(0.0, std::floor(fy0));
+      y1 = (int)std::min((double)(H - 1), std::ceil(fy1));
+    }
+    for (int by = y0 / kBinSize; by <= y1 / kBinSize; ++by)
+      for (int bx = x0 / kBinSize; bx <= x1 / kBinSize; ++bx) lists[by * bins_x + bx].push_back((uint16_t)d);
+  }
+  std::vector<uint32_t> start(nb + 1, 0);
+  for (int b = 0; b < nb; ++b) start[b + 1] = start[b] + (uint32_t)lists[b].size();
+  std::vector<uint16_t> ids(std::max<uint32_t>(start[nb], 1));
+  for (int b = 0; b < nb; ++b) std::copy(lists[b].begin(), lists[b].end(), ids.begin() + start[b]);
+  if ((size_t)(nb + 1) > bin_start_cap) {
+    devFree(d_bin_start);
+    bin_start_cap = nb + 1;
+    devAlloc(&d_bin_start, bin_start_cap);
+  }
+  if (ids.size() > bin_ids_cap) {
+    devFree(d_bin_ids);
+    bin_ids_cap = ids.size();
+    devAlloc(&d_bin_ids, bin_ids_cap);
+  }
+  CK(cudaMemcpyAsync(d_bin_start, start.data(), start.size() * 4, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_bin_ids, ids.data(), ids.size() * 2, cudaMemcpyHostToDevice, stream));
+  CK(cudaStreamSynchronize(stream));  // the host vectors are freed on return
+  h2d_bytes += start.size() * 4 + ids.size() * 2;
+}
+
 void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
   if (!has_scene) throw StateError("trace before set_scene");
   if (!has_camera) throw StateError("trace before set_camera");
@@ -880,6 +982,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
     CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
     CK(cudaEventRecord(ev_start, stream));
+    if (use_bins) buildScreenBins();
     for (size_t k = 0; k < waves.size(); ++k) traceWave(waves[k], cfg.debug_capture && k == 0);
     CK(cudaEventRecord(ev_stop, stream));
     Counters ctr;

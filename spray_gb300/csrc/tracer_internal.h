@@ -78,7 +78,9 @@ class Tracer {
   void freeScene();
   void freeBuffers();
   void traceWave(const Wave& w, bool capture);
-  void schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S);
+  void schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S,
+                bool primary = false);
+  void buildScreenBins();
   TraceArgs traceArgs(int order_by_depth, int S);
   SceneDev sceneDev() const;
   cudaEvent_t poolEvent();
@@ -129,6 +131,14 @@ class Tracer {
   uint32_t* d_segs = nullptr;
   DomNode* d_dnodes = nullptr;   // hierarchy over the domain boxes
   int dnode_count = 0;
+  // screen bins of candidate domains for the primary rays
+  static constexpr int kBinShift = 4;
+  static constexpr int kBinSize = 1 << kBinShift;
+  bool use_bins = true;
+  int bins_x = 0, bins_y = 0;
+  uint32_t* d_bin_start = nullptr;
+  uint16_t* d_bin_ids = nullptr;
+  size_t bin_start_cap = 0, bin_ids_cap = 0;
   LruSlots lru;
   int64_t domain_loads = 0;
 

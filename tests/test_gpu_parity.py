@@ -302,7 +302,8 @@ def test_scene_file_path(lib_built, oracle_mod, tmp_path):
     assert np.array_equal(bits(img), bits(wb))
 
 
-@pytest.mark.parametrize("kw", [dict(cache_size=16), dict(cache_size=5), dict(cache_bytes=3 << 20)])
+@pytest.mark.parametrize("kw", [dict(cache_size=16), dict(cache_size=5), dict(cache_bytes=3 << 20),
+                                dict(cache_size=16, schedule_policy=1)])
 def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     """Streaming domains through a small LRU cache changes loads, never the image."""
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
@@ -333,3 +334,17 @@ def test_out_of_core_queues_match_oracle(lib_built, oracle_mod, scene64):
     assert np.array_equal(q["domain"], oq["domain"]) and np.array_equal(q["ray"], oq["ray"])
     wb, _ = o.render_wavefront()
     assert np.array_equal(bits(img), bits(wb))
+
+
+def test_cache_aware_order_needs_fewer_loads(lib_built, scene64):
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=4, cache_size=24)
+    cam = scenes.orbit_camera(scene64)
+    loads = []
+    for pol in (0, 1):
+        t = sg.Tracer(cfg, schedule_policy=pol)
+        t.set_scene(scene64)
+        t.set_camera(*cam)
+        t.trace()
+        _, st = t.trace()
+        loads.append(st["domain_loads"])
+    assert loads[1] < loads[0]
