@@ -134,6 +134,7 @@ struct SchedArgs {
   uint32_t* list_cnt;
   uint32_t* hist;             // [nkeys][nwarps]
   long long* dstats;          // [D][list_size] ray counts per (domain, depth)
+  int want_stats;             // fill dstats (out-of-core order, debug hooks)
   uint2* entries;             // partitioned entries
   unsigned long long entry_cap;
   uint32_t* key_start;        // [nkeys + 1]

@@ -87,6 +87,8 @@ void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int n
 // spawned them, then list the other domains with their index in the full
 // sorted list as depth (ooc_isector.h:147-174).  Lists go to an arena, the
 // per-(key, warp) histogram to global memory.
+__device__ __forceinline__ bool fitsList(int cnt, int j) { return j < cnt; }
+
 __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
                                                              const DomainDev* __restrict__ doms,
                                                              int D, int nkeys, int nwarps) {
@@ -236,8 +238,19 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
           out[o++] = make_uint2(d | ((uint32_t)j << 16), __float_as_uint(lt[j]));
           uint32_t key = a.order_by_depth ? (uint32_t)(min(j, kDepthBuckets - 1) * D) + d : d;
           atomicAdd(&h[key], 1u);
-          if (j < a.list_size) atomicAdd((unsigned long long*)&a.dstats[(size_t)d * a.list_size + j], 1ull);
         }
+      }
+    }
+    if (a.want_stats) {
+      // DomainStats counts, one global atomic per distinct (domain, depth) of the warp
+      for (int j = 0; j < kMaxList; ++j) {
+        const bool has = active && fitsList(cnt, j) && j < a.list_size &&
+                         !(a.shadow && (int)ld[j] == origin);
+        if (!__any_sync(0xffffffffu, has)) break;
+        const uint32_t key = has ? ld[j] * (uint32_t)a.list_size + (uint32_t)j : 0xffffffffu;
+        const uint32_t m = __match_any_sync(0xffffffffu, key);
+        if (has && (__ffs(m) - 1) == lane)
+          atomicAdd((unsigned long long*)&a.dstats[key], (unsigned long long)__popc(m));
       }
     }
   }

@@ -688,6 +688,7 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.list_cnt = d_list_cnt;
   a.hist = d_hist;
   a.dstats = d_dstats;
+  a.want_stats = (ooc || cfg.debug_capture) ? 1 : 0;
   a.entries = d_entries;
   a.entry_cap = cap_entries;
   a.key_start = d_key_start;
