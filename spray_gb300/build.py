@@ -36,8 +36,13 @@ def _needs(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
+EXTRA_DEFINES = [d for d in os.environ.get("SPRAY_BUILD_DEFINES", "").split() if d]
+
+
 def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile every translation unit that changed and link the library."""
+    """Compile every translation unit that changed and link the library.
+
+    SPRAY_BUILD_DEFINES (space-separated -D flags) sets tuning constants."""
     BUILD.mkdir(exist_ok=True)
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "spray_gpu.h"]
     jobs = []
@@ -47,13 +52,13 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         o = BUILD / (src + ".o")
         objs.append(o)
         if force or _needs(o, [s] + headers):
-            jobs.append([NVCC] + NVCCFLAGS + ["-c", str(s), "-o", str(o)])
+            jobs.append([NVCC] + NVCCFLAGS + EXTRA_DEFINES + ["-c", str(s), "-o", str(o)])
     for src in CPP_SOURCES:
         s = CSRC / src
         o = BUILD / (src + ".o")
         objs.append(o)
         if force or _needs(o, [s] + headers):
-            jobs.append(["g++"] + CXXFLAGS + ["-c", str(s), "-o", str(o)])
+            jobs.append(["g++"] + CXXFLAGS + EXTRA_DEFINES + ["-c", str(s), "-o", str(o)])
     procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
              for j in jobs]
     failed = []

@@ -44,8 +44,11 @@ struct BinNode {  // binary build node
   bool leaf() const { return left < 0; }
 };
 
+#ifndef SPRAY_SAH_TRAVERSAL_COST
+#define SPRAY_SAH_TRAVERSAL_COST 1.0f
+#endif
 constexpr int kBins = 16;
-constexpr float kTraversalCost = 1.0f;
+constexpr float kTraversalCost = SPRAY_SAH_TRAVERSAL_COST;  // relative to one triangle test
 constexpr float kTriCost = 1.0f;
 
 struct Builder {

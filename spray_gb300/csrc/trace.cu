@@ -19,6 +19,9 @@ namespace {
 // Box test slack: (1 + 2*gamma(3)) rounded up (Ize, "Robust BVH Ray
 // Traversal", JCGT 2(2), 2013), so rounding never culls a box the ray touches.
 constexpr float kBoxSlack = 1.0000004f;
+#ifndef SPRAY_TRACE_MIN_BLOCKS
+#define SPRAY_TRACE_MIN_BLOCKS 4
+#endif
 constexpr int kStack = 64;
 
 struct TravRay {
@@ -262,7 +265,7 @@ __device__ __forceinline__ uint32_t entryOf(const TraceArgs& a, const uint32_t* 
 
 }  // namespace
 
-__global__ void __launch_bounds__(256, 4) kTraceClosest(TraceArgs a) {
+__global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
   uint32_t* sbeg = skeys + a.nkeys + 1;
@@ -360,7 +363,7 @@ void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nbloc
   kResolve<<<nblocks, 256, 0, s>>>(a, hit_ns);
 }
 
-__global__ void __launch_bounds__(256, 4) kTraceOccluded(TraceArgs a) {
+__global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
   uint32_t* sbeg = skeys + a.nkeys + 1;
