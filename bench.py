@@ -35,6 +35,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mrays/s at <=1e-3 image RMSE, learned vs plain scheduler; domain loads/frame"
+POLICIES = {"plain": (0, "plain speculative"), "resident": (1, "resident domains first"),
+            "batched": (2, "batched passes (shadow b + radiance b+1), culled domains not loaded")}
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
@@ -172,6 +174,9 @@ def main():
     ap.add_argument("--cpu-scale", type=int, default=2, help="CPU baseline frame downscale per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
+    ap.add_argument("--policy", default="plain", choices=list(POLICIES),
+                    help="out-of-core domain order (plain: the reference's DomainStats order)")
+    ap.add_argument("--ooc-batch", type=int, default=0, help="domains per batch under --policy batched")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide the image size (profiling captures on a small frame only)")
     args = ap.parse_args()
@@ -227,6 +232,8 @@ def main():
     if args.scale > 1:
         cfg["image_w"] = max(8, cfg["image_w"] // args.scale)
         cfg["image_h"] = max(8, cfg["image_h"] // args.scale)
+    cfg["schedule_policy"] = POLICIES[args.policy][0]
+    cfg["ooc_batch"] = args.ooc_batch
     tracer = sg.Tracer(cfg, device=local)
     tracer.set_scene(scene)
     # weak scaling: each rank renders its own seeded view of the scene
@@ -303,7 +310,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": allmax(dev_ms / args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded wavelet isosurface scene, seeded orbit camera)",
-        "config": {"workload": describe(args.config, spec, cfg), "scheduler": "plain speculative",
+        "config": {"workload": describe(args.config, spec, cfg), "scheduler": POLICIES[args.policy][1],
                    "domains": len(scene.domains), "triangles": s0["scene_triangles"],
                    "image": [W, H], "spp": cfg["pixel_samples"], "bounces": cfg["bounces"],
                    "l2": "256 MiB buffer written before every timed frame; ray state > L2",

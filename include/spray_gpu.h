@@ -72,7 +72,12 @@ typedef struct spray_gpu_config {
   int32_t debug_capture;        /* keep the first wavefront's stage buffers for the debug hooks (0) */
   int32_t device;               /* CUDA device ordinal (0) */
   int32_t schedule_policy;      /* out-of-core domain order: 0 DomainStats score order (the
-                                   reference's), 1 resident domains first (0) */
+                                   reference's), 1 resident domains first, 2 batched: the shadow
+                                   rays of depth b and the radiance rays of depth b+1 share one
+                                   pass over the domains, resident domains go first, and a domain
+                                   whose entries were all culled before its turn is not loaded (0) */
+  int32_t ooc_batch;            /* out-of-core, policy 2: domains made resident per traced batch;
+                                   0 = a quarter of the cache capacity (0) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as

@@ -39,6 +39,7 @@ class ConfigC(C.Structure):
         ("rr_depth", C.c_int32), ("cull", C.c_int32), ("cache_bytes", C.c_int64),
         ("wave_samples", C.c_int64), ("debug_capture", C.c_int32), ("device", C.c_int32),
         ("schedule_policy", C.c_int32),
+        ("ooc_batch", C.c_int32),
     ]
 
 

@@ -209,5 +209,25 @@ void launchRetireImpl(cudaStream_t s, float4* image, int64_t npix, int spp, cons
                       double scale, int nblocks);
 void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int list_size,
                   long long* scores, int32_t* order);
+// Out of core: entries of each listed domain that are still live.  A radiance
+// entry is dead when its ray already holds a hit nearer than the entry's
+// domain (its record is then written as a miss, as the trace kernel would);
+// a shadow entry is dead when its ray is already occluded.  live[d] counts
+// radiance entries and live[D + d] shadow entries.  Either queue may be null.
+struct LiveArgs {
+  const uint2* rentries;
+  const uint32_t* rkey_start;
+  const uint64_t* ray_key;
+  uint64_t* rec_key;
+  const uint2* sentries;
+  const uint32_t* skey_start;
+  const uint8_t* occluded;
+  const int32_t* domains;  // the domains to count
+  int ndomains;
+  int D;
+  int cull;
+  uint32_t* live;
+};
+void launchCountLive(cudaStream_t s, const LiveArgs& a);
 
 }  // namespace spray

@@ -408,4 +408,52 @@ void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {
   kTraceOccluded<<<nblocks, 256, smem, s>>>(a);
 }
 
+// One block per listed domain; the same cull test as kTraceClosest.
+__global__ void __launch_bounds__(256) kCountLive(LiveArgs a) {
+  __shared__ uint32_t wsum[2][8];
+  const int d = a.domains[blockIdx.x];
+  uint32_t nr = 0, ns = 0;
+  if (a.rentries) {
+    const uint32_t e0 = a.rkey_start[d], e1 = a.rkey_start[d + 1];
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const uint2 ent = a.rentries[e];
+      bool live = true;
+      if (a.cull) {
+        const uint64_t cur = a.ray_key[ent.x & kRayIdMask];
+        live = !(cur != kNoHit && __uint_as_float(ent.y) > hitKeyT(cur));
+      }
+      if (live) ++nr;
+      else a.rec_key[e] = kNoHit;
+    }
+  }
+  if (a.sentries) {
+    const uint32_t e0 = a.skey_start[d], e1 = a.skey_start[d + 1];
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x)
+      if (!a.occluded[a.sentries[e].x & kRayIdMask]) ++ns;
+  }
+  for (int o = 16; o; o >>= 1) {
+    nr += __shfl_down_sync(0xffffffffu, nr, o);
+    ns += __shfl_down_sync(0xffffffffu, ns, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    wsum[0][warp] = nr;
+    wsum[1][warp] = ns;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tr = 0, ts = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      tr += wsum[0][w];
+      ts += wsum[1][w];
+    }
+    a.live[d] = tr;
+    a.live[a.D + d] = ts;
+  }
+}
+
+void launchCountLive(cudaStream_t s, const LiveArgs& a) {
+  if (a.ndomains > 0) kCountLive<<<a.ndomains, 256, 0, s>>>(a);
+}
+
 }  // namespace spray

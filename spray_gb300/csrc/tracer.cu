@@ -139,6 +139,9 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   if (cfg.max_samples_per_rank <= 0) throw std::invalid_argument("max_samples_per_rank must be positive");
   if (cfg.num_ranks <= 0 || cfg.rank < 0 || cfg.rank >= cfg.num_ranks)
     throw std::invalid_argument("rank must be in [0, num_ranks)");
+  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 2)
+    throw std::invalid_argument("schedule_policy must be 0, 1 or 2");
+  if (cfg.ooc_batch < 0) throw std::invalid_argument("ooc_batch must be >= 0");
   int ndev = 0;
   CK(cudaGetDeviceCount(&ndev));
   if (cfg.device < 0 || cfg.device >= ndev) throw CudaError("no CUDA device " + std::to_string(cfg.device));
@@ -166,6 +169,10 @@ void Tracer::freeScene() {
   h_pinned = nullptr;
   if (h_stage) cudaFreeHost(h_stage);
   h_stage = nullptr;
+  if (h_live) cudaFreeHost(h_live);
+  h_live = nullptr;
+  devFree(d_live);
+  devFree(d_live_doms);
   ooc = false;
   devFree(d_segs);
   devFree(d_dnodes);
@@ -212,6 +219,10 @@ void Tracer::freeBuffers() {
   devFree(d_entries);
   devFree(d_key_start);
   devFree(d_num_entries);
+  devFree(d_sentries);
+  devFree(d_skey_start);
+  devFree(d_snum_entries);
+  devFree(d_alive_idx_prev);
   devFree(d_rec_key);
   devFree(d_rec_attr);
   devFree(d_work);
@@ -430,8 +441,12 @@ void Tracer::setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t
   devAlloc(&d_faces, 3 * (size_t)capacity * max_tris);
   devAlloc(&d_colors, (size_t)capacity * max_verts);
   devAlloc(&d_normals, 3 * (size_t)capacity * max_verts);
-  devAlloc(&d_segs, 2 * (size_t)D + 2);
-  CK(cudaHostAlloc((void**)&h_stage, D * sizeof(DomainDev) + (2 * (size_t)D + 2) * 4, cudaHostAllocDefault));
+  // two segment tables (radiance, shadow) of D + 1 begins and D + 1 prefixes each
+  devAlloc(&d_segs, 4 * (size_t)D + 4);
+  CK(cudaHostAlloc((void**)&h_stage, D * sizeof(DomainDev) + (4 * (size_t)D + 4) * 4, cudaHostAllocDefault));
+  devAlloc(&d_live, 2 * (size_t)D);
+  devAlloc(&d_live_doms, D);
+  CK(cudaHostAlloc((void**)&h_live, 3 * (size_t)D * 4, cudaHostAllocDefault));
   CK(cudaMemcpy(d_domains, hdoms.data(), D * sizeof(DomainDev), cudaMemcpyHostToDevice));
   lru.init(capacity);
 }
@@ -646,6 +661,12 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_entries, E);
   devAlloc(&d_key_start, nkeys + 1);
   devAlloc(&d_num_entries, 1);
+  if (ooc && cfg.schedule_policy == 2) {
+    devAlloc(&d_sentries, E);
+    devAlloc(&d_skey_start, nkeys + 1);
+    devAlloc(&d_snum_entries, 1);
+    devAlloc(&d_alive_idx_prev, N);
+  }
   devAlloc(&d_rec_key, E);
   devAlloc(&d_rec_attr, E);
   devAlloc(&d_work, kDepthBuckets);
@@ -661,7 +682,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
 }
 
 void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S,
-                      bool primary) {
+                      bool primary, bool into_shadow_queues) {
   SchedArgs a{};
   a.shadow = shadow;
   a.count = count;
@@ -689,10 +710,10 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.hist = d_hist;
   a.dstats = d_dstats;
   a.want_stats = (ooc || cfg.debug_capture) ? 1 : 0;
-  a.entries = d_entries;
+  a.entries = into_shadow_queues ? d_sentries : d_entries;
   a.entry_cap = cap_entries;
-  a.key_start = d_key_start;
-  a.num_entries = d_num_entries;
+  a.key_start = into_shadow_queues ? d_skey_start : d_key_start;
+  a.num_entries = into_shadow_queues ? d_snum_entries : d_num_entries;
   a.ctr = d_ctr;
   CK(cudaMemsetAsync(d_arena_top, 0, sizeof(unsigned long long), stream));
   launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp);
@@ -743,8 +764,8 @@ cudaEvent_t Tracer::poolEvent() {
   return ev_pool[ev_used++];
 }
 
-void Tracer::traceWave(const Wave& w, bool capture) {
-  const int S = std::max(slots(), 1);
+// Uploads the wave's tiles and generates its primary rays.
+void Tracer::beginWave(const Wave& w) {
   const int spp = cfg.pixel_samples;
   std::vector<TileDev> td(w.num_tiles);
   int64_t base = 0;
@@ -759,6 +780,40 @@ void Tracer::traceWave(const Wave& w, bool capture) {
   launchGenPrimary(stream, cam, d_tiles, w.num_tiles, w.samples, spp, cfg.image_w, rays[0],
                    d_alive_list, d_alive_count, d_alive_idx, d_ctr);
   launches += 1;
+}
+
+ShadeArgs Tracer::shadeArgs(int b, int S) {
+  ShadeArgs sa{};
+  sa.scene = sceneDev();
+  sa.count = d_alive_count;
+  sa.list = d_alive_list;
+  sa.rays = rays[cur];
+  sa.next = rays[cur ^ 1];
+  sa.next_flag = d_next_flag;
+  sa.ray_key = d_ray_key;
+  sa.hit_ns = d_hit_ns;
+  sa.sh = sh;
+  sa.shadow_flag = d_shadow_flag;
+  sa.slots = S;
+  sa.depth = b;
+  sa.ao_mode = cfg.ao_mode;
+  sa.ao_samples = cfg.ao_samples;
+  sa.bounces = cfg.bounces;
+  sa.rr_depth = cfg.rr_depth;
+  sa.ao_light_shadow = cfg.ao_light_shadow;
+  sa.ao_max_distance = cfg.ao_max_distance;
+  for (int c = 0; c < 3; ++c) sa.ks[c] = cfg.ks[c];
+  sa.shininess = cfg.shininess;
+  sa.lights = d_lights;
+  sa.num_lights = (int)lights.size();
+  sa.ctr = d_ctr;
+  return sa;
+}
+
+void Tracer::traceWave(const Wave& w, bool capture) {
+  const int S = std::max(slots(), 1);
+  const int spp = cfg.pixel_samples;
+  beginWave(w);
   const int order_by_depth = (cfg.cull && !ooc) ? 1 : 0;
   const int nblk = num_sms * 4;
   for (int b = 0; b < cfg.bounces; ++b) {
@@ -785,16 +840,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     if (ooc) {
       order = scoreOrder();
       if (cfg.schedule_policy == 1) {
-        // resident domains first (most recently used first), then score order
-        std::vector<int> ro;
-        std::vector<char> seen(D, 0);
-        for (auto it = lru.blocks.rbegin(); it != lru.blocks.rend(); ++it) {
-          ro.push_back(it->second);
-          seen[it->second] = 1;
-        }
-        for (int d : order)
-          if (!seen[d]) ro.push_back(d);
-        traceOutOfCore(false, ro, S);
+        traceOutOfCore(false, residentFirst(order), S);
       } else {
         traceOutOfCore(false, order, S);
       }
@@ -817,31 +863,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     if (capture) captureHits(b);
     // shade
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
-    ShadeArgs sa{};
-    sa.scene = sceneDev();
-    sa.count = d_alive_count;
-    sa.list = d_alive_list;
-    sa.rays = rays[cur];
-    sa.next = rays[cur ^ 1];
-    sa.next_flag = d_next_flag;
-    sa.ray_key = d_ray_key;
-    sa.hit_ns = d_hit_ns;
-    sa.sh = sh;
-    sa.shadow_flag = d_shadow_flag;
-    sa.slots = S;
-    sa.depth = b;
-    sa.ao_mode = cfg.ao_mode;
-    sa.ao_samples = cfg.ao_samples;
-    sa.bounces = cfg.bounces;
-    sa.rr_depth = cfg.rr_depth;
-    sa.ao_light_shadow = cfg.ao_light_shadow;
-    sa.ao_max_distance = cfg.ao_max_distance;
-    for (int c = 0; c < 3; ++c) sa.ks[c] = cfg.ks[c];
-    sa.shininess = cfg.shininess;
-    sa.lights = d_lights;
-    sa.num_lights = (int)lights.size();
-    sa.ctr = d_ctr;
-    launchShade(stream, sa, nblk);
+    launchShade(stream, shadeArgs(b, S), nblk);
     launches += 1;
     // shadow rays -> queues -> occlusion
     launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
@@ -852,14 +874,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     if (ooc && cfg.schedule_policy == 0) {
       traceOutOfCore(true, order, S);
     } else if (ooc) {
-      // resident domains first (most recently used first), then the rest in score order
-      std::vector<int> sorder;
-      for (auto it = lru.blocks.rbegin(); it != lru.blocks.rend(); ++it) sorder.push_back(it->second);
-      std::vector<char> seen(D, 0);
-      for (int d : sorder) seen[d] = 1;
-      for (int d : order)
-        if (!seen[d]) sorder.push_back(d);
-      traceOutOfCore(true, sorder, S);
+      traceOutOfCore(true, residentFirst(order), S);
     } else {
       CK(cudaMemsetAsync(d_work, 0, 4, stream));
       TraceArgs to = traceArgs(0, S);
@@ -883,6 +898,180 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       launches += 3;
       cur ^= 1;
     }
+  }
+}
+
+// Resident domains first (most recently used first), then the rest of `order`.
+std::vector<int> Tracer::residentFirst(const std::vector<int>& order) const {
+  std::vector<int> ro;
+  std::vector<char> seen(D, 0);
+  for (auto it = lru.blocks.rbegin(); it != lru.blocks.rend(); ++it) {
+    ro.push_back(it->second);
+    seen[it->second] = 1;
+  }
+  for (int d : order)
+    if (!seen[d]) ro.push_back(d);
+  return ro;
+}
+
+// Out of core, batched: one pass over the domains traces the radiance queues
+// and/or the shadow queues while each domain is resident.  Before each batch
+// the live entries of every remaining domain are counted on the device; a
+// domain none of whose entries is still live (all culled by nearer hits, or
+// all of its shadow rays already occluded) is dropped without being loaded.
+// Dropping changes neither hit nor occlusion: a culled entry cannot beat its
+// ray's hit, and an occluded shadow ray stays occluded.
+void Tracer::oocPass(bool with_r, bool with_s, int S) {
+  std::vector<uint32_t> rk(D + 1, 0), sk(D + 1, 0);
+  uint32_t rn = 0, sn = 0;
+  if (with_r) {
+    CK(cudaMemcpyAsync(rk.data(), d_key_start, (D + 1) * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&rn, d_num_entries, 4, cudaMemcpyDeviceToHost, stream));
+  }
+  if (with_s) {
+    CK(cudaMemcpyAsync(sk.data(), d_skey_start, (D + 1) * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&sn, d_snum_entries, 4, cudaMemcpyDeviceToHost, stream));
+  }
+  CK(cudaStreamSynchronize(stream));
+  // a queue that overflowed holds no entries; the frame is traced again with larger queues
+  if (with_r && rk[D] != rn) with_r = false;
+  if (with_s && sk[D] != sn) with_s = false;
+  if (!with_r && !with_s) return;
+  std::vector<int> remaining;
+  for (int d : residentFirst(scoreOrder()))
+    if ((with_r && rk[d + 1] > rk[d]) || (with_s && sk[d + 1] > sk[d])) remaining.push_back(d);
+  const int B = cfg.ooc_batch > 0 ? std::min(cfg.ooc_batch, cache_capacity)
+                                   : std::max(1, cache_capacity / 4);
+  int32_t* hdoms_list = reinterpret_cast<int32_t*>(h_live);
+  uint32_t* hlive = h_live + D;
+  while (!remaining.empty()) {
+    std::memcpy(hdoms_list, remaining.data(), remaining.size() * 4);
+    CK(cudaMemcpyAsync(d_live_doms, hdoms_list, remaining.size() * 4, cudaMemcpyHostToDevice, stream));
+    LiveArgs la{};
+    la.rentries = with_r ? d_entries : nullptr;
+    la.rkey_start = d_key_start;
+    la.ray_key = d_ray_key;
+    la.rec_key = d_rec_key;
+    la.sentries = with_s ? d_sentries : nullptr;
+    la.skey_start = d_skey_start;
+    la.occluded = sh.occluded;
+    la.domains = d_live_doms;
+    la.ndomains = (int)remaining.size();
+    la.D = D;
+    la.cull = cfg.cull;
+    la.live = d_live;
+    launchCountLive(stream, la);
+    launches += 1;
+    CK(cudaMemcpyAsync(hlive, d_live, 2 * (size_t)D * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    std::vector<int> batch, rest;
+    for (int d : remaining) {
+      const bool lr = with_r && hlive[d] > 0, ls = with_s && hlive[D + d] > 0;
+      if (!lr && !ls) continue;  // nothing left to trace here: not loaded
+      if ((int)batch.size() < B) batch.push_back(d);
+      else rest.push_back(d);
+    }
+    if (batch.empty()) break;
+    for (int d : batch) {
+      int slot, evicted;
+      if (!lru.load(d, &slot, &evicted)) {
+        if (evicted >= 0) hdoms[evicted].resident = 0;
+        loadDomain(d, slot);
+      }
+    }
+    // domain table, then one segment table per queue: begins (D + 1) and prefixes (D + 1)
+    DomainDev* sd = reinterpret_cast<DomainDev*>(h_stage);
+    std::memcpy(sd, hdoms.data(), D * sizeof(DomainDev));
+    uint32_t* seg = reinterpret_cast<uint32_t*>(h_stage + D * sizeof(DomainDev));
+    int nseg[2] = {0, 0};
+    for (int q = 0; q < 2; ++q) {
+      const std::vector<uint32_t>& ks = q == 0 ? rk : sk;
+      const bool on = q == 0 ? with_r : with_s;
+      uint32_t* beg = seg + q * (2 * D + 2);
+      uint32_t* pre = beg + D + 1;
+      uint32_t run = 0;
+      if (on)
+        for (int d : batch) {
+          if (hlive[q * D + d] == 0) continue;
+          beg[nseg[q]] = ks[d];
+          pre[nseg[q]] = run;
+          run += ks[d + 1] - ks[d];
+          ++nseg[q];
+        }
+      pre[nseg[q]] = run;
+    }
+    CK(cudaMemcpyAsync(d_domains, sd, D * sizeof(DomainDev), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_segs, seg, (4 * (size_t)D + 4) * 4, cudaMemcpyHostToDevice, stream));
+    for (int q = 0; q < 2; ++q) {
+      if (nseg[q] == 0) continue;
+      CK(cudaMemsetAsync(d_work, 0, 4, stream));
+      TraceArgs ta = traceArgs(0, S);
+      if (q == 1) {
+        ta.entries = d_sentries;
+        ta.key_start = d_skey_start;
+        ta.num_entries = d_snum_entries;
+      }
+      ta.seg_begin = d_segs + q * (2 * D + 2);
+      ta.seg_prefix = ta.seg_begin + D + 1;
+      ta.nseg = nseg[q];
+      cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
+      CK(cudaEventRecord(e0, stream));
+      if (q == 1) launchTraceOccluded(stream, ta, num_sms * 4);
+      else launchTraceClosest(stream, ta, num_sms * 4);
+      CK(cudaEventRecord(e1, stream));
+      (q == 1 ? occl_events : trace_events).push_back({e0, e1});
+      launches += 1;
+    }
+    // the staging buffers are reused by the next batch
+    CK(cudaStreamSynchronize(stream));
+    remaining.swap(rest);
+  }
+}
+
+// Out of core, batched (schedule_policy 2): the shadow rays of depth b and the
+// radiance rays of depth b + 1 are both spawned by the shader at depth b and
+// are independent of each other, so they are queued together and traced in
+// one pass over the domains; depth b is retired after that pass.  The image is
+// the same as the unbatched order's: only the order of the traced entries
+// changes, and hits fold through the order-independent packed atomicMin.
+void Tracer::traceWaveBatched(const Wave& w) {
+  const int S = std::max(slots(), 1);
+  const int spp = cfg.pixel_samples;
+  const int nblk = num_sms * 4;
+  beginWave(w);
+  auto scheduleRadiance = [&](bool primary) {
+    CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
+    cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
+    CK(cudaEventRecord(s0, stream));
+    schedule(false, 0, d_alive_count, d_alive_list, S, primary);
+    CK(cudaEventRecord(s1, stream));
+    sched_events.push_back({s0, s1});
+  };
+  scheduleRadiance(true);
+  oocPass(true, false, S);
+  for (int b = 0; b < cfg.bounces; ++b) {
+    TraceArgs ta = traceArgs(0, S);
+    launchResolve(stream, ta, d_hit_ns, nblk);
+    CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
+    launchShade(stream, shadeArgs(b, S), nblk);
+    launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
+                  nullptr, d_block_tmp, compact_blocks);
+    launches += 5;
+    schedule(true, 0, d_shadow_count, d_shadow_list, S, false, true);
+    const int32_t* retire_idx = d_alive_idx;
+    const bool more = b + 1 < cfg.bounces;
+    if (more) {
+      std::swap(d_alive_idx, d_alive_idx_prev);
+      launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count,
+                    d_alive_idx, d_block_tmp, compact_blocks);
+      launches += 3;
+      cur ^= 1;
+      scheduleRadiance(false);
+    }
+    oocPass(more, true, S);
+    launchRetireImpl(stream, d_image, w.samples / spp, spp, d_pixid, retire_idx, sh, d_shadow_flag, S,
+                     1.0 / (double)spp, nblk);
+    launches += 1;
   }
 }
 
@@ -984,7 +1173,11 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
     CK(cudaEventRecord(ev_start, stream));
     if (use_bins) buildScreenBins();
-    for (size_t k = 0; k < waves.size(); ++k) traceWave(waves[k], cfg.debug_capture && k == 0);
+    for (size_t k = 0; k < waves.size(); ++k) {
+      const bool capture = cfg.debug_capture && k == 0;
+      if (ooc && cfg.schedule_policy == 2 && !capture) traceWaveBatched(waves[k]);
+      else traceWave(waves[k], capture);
+    }
     CK(cudaEventRecord(ev_stop, stream));
     Counters ctr;
     CK(cudaMemcpyAsync(&ctr, d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, stream));

@@ -78,8 +78,11 @@ class Tracer {
   void freeScene();
   void freeBuffers();
   void traceWave(const Wave& w, bool capture);
+  void traceWaveBatched(const Wave& w);
+  void beginWave(const Wave& w);
+  ShadeArgs shadeArgs(int b, int S);
   void schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S,
-                bool primary = false);
+                bool primary = false, bool into_shadow_queues = false);
   void buildScreenBins();
   TraceArgs traceArgs(int order_by_depth, int S);
   SceneDev sceneDev() const;
@@ -93,6 +96,8 @@ class Tracer {
                       size_t max_verts, size_t slot_bytes);
   void loadDomain(int d, int slot);
   void traceOutOfCore(bool shadow, const std::vector<int>& order, int S);
+  void oocPass(bool with_radiance, bool with_shadow, int S);
+  std::vector<int> residentFirst(const std::vector<int>& order) const;
   std::vector<int> scoreOrder();
 
   spray_gpu_config cfg;
@@ -170,6 +175,13 @@ class Tracer {
   uint32_t* d_list_cnt = nullptr;
   uint32_t* d_hist = nullptr;
   long long* d_dstats = nullptr;
+  uint2* d_sentries = nullptr;     // batched out of core: shadow queues beside the radiance ones
+  uint32_t* d_skey_start = nullptr;
+  uint32_t* d_snum_entries = nullptr;
+  int32_t* d_alive_idx_prev = nullptr;  // alive index of the depth being retired
+  uint32_t* d_live = nullptr;      // live entries per domain (radiance, shadow)
+  int32_t* d_live_doms = nullptr;
+  uint32_t* h_live = nullptr;      // pinned: domain list (D) + live counts (2 D)
   uint2* d_entries = nullptr;
   uint32_t* d_key_start = nullptr;
   uint32_t* d_num_entries = nullptr;

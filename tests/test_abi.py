@@ -58,3 +58,12 @@ def test_invalid_config_rejected(lib_built):
     with pytest.raises(sg.SprayError) as e:
         sg.Tracer(image_w=0, image_h=8)
     assert e.value.code in (sg.EINVAL, sg.ECUDA)
+
+
+@pytest.mark.parametrize("kw", [dict(schedule_policy=3), dict(schedule_policy=-1), dict(ooc_batch=-1)])
+def test_out_of_core_options_validated(lib_built, kw):
+    """Options are checked before any device is touched."""
+    import spray_gb300 as sg
+    with pytest.raises(sg.SprayError) as e:
+        sg.Tracer(image_w=8, image_h=8, **kw)
+    assert e.value.code == sg.EINVAL

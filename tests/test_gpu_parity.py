@@ -303,7 +303,10 @@ def test_scene_file_path(lib_built, oracle_mod, tmp_path):
 
 
 @pytest.mark.parametrize("kw", [dict(cache_size=16), dict(cache_size=5), dict(cache_bytes=3 << 20),
-                                dict(cache_size=16, schedule_policy=1)])
+                                dict(cache_size=16, schedule_policy=1),
+                                dict(cache_size=16, schedule_policy=2),
+                                dict(cache_size=5, schedule_policy=2, ooc_batch=1),
+                                dict(cache_bytes=3 << 20, schedule_policy=2, ooc_batch=3)])
 def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     """Streaming domains through a small LRU cache changes loads, never the image."""
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
@@ -340,7 +343,7 @@ def test_cache_aware_order_needs_fewer_loads(lib_built, scene64):
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=4, cache_size=24)
     cam = scenes.orbit_camera(scene64)
     loads = []
-    for pol in (0, 1):
+    for pol in (0, 1, 2):
         t = sg.Tracer(cfg, schedule_policy=pol)
         t.set_scene(scene64)
         t.set_camera(*cam)
@@ -348,3 +351,24 @@ def test_cache_aware_order_needs_fewer_loads(lib_built, scene64):
         _, st = t.trace()
         loads.append(st["domain_loads"])
     assert loads[1] < loads[0]
+    assert loads[2] < loads[1]
+
+
+def test_batched_pass_skips_fully_culled_domains(lib_built, scene64):
+    """Batched out-of-core passes trace no more entries than the plain order and
+    never load a domain whose entries were all culled, with the same image."""
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3, cache_size=16)
+    cam = scenes.orbit_camera(scene64)
+    out = {}
+    for pol, batch in ((0, 0), (2, 2)):
+        t = sg.Tracer(cfg, schedule_policy=pol, ooc_batch=batch)
+        t.set_scene(scene64)
+        t.set_camera(*cam)
+        out[pol] = t.trace()
+    (img0, st0), (img2, st2) = out[0], out[2]
+    assert np.array_equal(bits(img0), bits(img2))
+    assert st2["rays_shadow"] == st0["rays_shadow"] and st2["rays_bounce"] == st0["rays_bounce"]
+    assert st2["visits_radiance"] <= st0["visits_radiance"]
+    assert st2["visits_shadow"] <= st0["visits_shadow"]
+    assert st2["domain_loads"] < st0["domain_loads"]
+
