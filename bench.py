@@ -322,6 +322,7 @@ def main():
         "visits_per_ray": (s0["visits_radiance"] + s0["visits_shadow"]) / max(nrays, 1),
         "visits_culled": s0["visits_culled"],
         "domain_loads_per_frame": s0["domain_loads"],
+        "breakdown_ms_per_frame": {k: s0[f"{k}_ms"] for k in ("frame", "schedule", "trace", "occlude", "h2d")},
         "h2d_bytes_per_frame": s0["h2d_bytes"],
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,

@@ -76,8 +76,9 @@ typedef struct spray_gpu_config {
                                    rays of depth b and the radiance rays of depth b+1 share one
                                    pass over the domains, resident domains go first, and a domain
                                    whose entries were all culled before its turn is not loaded (0) */
-  int32_t ooc_batch;            /* out-of-core, policy 2: domains made resident per traced batch;
-                                   0 = a quarter of the cache capacity (0) */
+  int32_t ooc_batch;            /* out-of-core, policy 2: domains made resident per traced batch,
+                                   at most half the cache capacity so that the next batch's copies
+                                   overlap this batch's traces; 0 = half the capacity (0) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as
@@ -133,6 +134,7 @@ typedef struct spray_gpu_stats {
   int64_t tris_shadow;      /* triangles tested by occlusion traversal */
   int64_t scene_triangles;  /* triangles in the scene */
   int64_t scene_bytes;      /* device bytes of BVH nodes, triangles and shading data */
+  double h2d_ms;            /* device time of the out-of-core domain copies (copy stream) */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

@@ -66,6 +66,7 @@ class StatsC(C.Structure):
         ("trace_launches", C.c_int64), ("occlude_launches", C.c_int64),
         ("nodes_radiance", C.c_int64), ("tris_radiance", C.c_int64), ("nodes_shadow", C.c_int64),
         ("tris_shadow", C.c_int64), ("scene_triangles", C.c_int64), ("scene_bytes", C.c_int64),
+        ("h2d_ms", C.c_double),
     ]
 
     def asdict(self) -> dict:

@@ -148,6 +148,7 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   CK(cudaSetDevice(cfg.device));
   CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, cfg.device));
   CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&cstream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&ev_start));
   CK(cudaEventCreate(&ev_stop));
   devAlloc(&d_ctr, 1);
@@ -162,6 +163,7 @@ Tracer::~Tracer() {
   if (ev_start) cudaEventDestroy(ev_start);
   if (ev_stop) cudaEventDestroy(ev_stop);
   if (stream) cudaStreamDestroy(stream);
+  if (cstream) cudaStreamDestroy(cstream);
 }
 
 void Tracer::freeScene() {
@@ -484,8 +486,8 @@ bool LruSlots::load(int domain, int* slot, int* evicted) {
   return false;
 }
 
-// Copies a domain into a device slot (stream-ordered, from pinned memory).
-void Tracer::loadDomain(int d, int slot) {
+// Copies a domain into a device slot (ordered on stream s, from pinned memory).
+void Tracer::loadDomain(int d, int slot, cudaStream_t s) {
   DomainDev& dd = hdoms[d];
   const size_t nn = (size_t)dd.num_nodes, nt = (size_t)dd.num_tris;
   // vertex count: colours + normals follow the faces in the pinned block
@@ -497,15 +499,15 @@ void Tracer::loadDomain(int d, int slot) {
   dd.vert_base = (int32_t)(slot * slot_verts);
   dd.resident = 1;
   size_t b_nodes = nn * sizeof(BvhNode4), b_tris = 3 * nt * sizeof(float4), b_faces = 3 * nt * 4;
-  CK(cudaMemcpyAsync(d_nodes + dd.node_base, q, b_nodes, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_nodes + dd.node_base, q, b_nodes, cudaMemcpyHostToDevice, s));
   q += b_nodes;
-  CK(cudaMemcpyAsync(d_tris + 3 * (size_t)dd.tri_base, q, b_tris, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_tris + 3 * (size_t)dd.tri_base, q, b_tris, cudaMemcpyHostToDevice, s));
   q += b_tris;
-  CK(cudaMemcpyAsync(d_faces + 3 * (size_t)dd.face_base, q, b_faces, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_faces + 3 * (size_t)dd.face_base, q, b_faces, cudaMemcpyHostToDevice, s));
   q += b_faces;
-  CK(cudaMemcpyAsync(d_colors + dd.vert_base, q, nv * 4, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_colors + dd.vert_base, q, nv * 4, cudaMemcpyHostToDevice, s));
   q += nv * 4;
-  CK(cudaMemcpyAsync(d_normals + 3 * (size_t)dd.vert_base, q, 3 * nv * 4, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(d_normals + 3 * (size_t)dd.vert_base, q, 3 * nv * 4, cudaMemcpyHostToDevice, s));
   h2d_bytes += b_nodes + b_tris + b_faces + nv * 16;
   ++domain_loads;
 }
@@ -528,7 +530,7 @@ void Tracer::traceOutOfCore(bool shadow, const std::vector<int>& order, int S) {
       int slot, evicted;
       if (!lru.load(todo[k], &slot, &evicted)) {
         if (evicted >= 0) hdoms[evicted].resident = 0;
-        loadDomain(todo[k], slot);
+        loadDomain(todo[k], slot, stream);
       }
     }
     // stage the domain table and the segment table (begin, prefix) of this batch
@@ -940,45 +942,71 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
   std::vector<int> remaining;
   for (int d : residentFirst(scoreOrder()))
     if ((with_r && rk[d + 1] > rk[d]) || (with_s && sk[d + 1] > sk[d])) remaining.push_back(d);
-  const int B = cfg.ooc_batch > 0 ? std::min(cfg.ooc_batch, cache_capacity)
-                                   : std::max(1, cache_capacity / 4);
+  // a batch's copies run on the copy stream while the previous batch traces;
+  // two batches fit the cache together, so a copy never evicts a domain that
+  // the running trace reads (and the batch before it has finished)
+  const int half = std::max(1, cache_capacity / 2);
+  const int B = std::min(cfg.ooc_batch > 0 ? cfg.ooc_batch : half, half);
   int32_t* hdoms_list = reinterpret_cast<int32_t*>(h_live);
   uint32_t* hlive = h_live + D;
-  while (!remaining.empty()) {
-    std::memcpy(hdoms_list, remaining.data(), remaining.size() * 4);
-    CK(cudaMemcpyAsync(d_live_doms, hdoms_list, remaining.size() * 4, cudaMemcpyHostToDevice, stream));
-    LiveArgs la{};
-    la.rentries = with_r ? d_entries : nullptr;
-    la.rkey_start = d_key_start;
-    la.ray_key = d_ray_key;
-    la.rec_key = d_rec_key;
-    la.sentries = with_s ? d_sentries : nullptr;
-    la.skey_start = d_skey_start;
-    la.occluded = sh.occluded;
-    la.domains = d_live_doms;
-    la.ndomains = (int)remaining.size();
-    la.D = D;
-    la.cull = cfg.cull;
-    la.live = d_live;
-    launchCountLive(stream, la);
-    launches += 1;
-    CK(cudaMemcpyAsync(hlive, d_live, 2 * (size_t)D * 4, cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    std::vector<int> batch, rest;
+  // live counts of `doms`, written to hlive when `done` has completed
+  auto countLive = [&](const std::vector<int>& doms, cudaEvent_t done) {
+    if (!doms.empty()) {
+      std::memcpy(hdoms_list, doms.data(), doms.size() * 4);
+      CK(cudaMemcpyAsync(d_live_doms, hdoms_list, doms.size() * 4, cudaMemcpyHostToDevice, stream));
+      LiveArgs la{};
+      la.rentries = with_r ? d_entries : nullptr;
+      la.rkey_start = d_key_start;
+      la.ray_key = d_ray_key;
+      la.rec_key = d_rec_key;
+      la.sentries = with_s ? d_sentries : nullptr;
+      la.skey_start = d_skey_start;
+      la.occluded = sh.occluded;
+      la.domains = d_live_doms;
+      la.ndomains = (int)doms.size();
+      la.D = D;
+      la.cull = cfg.cull;
+      la.live = d_live;
+      launchCountLive(stream, la);
+      launches += 1;
+      CK(cudaMemcpyAsync(hlive, d_live, 2 * (size_t)D * 4, cudaMemcpyDeviceToHost, stream));
+    }
+    CK(cudaEventRecord(done, stream));
+  };
+  // the next batch: the first B domains of `remaining` with live entries; the
+  // rest stay in `remaining`, domains without live entries are dropped
+  auto select = [&](std::vector<int>& remaining, std::vector<int>& batch) {
+    std::vector<int> rest;
+    batch.clear();
     for (int d : remaining) {
       const bool lr = with_r && hlive[d] > 0, ls = with_s && hlive[D + d] > 0;
       if (!lr && !ls) continue;  // nothing left to trace here: not loaded
       if ((int)batch.size() < B) batch.push_back(d);
       else rest.push_back(d);
     }
-    if (batch.empty()) break;
+    remaining.swap(rest);
+  };
+  auto issueLoads = [&](const std::vector<int>& batch, cudaEvent_t loaded) {
+    cudaEvent_t c0 = poolEvent();
+    CK(cudaEventRecord(c0, cstream));
     for (int d : batch) {
       int slot, evicted;
       if (!lru.load(d, &slot, &evicted)) {
         if (evicted >= 0) hdoms[evicted].resident = 0;
-        loadDomain(d, slot);
+        loadDomain(d, slot, cstream);
       }
     }
+    CK(cudaEventRecord(loaded, cstream));
+    copy_events.push_back({c0, loaded});
+  };
+  std::vector<int> batch, next;
+  cudaEvent_t counted = poolEvent();
+  countLive(remaining, counted);
+  CK(cudaEventSynchronize(counted));
+  select(remaining, batch);
+  cudaEvent_t loaded = poolEvent();
+  if (!batch.empty()) issueLoads(batch, loaded);
+  while (!batch.empty()) {
     // domain table, then one segment table per queue: begins (D + 1) and prefixes (D + 1)
     DomainDev* sd = reinterpret_cast<DomainDev*>(h_stage);
     std::memcpy(sd, hdoms.data(), D * sizeof(DomainDev));
@@ -1002,6 +1030,10 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
     }
     CK(cudaMemcpyAsync(d_domains, sd, D * sizeof(DomainDev), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_segs, seg, (4 * (size_t)D + 4) * 4, cudaMemcpyHostToDevice, stream));
+    // counts for the batch after this one, taken before this one traces
+    counted = poolEvent();
+    countLive(remaining, counted);
+    CK(cudaStreamWaitEvent(stream, loaded, 0));
     for (int q = 0; q < 2; ++q) {
       if (nseg[q] == 0) continue;
       CK(cudaMemsetAsync(d_work, 0, 4, stream));
@@ -1022,10 +1054,19 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
       (q == 1 ? occl_events : trace_events).push_back({e0, e1});
       launches += 1;
     }
-    // the staging buffers are reused by the next batch
-    CK(cudaStreamSynchronize(stream));
-    remaining.swap(rest);
+    // the counts (and every trace before this batch's) have completed: the
+    // staging buffers are free and the next batch's copies can start
+    CK(cudaEventSynchronize(counted));
+    select(remaining, next);
+    batch.swap(next);
+    if (!batch.empty()) {
+      // a cache too small for two batches copies only after the trace has finished
+      if (2 * B > cache_capacity) CK(cudaStreamSynchronize(stream));
+      loaded = poolEvent();
+      issueLoads(batch, loaded);
+    }
   }
+  CK(cudaStreamSynchronize(stream));
 }
 
 // Out of core, batched (schedule_policy 2): the shadow rays of depth b and the
@@ -1168,6 +1209,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     sched_events.clear();
     trace_events.clear();
     occl_events.clear();
+    copy_events.clear();
     dbg.clear();
     CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
     CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
@@ -1235,6 +1277,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->tris_shadow = (int64_t)ctr.tris_shadow;
       st->scene_triangles = (int64_t)total_tris;
       st->scene_bytes = (int64_t)scene_bytes;
+      st->h2d_ms = sum(copy_events);
     }
     return;
   }

@@ -94,7 +94,7 @@ class Tracer {
   void captureShadows(int b, int S);
   void setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t max_nodes, size_t max_tris,
                       size_t max_verts, size_t slot_bytes);
-  void loadDomain(int d, int slot);
+  void loadDomain(int d, int slot, cudaStream_t s);
   void traceOutOfCore(bool shadow, const std::vector<int>& order, int S);
   void oocPass(bool with_radiance, bool with_shadow, int S);
   std::vector<int> residentFirst(const std::vector<int>& order) const;
@@ -103,10 +103,11 @@ class Tracer {
   spray_gpu_config cfg;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t cstream = nullptr;  // out-of-core domain copies, ahead of the traces
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sched_events, trace_events, occl_events;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sched_events, trace_events, occl_events, copy_events;
 
   // scene
   bool has_scene = false, has_camera = false;

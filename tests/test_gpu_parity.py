@@ -306,6 +306,7 @@ def test_scene_file_path(lib_built, oracle_mod, tmp_path):
                                 dict(cache_size=16, schedule_policy=1),
                                 dict(cache_size=16, schedule_policy=2),
                                 dict(cache_size=5, schedule_policy=2, ooc_batch=1),
+                                dict(cache_size=1, schedule_policy=2),
                                 dict(cache_bytes=3 << 20, schedule_policy=2, ooc_batch=3)])
 def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     """Streaming domains through a small LRU cache changes loads, never the image."""
