@@ -278,6 +278,40 @@ int spray_gpu_schedule_static(const float* domain_bounds, int32_t num_domains, c
                               uint32_t* entries, int64_t entry_capacity, uint32_t* domain_start,
                               int64_t* num_entries, void* stream);
 
+/* ---------------------------------------------------------------- learned proposal
+ * The learned domain-order proposal (schedule_policy 3) is a 54-64-64-64-8
+ * MLP with BF16 weights and FP32 accumulation on the tensor cores.  SpRay has
+ * no learned component, so these entry points have no reference counterpart;
+ * they expose the network's kernels on caller-owned device buffers (testing,
+ * offline training).  All pointers are device pointers; every call blocks
+ * until its work has finished.  `params` holds spray_mlp_param_count() floats
+ * (W1 b1 W2 b2 W3 b3 W4 b4, weights [out][in], W1 64x64 with input columns
+ * 54..63 zero, W4 16x64 with rows 8..15 zero); `boxes` 6 floats per domain;
+ * `norm` = centre xyz and scale, features are (p - centre) * scale. */
+typedef struct spray_mlp_sample {
+  float org[3];
+  float dir[3];
+  uint16_t cand[8];   /* candidate domains in (entry t, id) order */
+  int32_t ncand;      /* 0..8 */
+  int32_t label;      /* position of the candidate holding the closest hit, -1 none */
+} spray_mlp_sample;
+
+int32_t spray_mlp_param_count(void);
+/* logits [n][8] (absent candidates -inf) and their argmax per sample */
+int spray_mlp_forward_dev(const float* params, const float* boxes, const float norm[4],
+                          const spray_mlp_sample* samples, int64_t n, float* logits, int32_t* pred,
+                          int32_t device);
+/* gradient of the mean cross-entropy over the labelled samples:
+ * grad[param_count + 2] = gradient, loss sum, labelled count */
+int spray_mlp_grad_dev(const float* params, const float* boxes, const float norm[4],
+                       const spray_mlp_sample* samples, int64_t n, float* grad, int32_t device);
+/* `steps` Adam steps (lr; beta1 0.9, beta2 0.999, eps 1e-8) over consecutive
+ * batches of `batch` samples (wrapping), Adam step numbers first_step,
+ * first_step + 1, ...; losses[steps] receives each step's mean loss (may be NULL) */
+int spray_mlp_train_dev(float* params, float* adam_m, float* adam_v, const float* boxes,
+                        const float norm[4], const spray_mlp_sample* samples, int64_t n, int32_t batch,
+                        float lr, int32_t steps, int32_t first_step, float* losses, int32_t device);
+
 #ifdef __cplusplus
 }
 #endif

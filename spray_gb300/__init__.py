@@ -128,6 +128,12 @@ def lib() -> C.CDLL:
                                              P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.spray_gpu_schedule_static.argtypes = [P, C.c_int32, P, P, C.c_int32, C.c_int32, P, C.c_int64, P,
                                                 C.POINTER(C.c_int64), P]
+        F4 = C.POINTER(C.c_float)
+        L.spray_mlp_param_count.restype = C.c_int32
+        L.spray_mlp_forward_dev.argtypes = [P, P, F4, P, C.c_int64, P, P, C.c_int32]
+        L.spray_mlp_grad_dev.argtypes = [P, P, F4, P, C.c_int64, P, C.c_int32]
+        L.spray_mlp_train_dev.argtypes = [P, P, P, P, F4, P, C.c_int64, C.c_int32, C.c_float, C.c_int32,
+                                          C.c_int32, P, C.c_int32]
         _lib_handle = L
     return _lib_handle
 
@@ -321,6 +327,45 @@ def schedule_static(domain_bounds_ptr: int, num_domains: int, org_ptr: int, dir_
                                            C.c_void_p(domain_start_ptr), C.byref(n),
                                            C.c_void_p(stream) if stream else None))
     return n.value
+
+
+# spray_mlp_sample
+MLP_SAMPLE_DTYPE = np.dtype([("org", "<f4", 3), ("dir", "<f4", 3), ("cand", "<u2", 8), ("ncand", "<i4"),
+                             ("label", "<i4")])
+
+
+def mlp_param_count() -> int:
+    return int(lib().spray_mlp_param_count())
+
+
+def _norm(norm) -> C.Array:
+    return (C.c_float * 4)(*[float(x) for x in norm])
+
+
+def mlp_forward(params_ptr: int, boxes_ptr: int, norm, samples_ptr: int, n: int, logits_ptr: int,
+                pred_ptr: int, device: int = 0) -> None:
+    """Learned proposal forward pass on device buffers (spray_mlp_forward_dev)."""
+    P = C.c_void_p
+    _check(lib().spray_mlp_forward_dev(P(params_ptr), P(boxes_ptr), _norm(norm), P(samples_ptr), n,
+                                       P(logits_ptr), P(pred_ptr), device))
+
+
+def mlp_grad(params_ptr: int, boxes_ptr: int, norm, samples_ptr: int, n: int, grad_ptr: int,
+             device: int = 0) -> None:
+    """Mean cross-entropy gradient, loss sum and labelled count (spray_mlp_grad_dev)."""
+    P = C.c_void_p
+    _check(lib().spray_mlp_grad_dev(P(params_ptr), P(boxes_ptr), _norm(norm), P(samples_ptr), n,
+                                    P(grad_ptr), device))
+
+
+def mlp_train(params_ptr: int, m_ptr: int, v_ptr: int, boxes_ptr: int, norm, samples_ptr: int, n: int,
+              batch: int, lr: float, steps: int, first_step: int = 1, losses_ptr: int = 0,
+              device: int = 0) -> None:
+    """Adam steps over consecutive batches (spray_mlp_train_dev)."""
+    P = C.c_void_p
+    _check(lib().spray_mlp_train_dev(P(params_ptr), P(m_ptr), P(v_ptr), P(boxes_ptr), _norm(norm),
+                                     P(samples_ptr), n, batch, lr, steps, first_step,
+                                     P(losses_ptr) if losses_ptr else None, device))
 
 
 def generate_wavelet(samples: int = 64, iso: float = 157.0, phase=(0.0, 0.0, 0.0)):
