@@ -36,7 +36,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mrays/s at <=1e-3 image RMSE, learned vs plain scheduler; domain loads/frame"
 POLICIES = {"plain": (0, "plain speculative"), "resident": (1, "resident domains first"),
-            "batched": (2, "batched passes (shadow b + radiance b+1), culled domains not loaded")}
+            "batched": (2, "batched passes (shadow b + radiance b+1), culled domains not loaded"),
+            "learned": (3, "learned domain-order proposal (online-trained MLP) + batched passes")}
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
@@ -234,6 +235,8 @@ def main():
         cfg["image_h"] = max(8, cfg["image_h"] // args.scale)
     cfg["schedule_policy"] = POLICIES[args.policy][0]
     cfg["ooc_batch"] = args.ooc_batch
+    if args.policy == "learned":
+        cfg["learn_frames"] = 1  # collect during the first warm-up frame, train after it
     tracer = sg.Tracer(cfg, device=local)
     tracer.set_scene(scene)
     # weak scaling: each rank renders its own seeded view of the scene
@@ -248,8 +251,13 @@ def main():
             torch.cuda.synchronize()
         return tracer.trace_device(img_dev.data_ptr())
 
-    for _ in range(args.warmup):
-        frame_device()
+    warm = [frame_device() for _ in range(args.warmup)]
+    learn = None
+    if args.policy == "learned":
+        w0 = next((w for w in warm if w["learn_ms"] > 0), None)
+        learn = {"trained_before_timing": bool(warm[-1]["learn_trained"]) if warm else False,
+                 "pairs": warm[-1]["learn_pairs"] if warm else 0,
+                 "train_ms": w0["learn_ms"] if w0 else None, "loss": w0["learn_loss"] if w0 else None}
 
     clk_path = ROOT / "gpurun_out" / f"clocks_rank{rank}.csv"
     clk_path.parent.mkdir(exist_ok=True)
@@ -333,6 +341,8 @@ def main():
                      "launches_per_frame": klaunch, "kernel_ms_per_frame": kms},
         "clocks": clocks,
     }
+    if learn is not None:
+        out["learn"] = learn
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         r, dt, c, _ = cpu_speculative(args.config, spec, cfg, threads, args.cpu_scale)

@@ -75,10 +75,24 @@ typedef struct spray_gpu_config {
                                    reference's), 1 resident domains first, 2 batched: the shadow
                                    rays of depth b and the radiance rays of depth b+1 share one
                                    pass over the domains, resident domains go first, and a domain
-                                   whose entries were all culled before its turn is not loaded (0) */
+                                   whose entries were all culled before its turn is not loaded;
+                                   3 learned: policy 2 out of core, plus the learned domain-order
+                                   proposal (a small MLP trained online on the tracer's own
+                                   (ray, winning domain) pairs) orders the work: in core, each
+                                   ray's entries up to its predicted domain are traced first and
+                                   the later ones front to back; out of core, domains holding
+                                   more predicted hits go first.  Images are unchanged (0) */
   int32_t ooc_batch;            /* out-of-core, policy 2: domains made resident per traced batch,
                                    at most half the cache capacity so that the next batch's copies
                                    overlap this batch's traces; 0 = half the capacity (0) */
+  int64_t learn_samples;        /* policy 3: training pairs collected before training (16777216) */
+  int32_t learn_batch;          /* policy 3: Adam batch size (65536) */
+  int32_t learn_epochs;         /* policy 3: passes over the collected pairs (2) */
+  float learn_lr;               /* policy 3: Adam learning rate (0.001) */
+  int32_t learn_seed;           /* policy 3: weight initialisation seed (1) */
+  int32_t learn_frames;         /* policy 3: train after this many frames even if fewer pairs
+                                   were collected (4) */
+  int32_t reserved0;
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as
@@ -135,6 +149,10 @@ typedef struct spray_gpu_stats {
   int64_t scene_triangles;  /* triangles in the scene */
   int64_t scene_bytes;      /* device bytes of BVH nodes, triangles and shading data */
   double h2d_ms;            /* device time of the out-of-core domain copies (copy stream) */
+  int64_t learn_pairs;      /* policy 3: training pairs collected so far */
+  int64_t learn_trained;    /* policy 3: 1 once the proposal has been trained */
+  double learn_ms;          /* policy 3: device time spent training after this frame */
+  double learn_loss;        /* policy 3: mean loss of the last training batch */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

@@ -39,7 +39,9 @@ class ConfigC(C.Structure):
         ("rr_depth", C.c_int32), ("cull", C.c_int32), ("cache_bytes", C.c_int64),
         ("wave_samples", C.c_int64), ("debug_capture", C.c_int32), ("device", C.c_int32),
         ("schedule_policy", C.c_int32),
-        ("ooc_batch", C.c_int32),
+        ("ooc_batch", C.c_int32), ("learn_samples", C.c_int64), ("learn_batch", C.c_int32),
+        ("learn_epochs", C.c_int32), ("learn_lr", C.c_float), ("learn_seed", C.c_int32),
+        ("learn_frames", C.c_int32), ("reserved0", C.c_int32),
     ]
 
 
@@ -66,7 +68,8 @@ class StatsC(C.Structure):
         ("trace_launches", C.c_int64), ("occlude_launches", C.c_int64),
         ("nodes_radiance", C.c_int64), ("tris_radiance", C.c_int64), ("nodes_shadow", C.c_int64),
         ("tris_shadow", C.c_int64), ("scene_triangles", C.c_int64), ("scene_bytes", C.c_int64),
-        ("h2d_ms", C.c_double),
+        ("h2d_ms", C.c_double), ("learn_pairs", C.c_int64), ("learn_trained", C.c_int64),
+        ("learn_ms", C.c_double), ("learn_loss", C.c_double),
     ]
 
     def asdict(self) -> dict:

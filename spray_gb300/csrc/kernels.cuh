@@ -132,7 +132,8 @@ struct SchedArgs {
   unsigned long long arena_cap;
   uint32_t* list_off;         // per scheduled ray
   uint32_t* list_cnt;
-  uint32_t* hist;             // [nkeys][nwarps]
+  uint32_t* hist;             // [nkeys][nchunks]
+  int nchunks;                // ray chunks, each with its own histogram column
   long long* dstats;          // [D][list_size] ray counts per (domain, depth)
   int want_stats;             // fill dstats (out-of-core order, debug hooks)
   uint2* entries;             // partitioned entries
@@ -140,7 +141,25 @@ struct SchedArgs {
   uint32_t* key_start;        // [nkeys + 1]
   uint32_t* num_entries;      // total entries (device)
   Counters* ctr;
+  // learned order: per scheduled ray the predicted list position of its hit;
+  // with order_by_depth the entries at or before it form bucket 0 and the
+  // later ones buckets 1, 2, 3+ (null: bucket = list position, capped at 3)
+  const uint8_t* pred;
+  int defer_hist;             // kSchedLists leaves the histogram to the partition step
 };
+
+// Rays per chunk of the scheduler: a multiple of 32 covering n rays in at
+// most nchunks chunks (chunk c holds rays [c * size, (c + 1) * size)).
+__host__ __device__ __forceinline__ uint64_t chunkSize(uint64_t n, int nchunks) {
+  return (((n + (uint64_t)nchunks - 1) / (uint64_t)nchunks) + 31u) & ~(uint64_t)31u;
+}
+
+// Depth bucket of the entry at list position j (p = predicted position, 0xff none).
+__host__ __device__ __forceinline__ uint32_t bucketOf(uint32_t j, uint32_t p) {
+  if (p == 0xffu) return j < 3u ? j : 3u;
+  if (j <= p) return 0u;
+  return j - p < 3u ? j - p : 3u;
+}
 
 struct TraceArgs {
   SceneDev scene;
@@ -192,6 +211,12 @@ void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int n
 // scan_tmp holds kMaxScanBlocks words.  Launches 5 kernels.
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
                     int nwarps, int nblocks, uint32_t* scan_tmp);
+// The two halves of launchSchedule: the per-ray domain lists (1 kernel), then
+// the partition into queues (histogram when deferred, scan, scatter: 4 or 5).
+void launchSchedLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
+                      int nwarps, int nblocks);
+void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int ndomains, int nwarps,
+                          uint32_t* scan_tmp);
 // Resident blocks per SM of the scheduling kernel for this shared-memory use.
 int schedBlocksPerSm(int D, int nkeys, int dnode_count);
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks);
@@ -216,7 +241,8 @@ void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int lis
 // radiance entries and live[D + d] shadow entries.  Either queue may be null.
 struct LiveArgs {
   const uint2* rentries;
-  const uint32_t* rkey_start;
+  const uint32_t* rkey_start;  // [rbuckets * D + 1]: key = bucket * D + domain
+  int rbuckets;
   const uint64_t* ray_key;
   uint64_t* rec_key;
   const uint2* sentries;

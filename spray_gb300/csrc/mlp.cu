@@ -615,7 +615,29 @@ __global__ void kCollectAdvance(const uint32_t* nsel, unsigned long long* filled
   *filled = base + min((uint64_t)*nsel, room);
 }
 
+// One atomic per distinct domain of a warp (rays of a warp often agree).
+__global__ void kPredCount(ArenaSource a, const uint8_t* __restrict__ pred, uint32_t* counts) {
+  const uint32_t n = *a.count;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n;
+       base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + lane;
+    uint32_t d = 0xffffffffu;
+    if (i < n) {
+      const uint32_t cnt = a.list_cnt[i];
+      if (cnt) d = a.arena[a.list_off[i] + min((uint32_t)pred[i], cnt - 1)].x & 0xffffu;
+    }
+    const uint32_t m = __match_any_sync(0xffffffffu, d);
+    if (d != 0xffffffffu && (__ffs(m) - 1) == lane) atomicAdd(&counts[d], (uint32_t)__popc(m));
+  }
+}
+
 }  // namespace
+
+void launchPredCount(cudaStream_t s, const ArenaSource& src, const uint8_t* pred, uint32_t* counts,
+                     int nblocks) {
+  kPredCount<<<nblocks, 256, 0, s>>>(src, pred, counts);
+}
 
 void launchPredictArena(cudaStream_t s, const Net& net, const ArenaSource& src, uint8_t* pred, int nblocks) {
   ArenaRows r{src, pred};

@@ -93,7 +93,11 @@ void launchCollect(cudaStream_t s, const ArenaSource& src, const uint64_t* ray_k
                    const DomainDev* domains, Sample* out, unsigned long long* filled,
                    uint64_t capacity, int8_t* label, uint8_t* flag, uint32_t* sel, uint32_t* nsel,
                    uint32_t* block_tmp, int nblocks);
-// Blocks per SM and shared memory of the kernels (for grid sizing).
+// Predicted hits per domain: counts[d] += 1 for the predicted candidate d of
+// every alive ray with at least one candidate (counts zeroed by the caller).
+void launchPredCount(cudaStream_t s, const ArenaSource& src, const uint8_t* pred, uint32_t* counts,
+                     int nblocks);
+// CTAs of the gradient kernel (one per SM: it holds all 512 tensor-memory columns).
 int gradBlocks(int num_sms);
 
 }  // namespace mlp

@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
   const int NN = a.dnode_count;
   float4* snode = reinterpret_cast<float4*>(smem);  // 4 float4 per hierarchy node
   float* sbox = reinterpret_cast<float*>(smem + 16 * NN);
-  uint32_t* hist = smem + 16 * NN + 6 * D;
+  uint32_t* hist = smem + 16 * NN + 6 * D;  // per warp: nkeys 16-bit counters, packed in pairs
+  const int hwords = (nkeys + 1) >> 1;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int d = threadIdx.x; d < D; d += blockDim.x) {
     for (int c = 0; c < 3; ++c) {
@@ -106,14 +107,20 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
   }
   for (int k = threadIdx.x; k < 4 * NN; k += blockDim.x)
     snode[k] = reinterpret_cast<const float4*>(a.dnodes)[k];
-  uint32_t* h = hist + (size_t)wib * nkeys;
-  for (int k = lane; k < nkeys; k += 32) h[k] = 0;
+  uint32_t* h = hist + (size_t)wib * hwords;
   __syncthreads();
   const uint32_t n = *a.count;
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-  const uint64_t per = ((uint64_t)n + nwarps - 1) / nwarps;
-  const uint64_t r0 = min((uint64_t)n, (uint64_t)gw * per);
-  const uint64_t r1 = min((uint64_t)n, r0 + per);
+  const int nch = a.nchunks;
+  const uint64_t csize = chunkSize(n, nch);
+  // chunks round-robin over the warps; a chunk's counts fit 16 bits (csize < 2^16)
+  for (int ch = gw; ch < nch; ch += nwarps) {
+  const uint64_t r0 = min((uint64_t)n, (uint64_t)ch * csize);
+  const uint64_t r1 = min((uint64_t)n, r0 + csize);
+  if (!a.defer_hist) {
+    for (int k = lane; k < hwords; k += 32) h[k] = 0;
+    __syncwarp();
+  }
   for (uint64_t base = r0; base < r1; base += 32) {
     const uint64_t i = base + lane;
     const bool active = i < r1;
@@ -181,6 +188,8 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
           const float4 l0 = snode[4 * node], h0 = snode[4 * node + 1];
           const float4 l1 = snode[4 * node + 2], h1 = snode[4 * node + 3];
           int next = -1;
+          float tn[2];
+          bool hit[2];
           for (int c = 0; c < 2; ++c) {
             const float4 lo = c ? l1 : l0, hi = c ? h1 : h0;
             const float nx = sx ? hi.x : lo.x, fx = sx ? lo.x : hi.x;
@@ -190,8 +199,16 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
                                    fmaxf((nz - org.z) * inv.z, kRayEpsilon));
             const float tt = fminf(fminf((fx - org.x) * inv.x, (fy - org.y) * inv.y),
                                    fminf((fz - org.z) * inv.z, tfar)) * 1.0000004f;
-            if (!(t0 <= tt)) continue;
-            const int ref = __float_as_int(lo.w);
+            hit[c] = t0 <= tt;
+            tn[c] = t0;
+          }
+          // nearer child first, so leaves arrive roughly in entry order and the
+          // sorted insertion above is mostly an append
+          const int first = (hit[1] && (!hit[0] || tn[1] < tn[0])) ? 1 : 0;
+          for (int k = 0; k < 2; ++k) {
+            const int c = k ^ first;
+            if (!hit[c]) continue;
+            const int ref = __float_as_int(c ? l1.w : l0.w);
             if (ref < 0) consider(~ref);
             else if (next < 0) next = ref;
             else if (sp < 40) stack[sp++] = ref;
@@ -230,14 +247,14 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
         if (a.shadow) {
           out[o++] = make_uint2((uint32_t)origin | (1u << 31), __float_as_uint(origin_t));
           uint32_t key = (uint32_t)origin;
-          atomicAdd(&h[key], 1u);
+          if (!a.defer_hist) atomicAdd(&h[key >> 1], 1u << ((key & 1u) << 4));
         }
         for (int j = 0; j < cnt; ++j) {
           uint32_t d = ld[j];
           if (a.shadow && (int)d == origin) continue;
           out[o++] = make_uint2(d | ((uint32_t)j << 16), __float_as_uint(lt[j]));
           uint32_t key = a.order_by_depth ? (uint32_t)(min(j, kDepthBuckets - 1) * D) + d : d;
-          atomicAdd(&h[key], 1u);
+          if (!a.defer_hist) atomicAdd(&h[key >> 1], 1u << ((key & 1u) << 4));
         }
       }
     }
@@ -255,7 +272,11 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
     }
   }
   __syncwarp();
-  for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nwarps + gw] = h[k];
+  if (!a.defer_hist) {
+    for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nch + ch] = (h[k >> 1] >> ((k & 1) << 4)) & 0xffffu;
+    __syncwarp();
+  }
+  }
 }
 
 // Pass 2: exclusive scan of the key-major histogram, three phases over many
@@ -351,14 +372,18 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
   uint32_t* fw1 = fw0 + 32 * kMaxEmit;
   const int gw = blockIdx.x * wpb + wib;
   if (gw >= nwarps) return;
-  for (int k = lane; k < nkeys; k += 32) running[k] = a.hist[(size_t)k * nwarps + gw];
-  __syncwarp();
   const uint32_t n = *a.count;
   if (*a.num_entries == 0) return;
-  const uint64_t per = ((uint64_t)n + nwarps - 1) / nwarps;
-  const uint64_t r0 = min((uint64_t)n, (uint64_t)gw * per);
-  const uint64_t r1 = min((uint64_t)n, r0 + per);
+  const int nch = a.nchunks;
+  const uint64_t csize = chunkSize(n, nch);
   const uint32_t lt = laneMaskLt();
+  for (int ch = gw; ch < nch; ch += nwarps) {
+  const uint64_t r0 = min((uint64_t)n, (uint64_t)ch * csize);
+  const uint64_t r1 = min((uint64_t)n, r0 + csize);
+  if (r0 >= r1) break;
+  __syncwarp();
+  for (int k = lane; k < nkeys; k += 32) running[k] = a.hist[(size_t)k * nch + ch];
+  __syncwarp();
   for (uint64_t base = r0; base < r1; base += 32) {
     const uint64_t i = base + lane;
     uint32_t cnt = 0, off = 0, rid = 0;
@@ -374,7 +399,7 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
       uint32_t d = e.x & 0xffffu;
       uint32_t depth = (e.x >> 16) & 0x7fffu;
       uint32_t origin = e.x >> 31;
-      uint32_t key = a.order_by_depth ? (uint32_t)(min((int)depth, kDepthBuckets - 1) * D) + d : d;
+      uint32_t key = a.order_by_depth ? bucketOf(depth, a.pred ? a.pred[i] : 0xffu) * D + d : d;
       fkey[pos + j] = key;
       fw0[pos + j] = (rid & kRayIdMask) | (min(depth, 31u) << kRayIdBits) | (origin << 31);
       fw1[pos + j] = e.y;
@@ -394,10 +419,49 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
     }
     __syncwarp();
   }
+  }
+}
+
+// Deferred histogram: the per-(key, warp) counts of kSchedLists, recounted
+// from the per-ray lists with the same ray partition, after the learned
+// proposal has set each ray's bucket boundary.
+__global__ void __launch_bounds__(128) kSchedHist(SchedArgs a, int D, int nkeys, int nwarps) {
+  extern __shared__ uint32_t smem[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t* h = smem + (size_t)wib * nkeys;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (gw >= nwarps) return;
+  const uint32_t n = *a.count;
+  const int nch = a.nchunks;
+  const uint64_t csize = chunkSize(n, nch);
+  for (int ch = gw; ch < nch; ch += nwarps) {
+  for (int k = lane; k < nkeys; k += 32) h[k] = 0;
+  __syncwarp();
+  const uint64_t r0 = min((uint64_t)n, (uint64_t)ch * csize);
+  const uint64_t r1 = min((uint64_t)n, r0 + csize);
+  for (uint64_t i = r0 + lane; i < r1; i += 32) {
+    const uint32_t cnt = a.list_cnt[i], off = a.list_off[i];
+    const uint32_t p = a.pred ? a.pred[i] : 0xffu;
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const uint2 e = a.arena[off + j];
+      const uint32_t d = e.x & 0xffffu;
+      const uint32_t depth = (e.x >> 16) & 0x7fffu;
+      const uint32_t key = a.order_by_depth ? bucketOf(depth, p) * D + d : d;
+      atomicAdd(&h[key], 1u);
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nch + ch] = h[k];
+  __syncwarp();
+  }
+}
+
+static size_t listsSmem(int D, int nkeys, int dnode_count) {
+  return (size_t)dnode_count * 64 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * ((nkeys + 1) / 2) * 4;
 }
 
 int schedBlocksPerSm(int D, int nkeys, int dnode_count) {
-  size_t smem = (size_t)dnode_count * 64 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
+  size_t smem = listsSmem(D, nkeys, dnode_count);
   cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int bps = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kSchedLists, kSchedThreads, smem) != cudaSuccess ||
@@ -406,18 +470,33 @@ int schedBlocksPerSm(int D, int nkeys, int dnode_count) {
   return bps;
 }
 
-void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
-                    int nblocks, uint32_t* scan_tmp) {
+void launchSchedLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
+                      int nblocks) {
   const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
-  size_t smem1 = (size_t)a.dnode_count * 64 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * nkeys * 4;
+  size_t smem1 = listsSmem(D, nkeys, a.dnode_count);
   cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
   kSchedLists<<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
-  const uint64_t M = (uint64_t)nkeys * nwarps;
+}
+
+void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
+                    int nblocks, uint32_t* scan_tmp) {
+  launchSchedLists(s, a, domains, D, nwarps, nblocks);
+  launchSchedPartition(s, a, D, nwarps, scan_tmp);
+}
+
+void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int D, int nwarps, uint32_t* scan_tmp) {
+  const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
+  if (a.defer_hist) {
+    const size_t smemh = (size_t)4 * nkeys * 4;
+    cudaFuncSetAttribute(kSchedHist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemh);
+    kSchedHist<<<(nwarps + 3) / 4, 128, smemh, s>>>(a, D, nkeys, nwarps);
+  }
+  const uint64_t M = (uint64_t)nkeys * a.nchunks;
   const int nb = (int)std::min<uint64_t>(kMaxScanBlocks, (M + 2047) / 2048);
   const uint64_t chunk = (M + nb - 1) / nb;
   kScanReduce<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp);
   kScanPartials<<<1, 1024, 0, s>>>(scan_tmp, nb);
-  kScanApply<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp, nb, nwarps, nkeys, a.key_start,
+  kScanApply<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp, nb, a.nchunks, nkeys, a.key_start,
                                           a.num_entries, a.entry_cap, a.ctr);
   const int wpb = 4;
   size_t smem3 = (size_t)wpb * nkeys * 4 + (size_t)wpb * 32 * kMaxEmit * 3 * 4;

@@ -139,8 +139,14 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   if (cfg.max_samples_per_rank <= 0) throw std::invalid_argument("max_samples_per_rank must be positive");
   if (cfg.num_ranks <= 0 || cfg.rank < 0 || cfg.rank >= cfg.num_ranks)
     throw std::invalid_argument("rank must be in [0, num_ranks)");
-  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 2)
-    throw std::invalid_argument("schedule_policy must be 0, 1 or 2");
+  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 3)
+    throw std::invalid_argument("schedule_policy must be 0, 1, 2 or 3");
+  if (cfg.schedule_policy == 3 &&
+      (cfg.learn_samples < 0 || cfg.learn_batch <= 0 || cfg.learn_epochs < 0 || !(cfg.learn_lr > 0.0f) ||
+       cfg.learn_frames < 1))
+    throw std::invalid_argument(
+        "learned proposal needs learn_samples >= 0, learn_batch > 0, learn_epochs >= 0, learn_lr > 0, "
+        "learn_frames >= 1");
   if (cfg.ooc_batch < 0) throw std::invalid_argument("ooc_batch must be >= 0");
   int ndev = 0;
   CK(cudaGetDeviceCount(&ndev));
@@ -167,6 +173,7 @@ Tracer::~Tracer() {
 }
 
 void Tracer::freeScene() {
+  freeProposal();
   if (h_pinned) cudaFreeHost(h_pinned);
   h_pinned = nullptr;
   if (h_stage) cudaFreeHost(h_stage);
@@ -221,6 +228,11 @@ void Tracer::freeBuffers() {
   devFree(d_entries);
   devFree(d_key_start);
   devFree(d_num_entries);
+  devFree(d_pred);
+  devFree(d_lab);
+  devFree(d_lflag);
+  devFree(d_lsel);
+  devFree(d_lnsel);
   devFree(d_sentries);
   devFree(d_skey_start);
   devFree(d_snum_entries);
@@ -396,6 +408,7 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   devAlloc(&d_lights, lf.size());
   CK(cudaMemcpy(d_lights, lf.data(), lf.size() * 4, cudaMemcpyHostToDevice));
   freeBuffers();  // sizes depend on the domain count and slots
+  if (learned()) setupProposal();
   has_scene = true;
 }
 
@@ -443,9 +456,11 @@ void Tracer::setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t
   devAlloc(&d_faces, 3 * (size_t)capacity * max_tris);
   devAlloc(&d_colors, (size_t)capacity * max_verts);
   devAlloc(&d_normals, 3 * (size_t)capacity * max_verts);
-  // two segment tables (radiance, shadow) of D + 1 begins and D + 1 prefixes each
-  devAlloc(&d_segs, 4 * (size_t)D + 4);
-  CK(cudaHostAlloc((void**)&h_stage, D * sizeof(DomainDev) + (4 * (size_t)D + 4) * 4, cudaHostAllocDefault));
+  // segment tables (one per radiance depth bucket, one for shadows) of D + 1
+  // begins and D + 1 prefixes each
+  devAlloc(&d_segs, (kDepthBuckets + 1) * (2 * (size_t)D + 2));
+  CK(cudaHostAlloc((void**)&h_stage, D * sizeof(DomainDev) + (kDepthBuckets + 1) * (2 * (size_t)D + 2) * 4,
+                   cudaHostAllocDefault));
   devAlloc(&d_live, 2 * (size_t)D);
   devAlloc(&d_live_doms, D);
   CK(cudaHostAlloc((void**)&h_live, 3 * (size_t)D * 4, cudaHostAllocDefault));
@@ -624,6 +639,11 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   // one resident wave: each warp owns a contiguous chunk of rays
   sched_blocks = num_sms * schedBlocksPerSm(D, kDepthBuckets * D, dnode_count);
   sched_warps = sched_blocks * (kSchedThreads / 32);
+  // eight ray chunks per scheduling warp, so that uneven rays balance out;
+  // a chunk's per-key counts must fit 16 bits
+  sched_chunks = 8 * sched_warps;
+  if (chunkSize((uint64_t)1 << kRayIdBits, sched_chunks) >= 65536)
+    throw std::runtime_error("too few scheduling chunks for 16-bit histogram counters");
   if (nsamples <= cap_samples && cap_entries >= needed_entries) return;
   freeBuffers();
   int64_t N = std::max<int64_t>(nsamples, 1024);
@@ -658,12 +678,19 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_arena_top, 1);
   devAlloc(&d_list_off, NS);
   devAlloc(&d_list_cnt, NS);
-  devAlloc(&d_hist, (size_t)nkeys * sched_warps);
+  devAlloc(&d_hist, (size_t)nkeys * sched_chunks);
   devAlloc(&d_dstats, (size_t)D * cfg.list_size);
   devAlloc(&d_entries, E);
   devAlloc(&d_key_start, nkeys + 1);
   devAlloc(&d_num_entries, 1);
-  if (ooc && cfg.schedule_policy == 2) {
+  if (learned()) {
+    devAlloc(&d_pred, N);
+    devAlloc(&d_lab, N);
+    devAlloc(&d_lflag, N);
+    devAlloc(&d_lsel, N);
+    devAlloc(&d_lnsel, 1);
+  }
+  if (ooc && cfg.schedule_policy >= 2) {
     devAlloc(&d_sentries, E);
     devAlloc(&d_skey_start, nkeys + 1);
     devAlloc(&d_snum_entries, 1);
@@ -684,7 +711,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
 }
 
 void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S,
-                      bool primary, bool into_shadow_queues) {
+                      bool primary, bool into_shadow_queues, bool predicted) {
   SchedArgs a{};
   a.shadow = shadow;
   a.count = count;
@@ -710,6 +737,7 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.list_off = d_list_off;
   a.list_cnt = d_list_cnt;
   a.hist = d_hist;
+  a.nchunks = sched_chunks;
   a.dstats = d_dstats;
   a.want_stats = (ooc || cfg.debug_capture) ? 1 : 0;
   a.entries = into_shadow_queues ? d_sentries : d_entries;
@@ -718,8 +746,21 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.num_entries = into_shadow_queues ? d_snum_entries : d_num_entries;
   a.ctr = d_ctr;
   CK(cudaMemsetAsync(d_arena_top, 0, sizeof(unsigned long long), stream));
-  launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp);
-  launches += 5;
+  if (predicted) {
+    // lists, then the proposal's bucket boundary per ray, then the partition
+    a.defer_hist = 1;
+    launchSchedLists(stream, a, d_domains, D, sched_warps, sched_blocks);
+    mlp::ArenaSource src = arenaSource();
+    src.count = count;
+    src.list = list;
+    mlp::launchPredictArena(stream, proposalNet(), src, d_pred, num_sms * 4);
+    a.pred = d_pred;
+    launchSchedPartition(stream, a, D, sched_warps, d_scan_tmp);
+    launches += 7;
+  } else {
+    launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp);
+    launches += 5;
+  }
 }
 
 TraceArgs Tracer::traceArgs(int order_by_depth, int S) {
@@ -826,7 +867,8 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
     CK(cudaEventRecord(s0, stream));
-    schedule(false, order_by_depth, d_alive_count, d_alive_list, S, b == 0);
+    schedule(false, order_by_depth, d_alive_count, d_alive_list, S, b == 0, false,
+             learned() && proposal_trained && order_by_depth && !capture);
     CK(cudaEventRecord(s1, stream));
     sched_events.push_back({s0, s1});
     if (capture) {
@@ -862,6 +904,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     launchResolve(stream, ta, d_hit_ns, nblk);
     launches += 1;
+    if (learned() && !proposal_trained) collectPairs();
     if (capture) captureHits(b);
     // shade
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
@@ -923,11 +966,12 @@ std::vector<int> Tracer::residentFirst(const std::vector<int>& order) const {
 // all of its shadow rays already occluded) is dropped without being loaded.
 // Dropping changes neither hit nor occlusion: a culled entry cannot beat its
 // ray's hit, and an occluded shadow ray stays occluded.
-void Tracer::oocPass(bool with_r, bool with_s, int S) {
-  std::vector<uint32_t> rk(D + 1, 0), sk(D + 1, 0);
+void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
+  const int nrk = rb * D;  // radiance keys: bucket * D + domain
+  std::vector<uint32_t> rk(nrk + 1, 0), sk(D + 1, 0);
   uint32_t rn = 0, sn = 0;
   if (with_r) {
-    CK(cudaMemcpyAsync(rk.data(), d_key_start, (D + 1) * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(rk.data(), d_key_start, (nrk + 1) * 4, cudaMemcpyDeviceToHost, stream));
     CK(cudaMemcpyAsync(&rn, d_num_entries, 4, cudaMemcpyDeviceToHost, stream));
   }
   if (with_s) {
@@ -936,12 +980,31 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
   }
   CK(cudaStreamSynchronize(stream));
   // a queue that overflowed holds no entries; the frame is traced again with larger queues
-  if (with_r && rk[D] != rn) with_r = false;
+  if (with_r && rk[nrk] != rn) with_r = false;
   if (with_s && sk[D] != sn) with_s = false;
   if (!with_r && !with_s) return;
+  auto rcount = [&](int d) {
+    uint32_t c = 0;
+    for (int b = 0; b < rb; ++b) c += rk[b * D + d + 1] - rk[b * D + d];
+    return c;
+  };
+  std::vector<int> order = scoreOrder();
+  std::vector<uint32_t> pc;
+  if (use_pred_order) {
+    // resident domains first (most recently used first), then the domains that
+    // hold more predicted hits
+    pc.resize(D);
+    CK(cudaMemcpyAsync(pc.data(), d_predcount, D * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    auto more = [&](int x, int y) { return pc[x] > pc[y]; };
+    std::stable_sort(order.begin(), order.end(), more);
+    order = residentFirst(order);
+  } else {
+    order = residentFirst(order);
+  }
   std::vector<int> remaining;
-  for (int d : residentFirst(scoreOrder()))
-    if ((with_r && rk[d + 1] > rk[d]) || (with_s && sk[d + 1] > sk[d])) remaining.push_back(d);
+  for (int d : order)
+    if ((with_r && rcount(d) > 0) || (with_s && sk[d + 1] > sk[d])) remaining.push_back(d);
   // a batch's copies run on the copy stream while the previous batch traces;
   // two batches fit the cache together, so a copy never evicts a domain that
   // the running trace reads (and the batch before it has finished)
@@ -957,6 +1020,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
       LiveArgs la{};
       la.rentries = with_r ? d_entries : nullptr;
       la.rkey_start = d_key_start;
+      la.rbuckets = rb;
       la.ray_key = d_ray_key;
       la.rec_key = d_rec_key;
       la.sentries = with_s ? d_sentries : nullptr;
@@ -978,11 +1042,18 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
   auto select = [&](std::vector<int>& remaining, std::vector<int>& batch) {
     std::vector<int> rest;
     batch.clear();
-    for (int d : remaining) {
-      const bool lr = with_r && hlive[d] > 0, ls = with_s && hlive[D + d] > 0;
-      if (!lr && !ls) continue;  // nothing left to trace here: not loaded
-      if ((int)batch.size() < B) batch.push_back(d);
-      else rest.push_back(d);
+    const size_t counted_n = std::min(remaining.size(), (size_t)2 * B);
+    for (size_t k = 0; k < remaining.size(); ++k) {
+      const int d = remaining[k];
+      if (k < counted_n) {
+        const bool lr = with_r && hlive[d] > 0, ls = with_s && hlive[D + d] > 0;
+        if (!lr && !ls) continue;  // nothing left to trace here: not loaded
+        if ((int)batch.size() < B) {
+          batch.push_back(d);
+          continue;
+        }
+      }
+      rest.push_back(d);
     }
     remaining.swap(rest);
   };
@@ -999,65 +1070,85 @@ void Tracer::oocPass(bool with_r, bool with_s, int S) {
     CK(cudaEventRecord(loaded, cstream));
     copy_events.push_back({c0, loaded});
   };
+  // live counts cover a window of the next 2 B remaining domains: enough to
+  // fill a batch after drops, and each domain is counted about once
+  auto window = [&](const std::vector<int>& rem) {
+    return std::vector<int>(rem.begin(), rem.begin() + std::min(rem.size(), (size_t)2 * B));
+  };
+  // after a count: select, and while a whole window was dropped, count on
+  auto nextBatch = [&](std::vector<int>& batch) {
+    select(remaining, batch);
+    while (batch.empty() && !remaining.empty()) {
+      cudaEvent_t c = poolEvent();
+      countLive(window(remaining), c);
+      CK(cudaEventSynchronize(c));
+      select(remaining, batch);
+    }
+  };
   std::vector<int> batch, next;
   cudaEvent_t counted = poolEvent();
-  countLive(remaining, counted);
+  countLive(window(remaining), counted);
   CK(cudaEventSynchronize(counted));
-  select(remaining, batch);
+  nextBatch(batch);
   cudaEvent_t loaded = poolEvent();
   if (!batch.empty()) issueLoads(batch, loaded);
+  const size_t tbl = 2 * (size_t)D + 2;  // words per segment table
   while (!batch.empty()) {
-    // domain table, then one segment table per queue: begins (D + 1) and prefixes (D + 1)
+    // domain table, then segment tables: radiance bucket 0..rb-1, shadows
     DomainDev* sd = reinterpret_cast<DomainDev*>(h_stage);
     std::memcpy(sd, hdoms.data(), D * sizeof(DomainDev));
     uint32_t* seg = reinterpret_cast<uint32_t*>(h_stage + D * sizeof(DomainDev));
-    int nseg[2] = {0, 0};
-    for (int q = 0; q < 2; ++q) {
-      const std::vector<uint32_t>& ks = q == 0 ? rk : sk;
-      const bool on = q == 0 ? with_r : with_s;
-      uint32_t* beg = seg + q * (2 * D + 2);
+    std::vector<int> nseg(rb + 1, 0);
+    for (int q = 0; q <= rb; ++q) {
+      const bool shadow = q == rb;
+      const bool on = shadow ? with_s : with_r;
+      uint32_t* beg = seg + q * tbl;
       uint32_t* pre = beg + D + 1;
       uint32_t run = 0;
       if (on)
         for (int d : batch) {
-          if (hlive[q * D + d] == 0) continue;
-          beg[nseg[q]] = ks[d];
+          if (hlive[(shadow ? D : 0) + d] == 0) continue;
+          const uint32_t b0 = shadow ? sk[d] : rk[q * D + d], b1 = shadow ? sk[d + 1] : rk[q * D + d + 1];
+          if (b1 == b0) continue;
+          beg[nseg[q]] = b0;
           pre[nseg[q]] = run;
-          run += ks[d + 1] - ks[d];
+          run += b1 - b0;
           ++nseg[q];
         }
       pre[nseg[q]] = run;
     }
     CK(cudaMemcpyAsync(d_domains, sd, D * sizeof(DomainDev), cudaMemcpyHostToDevice, stream));
-    CK(cudaMemcpyAsync(d_segs, seg, (4 * (size_t)D + 4) * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_segs, seg, (rb + 1) * tbl * 4, cudaMemcpyHostToDevice, stream));
     // counts for the batch after this one, taken before this one traces
     counted = poolEvent();
-    countLive(remaining, counted);
+    countLive(window(remaining), counted);
     CK(cudaStreamWaitEvent(stream, loaded, 0));
-    for (int q = 0; q < 2; ++q) {
+    // radiance buckets front to back (or predicted first), then the shadows
+    for (int q = 0; q <= rb; ++q) {
       if (nseg[q] == 0) continue;
+      const bool shadow = q == rb;
       CK(cudaMemsetAsync(d_work, 0, 4, stream));
-      TraceArgs ta = traceArgs(0, S);
-      if (q == 1) {
+      TraceArgs ta = traceArgs(shadow ? 0 : (rb > 1 ? 1 : 0), S);
+      if (shadow) {
         ta.entries = d_sentries;
         ta.key_start = d_skey_start;
         ta.num_entries = d_snum_entries;
       }
-      ta.seg_begin = d_segs + q * (2 * D + 2);
+      ta.seg_begin = d_segs + q * tbl;
       ta.seg_prefix = ta.seg_begin + D + 1;
       ta.nseg = nseg[q];
       cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
       CK(cudaEventRecord(e0, stream));
-      if (q == 1) launchTraceOccluded(stream, ta, num_sms * 4);
+      if (shadow) launchTraceOccluded(stream, ta, num_sms * 4);
       else launchTraceClosest(stream, ta, num_sms * 4);
       CK(cudaEventRecord(e1, stream));
-      (q == 1 ? occl_events : trace_events).push_back({e0, e1});
+      (shadow ? occl_events : trace_events).push_back({e0, e1});
       launches += 1;
     }
     // the counts (and every trace before this batch's) have completed: the
     // staging buffers are free and the next batch's copies can start
     CK(cudaEventSynchronize(counted));
-    select(remaining, next);
+    nextBatch(next);
     batch.swap(next);
     if (!batch.empty()) {
       // a cache too small for two batches copies only after the trace has finished
@@ -1080,19 +1171,27 @@ void Tracer::traceWaveBatched(const Wave& w) {
   const int spp = cfg.pixel_samples;
   const int nblk = num_sms * 4;
   beginWave(w);
+  // radiance queues keyed by depth bucket when culling, so each batch traces
+  // its entries front to back (learned: predicted domain and those in front
+  // of it first)
+  const int order_by_depth = cfg.cull ? 1 : 0;
+  const int rb = order_by_depth ? kDepthBuckets : 1;
   auto scheduleRadiance = [&](bool primary) {
     CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
     CK(cudaEventRecord(s0, stream));
-    schedule(false, 0, d_alive_count, d_alive_list, S, primary);
+    const bool pred = learned() && proposal_trained;
+    schedule(false, order_by_depth, d_alive_count, d_alive_list, S, primary, false, pred && order_by_depth);
     CK(cudaEventRecord(s1, stream));
     sched_events.push_back({s0, s1});
+    if (pred) predictDomainCounts(!order_by_depth);
   };
   scheduleRadiance(true);
-  oocPass(true, false, S);
+  oocPass(true, false, S, rb);
   for (int b = 0; b < cfg.bounces; ++b) {
     TraceArgs ta = traceArgs(0, S);
     launchResolve(stream, ta, d_hit_ns, nblk);
+    if (learned() && !proposal_trained) collectPairs();
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
     launchShade(stream, shadeArgs(b, S), nblk);
     launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
@@ -1109,11 +1208,170 @@ void Tracer::traceWaveBatched(const Wave& w) {
       cur ^= 1;
       scheduleRadiance(false);
     }
-    oocPass(more, true, S);
+    oocPass(more, true, S, rb);
     launchRetireImpl(stream, d_image, w.samples / spp, spp, d_pixid, retire_idx, sh, d_shadow_flag, S,
                      1.0 / (double)spp, nblk);
     launches += 1;
   }
+}
+
+// ---------------------------------------------------------------- proposal
+// The learned domain-order proposal: parameters initialised He-uniform from
+// a fixed seed, trained online on the (ray, candidates, winning position)
+// pairs the exact tracer produces during its first frames, then consulted to
+// order the trace.  It never decides a hit: every candidate entry is still
+// traced or culled by a hit that is nearer than its domain.
+namespace {
+uint64_t splitmix(uint64_t& x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+}  // namespace
+
+void Tracer::freeProposal() {
+  devFree(d_mlp);
+  devFree(d_mlp_partial);
+  devFree(d_boxes);
+  devFree(d_pairs);
+  devFree(d_pairs_filled);
+  devFree(d_predcount);
+  devFree(d_mlp_err);
+  proposal_trained = false;
+  frames_collected = 0;
+  adam_step = 0;
+  pairs_filled = 0;
+}
+
+void Tracer::setupProposal() {
+  freeProposal();
+  namespace ml = mlp;
+  std::vector<float> p(3 * ml::kParams + ml::kPartial, 0.0f);
+  uint64_t st = (uint64_t)cfg.learn_seed * 0x2545F4914F6CDD1Dull + 1;
+  auto put = [&](int off, int rows, int cols, int real_rows, int real_cols, int fan_in) {
+    const double lim = std::sqrt(6.0 / fan_in);
+    for (int r = 0; r < real_rows; ++r)
+      for (int c = 0; c < real_cols; ++c) {
+        const double u = (double)(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+        p[off + r * cols + c] = (float)((2.0 * u - 1.0) * lim);
+      }
+    (void)rows;
+  };
+  put(ml::kW1, ml::kHid, ml::kK, ml::kHid, ml::kIn, ml::kIn);
+  put(ml::kW2, ml::kHid, ml::kHid, ml::kHid, ml::kHid, ml::kHid);
+  put(ml::kW3, ml::kHid, ml::kHid, ml::kHid, ml::kHid, ml::kHid);
+  put(ml::kW4, ml::kOutPad, ml::kHid, ml::kCand, ml::kHid, ml::kHid);
+  devAlloc(&d_mlp, p.size());
+  CK(cudaMemcpy(d_mlp, p.data(), p.size() * 4, cudaMemcpyHostToDevice));
+  devAlloc(&d_mlp_partial, (size_t)ml::gradBlocks(num_sms) * ml::kPartial);
+  // domain boxes and the normalisation of positions to the scene box
+  std::vector<float> bx(6 * (size_t)D);
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int d = 0; d < D; ++d)
+    for (int c = 0; c < 3; ++c) {
+      bx[6 * d + c] = hdoms[d].bmin[c];
+      bx[6 * d + 3 + c] = hdoms[d].bmax[c];
+      lo[c] = std::min(lo[c], hdoms[d].bmin[c]);
+      hi[c] = std::max(hi[c], hdoms[d].bmax[c]);
+    }
+  float half = 0.0f;
+  for (int c = 0; c < 3; ++c) {
+    mlp_norm.centre[c] = 0.5f * (lo[c] + hi[c]);
+    half = std::max(half, 0.5f * (hi[c] - lo[c]));
+  }
+  mlp_norm.scale = half > 0.0f ? 1.0f / half : 1.0f;
+  devAlloc(&d_boxes, bx.size());
+  CK(cudaMemcpy(d_boxes, bx.data(), bx.size() * 4, cudaMemcpyHostToDevice));
+  pairs_cap = (uint64_t)cfg.learn_samples;
+  if (pairs_cap) devAlloc(&d_pairs, pairs_cap);
+  devAlloc(&d_pairs_filled, 1);
+  CK(cudaMemset(d_pairs_filled, 0, sizeof(unsigned long long)));
+  devAlloc(&d_predcount, D);
+  devAlloc(&d_mlp_err, 1);
+  CK(cudaMemset(d_mlp_err, 0, sizeof(int)));
+}
+
+mlp::ArenaSource Tracer::arenaSource() const {
+  mlp::ArenaSource a;
+  a.count = d_alive_count;
+  a.list = d_alive_list;
+  a.org = rays[cur].org;
+  a.dir = rays[cur].dir;
+  a.arena = d_arena;
+  a.list_off = d_list_off;
+  a.list_cnt = d_list_cnt;
+  return a;
+}
+
+mlp::Net Tracer::proposalNet() const {
+  mlp::Net n;
+  n.params = d_mlp;
+  n.boxes = d_boxes;
+  n.norm = mlp_norm;
+  n.error = d_mlp_err;
+  return n;
+}
+
+// Training pairs of the radiance rays just resolved (their lists are still in
+// the arena); the pair buffer fills in alive order up to its capacity.
+void Tracer::collectPairs() {
+  if (!pairs_cap) return;
+  mlp::launchCollect(stream, arenaSource(), d_ray_key, d_domains, d_pairs, d_pairs_filled, pairs_cap, d_lab,
+                     d_lflag, d_lsel, d_lnsel, d_block_tmp, compact_blocks);
+  launches += 6;
+}
+
+// Predicted hits per domain for the out-of-core order (the prediction itself
+// is already in d_pred when the schedule used it).
+void Tracer::predictDomainCounts(bool run_predict) {
+  CK(cudaMemsetAsync(d_predcount, 0, (size_t)D * 4, stream));
+  if (run_predict) {
+    mlp::launchPredictArena(stream, proposalNet(), arenaSource(), d_pred, num_sms * 4);
+    launches += 1;
+  }
+  mlp::launchPredCount(stream, arenaSource(), d_pred, d_predcount, num_sms * 4);
+  launches += 1;
+  use_pred_order = true;
+}
+
+// learn_epochs passes of Adam (batch learn_batch) over the collected pairs.
+void Tracer::trainProposal() {
+  namespace ml = mlp;
+  const int64_t n = std::min<int64_t>(pairs_filled, (int64_t)pairs_cap);
+  cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
+  CK(cudaEventRecord(e0, stream));
+  float* params = d_mlp;
+  float* m = d_mlp + ml::kParams;
+  float* v = d_mlp + 2 * ml::kParams;
+  float* grad = d_mlp + 3 * ml::kParams;
+  if (n > 0) {
+    const int64_t B = std::min<int64_t>(cfg.learn_batch, n);
+    const int64_t per_epoch = (n + B - 1) / B;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((B + ml::kTile - 1) / ml::kTile,
+                                                                  ml::gradBlocks(num_sms)));
+    for (int64_t k = 0; k < per_epoch * cfg.learn_epochs; ++k) {
+      const int64_t start = (k % per_epoch) * B;
+      const int64_t len = std::min<int64_t>(B, n - start);
+      ml::launchGrad(stream, proposalNet(), d_pairs + start, len, 1.0f / (float)len, d_mlp_partial, grid);
+      ml::launchReduceAdam(stream, d_mlp_partial, grid, grad, params, m, v, cfg.learn_lr, ++adam_step);
+    }
+  }
+  CK(cudaEventRecord(e1, stream));
+  CK(cudaStreamSynchronize(stream));
+  CK(cudaGetLastError());
+  int err = 0;
+  CK(cudaMemcpy(&err, d_mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) throw std::runtime_error("a tensor-core wait of the learned proposal gave up");
+  float tail[2] = {0.f, 0.f};
+  if (n > 0) CK(cudaMemcpy(tail, grad + ml::kParams, sizeof(tail), cudaMemcpyDeviceToHost));
+  learn_loss = tail[1] > 0.f ? tail[0] / tail[1] : 0.0;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  learn_ms = ms;
+  proposal_trained = true;
+  // the pair buffer is no longer needed
+  devFree(d_pairs);
 }
 
 // Screen bins of the primary rays.  Each domain box is projected through the
@@ -1140,7 +1398,20 @@ void Tracer::buildScreenBins() {
   for (int k = 0; k < 3; ++k) fw[k] = (ll[k] + 0.5 * wv[k] + 0.5 * hv[k]) - pos[k];
   auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
   const double fw2 = dot(fw, fw), wv2 = dot(wv, wv), hv2 = dot(hv, hv);
+  // domains by distance from the camera to their boxes, so that each bin's
+  // list is close to the entry order of its rays
+  std::vector<std::pair<double, int>> near(D);
   for (int d = 0; d < D; ++d) {
+    double q2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double c = std::min(std::max(pos[k], (double)hdoms[d].bmin[k]), (double)hdoms[d].bmax[k]);
+      q2 += (c - pos[k]) * (c - pos[k]);
+    }
+    near[d] = {q2, d};
+  }
+  std::sort(near.begin(), near.end());
+  for (const auto& nd : near) {
+    const int d = nd.second;
     const DomainDev& dd = hdoms[d];
     double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
     bool everywhere = false;
@@ -1211,13 +1482,14 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     occl_events.clear();
     copy_events.clear();
     dbg.clear();
+    use_pred_order = false;
     CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
     CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
     CK(cudaEventRecord(ev_start, stream));
     if (use_bins) buildScreenBins();
     for (size_t k = 0; k < waves.size(); ++k) {
       const bool capture = cfg.debug_capture && k == 0;
-      if (ooc && cfg.schedule_policy == 2 && !capture) traceWaveBatched(waves[k]);
+      if (ooc && cfg.schedule_policy >= 2 && !capture) traceWaveBatched(waves[k]);
       else traceWave(waves[k], capture);
     }
     CK(cudaEventRecord(ev_stop, stream));
@@ -1232,6 +1504,13 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     if (ctr.list_overflows) throw OverflowError("a ray overlapped more than 32 domains");
     if (ctr.error_flags & (kErrBadNode | kErrTraversalBound))
       throw std::runtime_error("BVH traversal left its bounds (corrupt hierarchy)");
+    learn_ms = 0.0;
+    if (learned() && !proposal_trained) {
+      unsigned long long filled = 0;
+      CK(cudaMemcpy(&filled, d_pairs_filled, sizeof(filled), cudaMemcpyDeviceToHost));
+      pairs_filled = (int64_t)filled;
+      if (++frames_collected >= cfg.learn_frames || filled >= pairs_cap) trainProposal();
+    }
     size_t img_bytes = (size_t)cfg.image_w * cfg.image_h * sizeof(float4);
     if (out) {
       if (out_is_device) {
@@ -1278,6 +1557,10 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->scene_triangles = (int64_t)total_tris;
       st->scene_bytes = (int64_t)scene_bytes;
       st->h2d_ms = sum(copy_events);
+      st->learn_pairs = pairs_filled;
+      st->learn_trained = proposal_trained ? 1 : 0;
+      st->learn_ms = learn_ms;
+      st->learn_loss = learn_loss;
     }
     return;
   }
@@ -1485,6 +1768,12 @@ void spray_gpu_config_defaults(spray_gpu_config* c) {
   c->num_ranks = 1;
   c->rank = 0;
   c->cull = 1;
+  c->learn_samples = (int64_t)1 << 24;
+  c->learn_batch = 65536;
+  c->learn_epochs = 2;
+  c->learn_lr = 1e-3f;
+  c->learn_seed = 1;
+  c->learn_frames = 4;
 }
 
 const char* spray_gpu_last_error(void) { return spray::g_last_error.c_str(); }

@@ -12,6 +12,7 @@
 
 #include "../../include/spray_gpu.h"
 #include "kernels.cuh"
+#include "mlp.cuh"
 
 namespace spray {
 
@@ -82,7 +83,16 @@ class Tracer {
   void beginWave(const Wave& w);
   ShadeArgs shadeArgs(int b, int S);
   void schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t* list, int S,
-                bool primary = false, bool into_shadow_queues = false);
+                bool primary = false, bool into_shadow_queues = false, bool predicted = false);
+  // learned domain-order proposal (schedule_policy 3)
+  bool learned() const { return cfg.schedule_policy == 3; }
+  void setupProposal();
+  void freeProposal();
+  mlp::ArenaSource arenaSource() const;
+  mlp::Net proposalNet() const;
+  void collectPairs();
+  void predictDomainCounts(bool run_predict);
+  void trainProposal();
   void buildScreenBins();
   TraceArgs traceArgs(int order_by_depth, int S);
   SceneDev sceneDev() const;
@@ -96,7 +106,7 @@ class Tracer {
                       size_t max_verts, size_t slot_bytes);
   void loadDomain(int d, int slot, cudaStream_t s);
   void traceOutOfCore(bool shadow, const std::vector<int>& order, int S);
-  void oocPass(bool with_radiance, bool with_shadow, int S);
+  void oocPass(bool with_radiance, bool with_shadow, int S, int rbuckets);
   std::vector<int> residentFirst(const std::vector<int>& order) const;
   std::vector<int> scoreOrder();
 
@@ -155,7 +165,7 @@ class Tracer {
   // wave buffers
   int64_t cap_samples = 0;
   uint64_t cap_entries = 0, needed_entries = 0;
-  int sched_blocks = 0, sched_warps = 0, compact_blocks = 0;
+  int sched_blocks = 0, sched_warps = 0, sched_chunks = 0, compact_blocks = 0;
   int cur = 0;
   RayBuf rays[2] = {};
   int32_t* d_pixid = nullptr;
@@ -176,6 +186,29 @@ class Tracer {
   uint32_t* d_list_cnt = nullptr;
   uint32_t* d_hist = nullptr;
   long long* d_dstats = nullptr;
+  // learned proposal: parameters | Adam m | Adam v | gradient, per-CTA
+  // partials, domain boxes, collected pairs, per-alive-ray prediction and
+  // collection scratch, predicted hits per domain
+  float* d_mlp = nullptr;
+  float* d_mlp_partial = nullptr;
+  float* d_boxes = nullptr;
+  mlp::Sample* d_pairs = nullptr;
+  unsigned long long* d_pairs_filled = nullptr;
+  uint8_t* d_pred = nullptr;
+  int8_t* d_lab = nullptr;
+  uint8_t* d_lflag = nullptr;
+  uint32_t* d_lsel = nullptr;
+  uint32_t* d_lnsel = nullptr;
+  uint32_t* d_predcount = nullptr;
+  int* d_mlp_err = nullptr;
+  mlp::Norm mlp_norm{};
+  uint64_t pairs_cap = 0;
+  bool proposal_trained = false;
+  bool use_pred_order = false;  // this pass orders domains by predicted hits
+  int frames_collected = 0;
+  int adam_step = 0;
+  double learn_ms = 0.0, learn_loss = 0.0;
+  int64_t pairs_filled = 0;
   uint2* d_sentries = nullptr;     // batched out of core: shadow queues beside the radiance ones
   uint32_t* d_skey_start = nullptr;
   uint32_t* d_snum_entries = nullptr;

@@ -60,7 +60,9 @@ def test_invalid_config_rejected(lib_built):
     assert e.value.code in (sg.EINVAL, sg.ECUDA)
 
 
-@pytest.mark.parametrize("kw", [dict(schedule_policy=3), dict(schedule_policy=-1), dict(ooc_batch=-1)])
+@pytest.mark.parametrize("kw", [dict(schedule_policy=4), dict(schedule_policy=-1), dict(ooc_batch=-1),
+                                dict(schedule_policy=3, learn_batch=0), dict(schedule_policy=3, learn_lr=0.0),
+                                dict(schedule_policy=3, learn_frames=0)])
 def test_out_of_core_options_validated(lib_built, kw):
     """Options are checked before any device is touched."""
     import spray_gb300 as sg

@@ -373,3 +373,51 @@ def test_batched_pass_skips_fully_culled_domains(lib_built, scene64):
     assert st2["visits_shadow"] <= st0["visits_shadow"]
     assert st2["domain_loads"] < st0["domain_loads"]
 
+
+
+LEARN = dict(schedule_policy=3, learn_frames=1, learn_batch=8192, learn_epochs=8)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(cache_size=16), dict(cache_size=5, ooc_batch=1)])
+def test_learned_proposal_keeps_the_image(lib_built, kw):
+    """The learned order changes which entries are traced when, never the image."""
+    scene = scenes.wavelet_grid(4, 32, colors="albedo", light="quad")
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=4, rr_depth=3)
+    cam = scenes.orbit_camera(scene)
+    ref = sg.Tracer(cfg)
+    ref.set_scene(scene)
+    ref.set_camera(*cam)
+    want, _ = ref.trace()
+    t = sg.Tracer(cfg, **LEARN, **kw)
+    t.set_scene(scene)
+    t.set_camera(*cam)
+    img1, st1 = t.trace()  # collects pairs, trains after the frame
+    assert st1["learn_trained"] == 1 and st1["learn_pairs"] > 1000 and st1["learn_ms"] > 0
+    assert np.isfinite(st1["learn_loss"]) and st1["learn_loss"] < np.log(8)
+    img2, st2 = t.trace()  # ordered by the trained proposal
+    img3, _ = t.trace()
+    for img in (img1, img2, img3):
+        assert np.array_equal(bits(img), bits(want))
+    assert st2["learn_ms"] == 0
+
+
+def test_trained_proposal_gains_over_untrained(lib_built):
+    """Out of core, the trained network's order culls more radiance entries than
+    the same method with the untrained (randomly initialised) network."""
+    scene = scenes.wavelet_grid(4, 32, colors="albedo", light="quad")
+    cfg = small_config(image_w=320, image_h=240, ao_mode=0, pixel_samples=4, bounces=4, rr_depth=3,
+                       cache_size=16)
+    cam = scenes.orbit_camera(scene)
+    out = {}
+    for name, epochs in (("untrained", 0), ("trained", 8)):
+        t = sg.Tracer(cfg, **dict(LEARN, learn_epochs=epochs))
+        t.set_scene(scene)
+        t.set_camera(*cam)
+        t.trace()
+        img, st = t.trace()
+        out[name] = (img, st)
+    (iu, su), (it, s_t) = out["untrained"], out["trained"]
+    assert su["learn_trained"] == 1 and s_t["learn_trained"] == 1
+    assert np.array_equal(bits(iu), bits(it))
+    assert s_t["visits_radiance"] < 0.95 * su["visits_radiance"], (s_t["visits_radiance"], su["visits_radiance"])
+    assert s_t["visits_culled"] > su["visits_culled"]
