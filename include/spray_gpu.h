@@ -92,7 +92,8 @@ typedef struct spray_gpu_config {
   int32_t learn_seed;           /* policy 3: weight initialisation seed (1) */
   int32_t learn_frames;         /* policy 3: train after this many frames even if fewer pairs
                                    were collected (4) */
-  int32_t reserved0;
+  int32_t graphs;               /* in core: capture the frame's launches once into a CUDA graph and
+                                   replay it while the buffers stay the same (1) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as

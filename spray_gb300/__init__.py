@@ -41,7 +41,7 @@ class ConfigC(C.Structure):
         ("schedule_policy", C.c_int32),
         ("ooc_batch", C.c_int32), ("learn_samples", C.c_int64), ("learn_batch", C.c_int32),
         ("learn_epochs", C.c_int32), ("learn_lr", C.c_float), ("learn_seed", C.c_int32),
-        ("learn_frames", C.c_int32), ("reserved0", C.c_int32),
+        ("learn_frames", C.c_int32), ("graphs", C.c_int32),
     ]
 
 

@@ -205,7 +205,8 @@ struct ShadeArgs {
 };
 
 // ---------------------------------------------------------------- launchers
-void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int ntiles,
+// The camera is read from device memory, so a captured frame follows camera changes.
+void launchGenPrimary(cudaStream_t s, const CameraDev* cam, const TileDev* tiles, int ntiles,
                       int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
                       uint32_t* alive_count, int32_t* alive_idx, Counters* ctr);
 // scan_tmp holds kMaxScanBlocks words.  Launches 5 kernels.

@@ -31,11 +31,12 @@ __device__ __forceinline__ uint32_t warpExclusiveScan(uint32_t v, uint32_t* tota
 // (src/ooc/ooc_tracer.inl:84-172) with Camera::generateRay
 // (src/render/camera.h:173-209): u = x / W, v = y / H, jitter drawn from a
 // sampler seeded with the tile-local sample id when pixel_samples > 1.
-__global__ void kGenPrimary(CameraDev cam, const TileDev* __restrict__ tiles, int ntiles,
+__global__ void kGenPrimary(const CameraDev* __restrict__ camp, const TileDev* __restrict__ tiles, int ntiles,
                             int64_t nsamples, int spp, int image_w, RayBuf rays,
                             uint32_t* alive_list, uint32_t* alive_count, int32_t* alive_idx,
                             Counters* ctr) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const CameraDev cam = *camp;
   if (i == 0) {
     *alive_count = (uint32_t)nsamples;
     atomicAdd(&ctr->rays_primary, (unsigned long long)nsamples);
@@ -70,7 +71,7 @@ __global__ void kGenPrimary(CameraDev cam, const TileDev* __restrict__ tiles, in
   alive_idx[i] = (int32_t)i;
 }
 
-void launchGenPrimary(cudaStream_t s, CameraDev cam, const TileDev* tiles, int ntiles,
+void launchGenPrimary(cudaStream_t s, const CameraDev* cam, const TileDev* tiles, int ntiles,
                       int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
                       uint32_t* alive_count, int32_t* alive_idx, Counters* ctr) {
   int threads = 256;

@@ -158,13 +158,16 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   CK(cudaEventCreate(&ev_start));
   CK(cudaEventCreate(&ev_stop));
   devAlloc(&d_ctr, 1);
+  devAlloc(&d_cam, 1);
 }
 
 Tracer::~Tracer() {
   cudaSetDevice(cfg.device);
   freeScene();
   freeBuffers();
+  dropGraph();
   devFree(d_ctr);
+  devFree(d_cam);
   for (auto& e : ev_pool) cudaEventDestroy(e);
   if (ev_start) cudaEventDestroy(ev_start);
   if (ev_stop) cudaEventDestroy(ev_stop);
@@ -198,7 +201,14 @@ void Tracer::freeScene() {
   devFree(d_lights);
 }
 
+void Tracer::dropGraph() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  graph_exec = nullptr;
+  graph_gen = 0;
+}
+
 void Tracer::freeBuffers() {
+  ++buf_gen;
   for (int k = 0; k < 2; ++k) {
     devFree(rays[k].org);
     devFree(rays[k].dir);
@@ -631,6 +641,15 @@ void Tracer::planWaves() {
     }
     waves.push_back(w);
   }
+  wave_tiles.assign(tiles.size(), TileDev{});
+  for (const Wave& w : waves) {
+    int64_t base = 0;
+    for (int k = 0; k < w.num_tiles; ++k) {
+      const HostTile& t = tiles[w.first_tile + k];
+      wave_tiles[w.first_tile + k] = TileDev{t.x, t.y, t.w, t.h, base};
+      base += (int64_t)t.w * t.h * cfg.pixel_samples;
+    }
+  }
 }
 
 void Tracer::ensureBuffers(int64_t nsamples) {
@@ -646,6 +665,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
     throw std::runtime_error("too few scheduling chunks for 16-bit histogram counters");
   if (nsamples <= cap_samples && cap_entries >= needed_entries) return;
   freeBuffers();
+  ++buf_gen;
   int64_t N = std::max<int64_t>(nsamples, 1024);
   int64_t NS = N * S;
   if (needed_entries == 0) needed_entries = (uint64_t)std::max<int64_t>(4 * N, 2 * NS);
@@ -798,6 +818,12 @@ SceneDev Tracer::sceneDev() const {
   return s;
 }
 
+// Timing event on the work stream; during graph capture it becomes an event
+// record node of the graph, so replays still time their kernels.
+void Tracer::record(cudaEvent_t e) {
+  CK(cudaEventRecordWithFlags(e, stream, capturing ? cudaEventRecordExternal : cudaEventRecordDefault));
+}
+
 cudaEvent_t Tracer::poolEvent() {
   if (ev_used == ev_pool.size()) {
     cudaEvent_t e;
@@ -807,21 +833,11 @@ cudaEvent_t Tracer::poolEvent() {
   return ev_pool[ev_used++];
 }
 
-// Uploads the wave's tiles and generates its primary rays.
+// Generates the wave's primary rays (tiles and camera are already on the device).
 void Tracer::beginWave(const Wave& w) {
-  const int spp = cfg.pixel_samples;
-  std::vector<TileDev> td(w.num_tiles);
-  int64_t base = 0;
-  for (int k = 0; k < w.num_tiles; ++k) {
-    const HostTile& t = tiles[w.first_tile + k];
-    td[k] = TileDev{t.x, t.y, t.w, t.h, base};
-    base += (int64_t)t.w * t.h * spp;
-  }
-  CK(cudaMemcpyAsync(d_tiles, td.data(), td.size() * sizeof(TileDev), cudaMemcpyHostToDevice, stream));
-  h2d_bytes += td.size() * sizeof(TileDev);
   cur = 0;
-  launchGenPrimary(stream, cam, d_tiles, w.num_tiles, w.samples, spp, cfg.image_w, rays[0],
-                   d_alive_list, d_alive_count, d_alive_idx, d_ctr);
+  launchGenPrimary(stream, d_cam, d_tiles + w.first_tile, w.num_tiles, w.samples, cfg.pixel_samples,
+                   cfg.image_w, rays[0], d_alive_list, d_alive_count, d_alive_idx, d_ctr);
   launches += 1;
 }
 
@@ -866,10 +882,10 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
     }
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
-    CK(cudaEventRecord(s0, stream));
+    record(s0);
     schedule(false, order_by_depth, d_alive_count, d_alive_list, S, b == 0, false,
              learned() && proposal_trained && order_by_depth && !capture);
-    CK(cudaEventRecord(s1, stream));
+    record(s1);
     sched_events.push_back({s0, s1});
     if (capture) {
       launchScores(stream, d_dstats, D, cfg.list_size, d_scores, d_order);
@@ -895,9 +911,9 @@ void Tracer::traceWave(const Wave& w, bool capture) {
         ta.bucket = order_by_depth ? k : -1;
         ta.work = d_work + k;
         cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
-        CK(cudaEventRecord(t0, stream));
+        record(t0);
         launchTraceClosest(stream, ta, num_sms * 4);
-        CK(cudaEventRecord(t1, stream));
+        record(t1);
         trace_events.push_back({t0, t1});
       }
       launches += nb;
@@ -924,9 +940,9 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       CK(cudaMemsetAsync(d_work, 0, 4, stream));
       TraceArgs to = traceArgs(0, S);
       cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
-      CK(cudaEventRecord(o0, stream));
+      record(o0);
       launchTraceOccluded(stream, to, num_sms * 4);
-      CK(cudaEventRecord(o1, stream));
+      record(o1);
       occl_events.push_back({o0, o1});
       launches += 1;
     }
@@ -1179,10 +1195,10 @@ void Tracer::traceWaveBatched(const Wave& w) {
   auto scheduleRadiance = [&](bool primary) {
     CK(cudaMemsetAsync(d_dstats, 0, (size_t)D * cfg.list_size * sizeof(long long), stream));
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
-    CK(cudaEventRecord(s0, stream));
+    record(s0);
     const bool pred = learned() && proposal_trained;
     schedule(false, order_by_depth, d_alive_count, d_alive_list, S, primary, false, pred && order_by_depth);
-    CK(cudaEventRecord(s1, stream));
+    record(s1);
     sched_events.push_back({s0, s1});
     if (pred) predictDomainCounts(!order_by_depth);
   };
@@ -1374,6 +1390,41 @@ void Tracer::trainProposal() {
   devFree(d_pairs);
 }
 
+// Records every launch of an in-core frame (counter and image clears, all
+// waves) into a CUDA graph.  Nothing in that sequence waits on the host: ray
+// and entry counts stay on the device, the camera and tiles are read from
+// device memory, so replaying the graph renders whatever camera was uploaded.
+void Tracer::captureFrame() {
+  dropGraph();
+  const int64_t l0 = launches;
+  sched_events.clear();
+  trace_events.clear();
+  occl_events.clear();
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
+  capturing = true;
+  try {
+    CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
+    CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
+    for (const Wave& w : waves) traceWave(w, false);
+  } catch (...) {
+    capturing = false;
+    cudaStreamEndCapture(stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  capturing = false;
+  CK(cudaStreamEndCapture(stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  graph_gen = buf_gen;
+  graph_launches = launches - l0;
+  graph_sched = sched_events;
+  graph_trace = trace_events;
+  graph_occl = occl_events;
+}
+
 // Screen bins of the primary rays.  Each domain box is projected through the
 // camera onto the image plane; the pixel rectangle of its 8 corners, widened
 // by two pixels, lists the domain in every bin it touches.  A box with a
@@ -1451,11 +1502,14 @@ void Tracer::buildScreenBins() {
     devFree(d_bin_start);
     bin_start_cap = nb + 1;
     devAlloc(&d_bin_start, bin_start_cap);
+    ++buf_gen;
   }
   if (ids.size() > bin_ids_cap) {
+    // headroom, so that camera moves rarely reallocate (and recapture)
     devFree(d_bin_ids);
-    bin_ids_cap = ids.size();
+    bin_ids_cap = ids.size() + ids.size() / 2;
     devAlloc(&d_bin_ids, bin_ids_cap);
+    ++buf_gen;
   }
   CK(cudaMemcpyAsync(d_bin_start, start.data(), start.size() * 4, cudaMemcpyHostToDevice, stream));
   CK(cudaMemcpyAsync(d_bin_ids, ids.data(), ids.size() * 2, cudaMemcpyHostToDevice, stream));
@@ -1483,14 +1537,28 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     copy_events.clear();
     dbg.clear();
     use_pred_order = false;
-    CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
-    CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
     CK(cudaEventRecord(ev_start, stream));
     if (use_bins) buildScreenBins();
-    for (size_t k = 0; k < waves.size(); ++k) {
-      const bool capture = cfg.debug_capture && k == 0;
-      if (ooc && cfg.schedule_policy >= 2 && !capture) traceWaveBatched(waves[k]);
-      else traceWave(waves[k], capture);
+    CK(cudaMemcpyAsync(d_cam, &cam, sizeof(CameraDev), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_tiles, wave_tiles.data(), wave_tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice,
+                       stream));
+    h2d_bytes += sizeof(CameraDev) + wave_tiles.size() * sizeof(TileDev);
+    const bool graphed = cfg.graphs && !ooc && !cfg.debug_capture && !learned();
+    if (graphed) {
+      if (!graph_exec || graph_gen != buf_gen) captureFrame();
+      CK(cudaGraphLaunch(graph_exec, stream));
+      launches = graph_launches;
+      sched_events = graph_sched;
+      trace_events = graph_trace;
+      occl_events = graph_occl;
+    } else {
+      CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
+      CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
+      for (size_t k = 0; k < waves.size(); ++k) {
+        const bool capture = cfg.debug_capture && k == 0;
+        if (ooc && cfg.schedule_policy >= 2 && !capture) traceWaveBatched(waves[k]);
+        else traceWave(waves[k], capture);
+      }
     }
     CK(cudaEventRecord(ev_stop, stream));
     Counters ctr;
@@ -1498,6 +1566,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     CK(cudaStreamSynchronize(stream));
     CK(cudaGetLastError());
     if (ctr.arena_overflows || ctr.entry_overflows) {
+      dropGraph();
       needed_entries = cap_entries * 2;
       continue;  // retrace with larger queues
     }
@@ -1774,6 +1843,7 @@ void spray_gpu_config_defaults(spray_gpu_config* c) {
   c->learn_lr = 1e-3f;
   c->learn_seed = 1;
   c->learn_frames = 4;
+  c->graphs = 1;
 }
 
 const char* spray_gpu_last_error(void) { return spray::g_last_error.c_str(); }

@@ -135,6 +135,17 @@ class Tracer {
   float* d_normals = nullptr;
   float* d_lights = nullptr;
   CameraDev cam{};
+  CameraDev* d_cam = nullptr;
+  std::vector<TileDev> wave_tiles;   // every wave's tiles, sample bases relative to the wave
+  // in-core frame captured as a CUDA graph; recaptured when buffers change
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t buf_gen = 1, graph_gen = 0;
+  int64_t graph_launches = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> graph_sched, graph_trace, graph_occl;
+  void captureFrame();
+  void record(cudaEvent_t e);
+  bool capturing = false;
+  void dropGraph();
   std::vector<size_t> domain_verts;
 
   // out-of-core cache

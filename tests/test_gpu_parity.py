@@ -421,3 +421,25 @@ def test_trained_proposal_gains_over_untrained(lib_built):
     assert np.array_equal(bits(iu), bits(it))
     assert s_t["visits_radiance"] < 0.95 * su["visits_radiance"], (s_t["visits_radiance"], su["visits_radiance"])
     assert s_t["visits_culled"] > su["visits_culled"]
+
+
+def test_graph_replay_follows_camera_and_matches_direct_launches(lib_built, scene64):
+    """The in-core frame captured as a CUDA graph renders what direct launches
+    render, across camera moves and several wavefronts per frame."""
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3, wave_samples=5000)
+    tg = sg.Tracer(cfg, graphs=1)
+    td = sg.Tracer(cfg, graphs=0)
+    for t in (tg, td):
+        t.set_scene(scene64)
+    for frame in range(3):
+        cam = scenes.orbit_camera(scene64, frame=frame)
+        out = []
+        for t in (tg, td):
+            t.set_camera(*cam)
+            out.append(t.trace())
+        (ig, sgr), (idr, sd) = out
+        assert np.array_equal(bits(ig), bits(idr)), frame
+        for k in ("rays_primary", "rays_shadow", "rays_bounce", "visits_radiance", "visits_shadow",
+                  "kernel_launches", "trace_launches"):
+            assert sgr[k] == sd[k], (frame, k)
+        assert sgr["trace_ms"] > 0 and sgr["frame_ms"] > 0
