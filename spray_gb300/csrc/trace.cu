@@ -88,8 +88,20 @@ __device__ __forceinline__ void raise(Counters* ctr, unsigned long long bit) {
   atomicOr(&ctr->error_flags, bit);
 }
 
+// Marks the end of a traversal (never a child reference: empty slots are skipped).
+constexpr int kDone = (int)kEmptyChild;
+
 // Closest hit in one domain.  best_key enters as the key to beat and leaves as
 // the best found; returns true when this domain improved it.
+//
+// While-while traversal: a thread expands inner nodes until the nearest
+// pending entry is a leaf (the loop ends when every active thread holds a
+// leaf or has finished), then the threads test their leaves together.  Inner
+// nodes and leaves share one near-to-far stack, so a leaf is tested only after
+// every nearer subtree, and entries beyond the best hit are dropped on pop.
+// The hit does not depend on the order: the packed (t | triangle) key is a
+// total order and a subtree is skipped only when its box starts beyond the
+// best t found.
 __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const TravRay& r,
                                 uint64_t& best_key, float& best_t, uint32_t& best_prim,
                                 float& best_u, float& best_v, Counters* ctr,
@@ -98,134 +110,138 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
   const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
   uint2 stack[kStack];
   int sp = 0;
-  int node = 0;
   bool found = false;
-  for (int steps = 0;; ++steps) {
-    if (steps >= kMaxSteps) {
-      raise(ctr, kErrTraversalBound);
-      break;
-    }
-    if ((unsigned)node >= (unsigned)dom.num_nodes) {
-      raise(ctr, kErrBadNode);
-      break;
-    }
-    float tn[4];
-    ++nnodes;
-    int mask = testChildren(nodes, node, r, kRayEpsilon, best_t, tn);
-    int4 ch = loadChildren(nodes, node);
-    // order hit children near to far
-    int ord[4], no = 0;
-    for (int c = 0; c < 4; ++c)
-      if ((mask & (1 << c)) && childAt(ch, c) != kEmptyChild) {
-        int j = no++;
-        while (j > 0 && tn[ord[j - 1]] > tn[c]) {
-          ord[j] = ord[j - 1];
-          --j;
-        }
-        ord[j] = c;
-      }
-    // leaves now, inner children onto the stack far to near
-    for (int k = 0; k < no; ++k) {
-      int c = ord[k];
-      int ref = childAt(ch, c);
-      if (ref < 0) {
-        if (tn[c] > best_t) continue;
-        uint32_t v = ~(uint32_t)ref;
-        uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
-        if (first + cnt > (uint32_t)dom.num_tris) {
-          raise(ctr, kErrBadNode);
-          continue;
-        }
-        ntris += cnt;
-        for (uint32_t q = 0; q < cnt; ++q) {
-          const float4* tp = tris + 3 * (size_t)(first + q);
-          float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
-          float t, u, vv;
-          if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z),
-                                v3(cc.x, cc.y, cc.z), kRayEpsilon, __int_as_float(0x7f800000),
-                                &t, &u, &vv)) {
-            uint32_t prim = __float_as_uint(a.w);
-            uint64_t key = packHitKey(t, dom.gprim_base + prim);
-            if (key < best_key) {
-              best_key = key;
-              best_t = t;
-              best_prim = prim;
-              best_u = u;
-              best_v = vv;
-              found = true;
-            }
-          }
-        }
-      }
-    }
-    for (int k = no - 1; k >= 0; --k) {
-      int c = ord[k];
-      int ref = childAt(ch, c);
-      if (ref >= 0 && sp < kStack) stack[sp++] = make_uint2((uint32_t)ref, __float_as_uint(tn[c]));
-    }
-    // pop the nearest pending node still in front of the best hit
-    bool next = false;
+  int steps = 0;
+  auto pop = [&]() -> int {
     while (sp > 0) {
-      uint2 e = stack[--sp];
-      if (__uint_as_float(e.y) <= best_t) {
-        node = (int)e.x;
-        next = true;
-        break;
+      const uint2 e = stack[--sp];
+      if (__uint_as_float(e.y) <= best_t) return (int)e.x;
+    }
+    return kDone;
+  };
+  int cur = 0;
+  while (cur != kDone) {
+    // inner nodes until the nearest pending entry is a leaf
+    while (cur >= 0) {
+      if (++steps > kMaxSteps) {
+        raise(ctr, kErrTraversalBound);
+        return found;
+      }
+      if ((unsigned)cur >= (unsigned)dom.num_nodes) {
+        raise(ctr, kErrBadNode);
+        return found;
+      }
+      float tn[4];
+      ++nnodes;
+      const int mask = testChildren(nodes, cur, r, kRayEpsilon, best_t, tn);
+      const int4 ch = loadChildren(nodes, cur);
+      int ord[4], no = 0;
+      for (int c = 0; c < 4; ++c)
+        if ((mask & (1 << c)) && childAt(ch, c) != kEmptyChild) {
+          int j = no++;
+          while (j > 0 && tn[ord[j - 1]] > tn[c]) {
+            ord[j] = ord[j - 1];
+            --j;
+          }
+          ord[j] = c;
+        }
+      // far to near, so the nearest child is on top
+      for (int k = no - 1; k >= 0; --k) {
+        if (sp == kStack) {
+          raise(ctr, kErrTraversalBound);
+          return found;
+        }
+        const int c = ord[k];
+        stack[sp++] = make_uint2((uint32_t)childAt(ch, c), __float_as_uint(tn[c]));
+      }
+      cur = pop();
+    }
+    if (cur == kDone) break;
+    // leaf
+    const uint32_t v = ~(uint32_t)cur;
+    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+    if (first + cnt > (uint32_t)dom.num_tris) {
+      raise(ctr, kErrBadNode);
+      return found;
+    }
+    ntris += cnt;
+    for (uint32_t q = 0; q < cnt; ++q) {
+      const float4* tp = tris + 3 * (size_t)(first + q);
+      const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+      float t, u, vv;
+      if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
+                            kRayEpsilon, __int_as_float(0x7f800000), &t, &u, &vv)) {
+        const uint32_t prim = __float_as_uint(a.w);
+        const uint64_t key = packHitKey(t, dom.gprim_base + prim);
+        if (key < best_key) {
+          best_key = key;
+          best_t = t;
+          best_prim = prim;
+          best_u = u;
+          best_v = vv;
+          found = true;
+        }
       }
     }
-    if (!next) break;
+    cur = pop();
   }
   return found;
 }
 
-// Any hit in (tnear, tfar) in one domain.
+// Any hit in (tnear, tfar) in one domain, with the same while-while loop.
 __device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar,
                             Counters* ctr, unsigned long long& nnodes, unsigned long long& ntris) {
   const BvhNode4* nodes = sc.nodes + dom.node_base;
   const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
   int stack[kStack];
   int sp = 0;
-  int node = 0;
-  for (int steps = 0;; ++steps) {
-    if (steps >= kMaxSteps) {
-      raise(ctr, kErrTraversalBound);
-      return false;
+  int steps = 0;
+  int cur = 0;
+  while (cur != kDone) {
+    while (cur >= 0) {
+      if (++steps > kMaxSteps) {
+        raise(ctr, kErrTraversalBound);
+        return false;
+      }
+      if ((unsigned)cur >= (unsigned)dom.num_nodes) {
+        raise(ctr, kErrBadNode);
+        return false;
+      }
+      float tn[4];
+      ++nnodes;
+      const int mask = testChildren(nodes, cur, r, kRayEpsilon, tfar, tn);
+      const int4 ch = loadChildren(nodes, cur);
+      for (int c = 0; c < 4; ++c) {
+        if (!(mask & (1 << c))) continue;
+        const int ref = childAt(ch, c);
+        if (ref == kEmptyChild) continue;
+        if (sp == kStack) {
+          raise(ctr, kErrTraversalBound);
+          return false;
+        }
+        stack[sp++] = ref;
+      }
+      cur = sp > 0 ? stack[--sp] : kDone;
     }
-    if ((unsigned)node >= (unsigned)dom.num_nodes) {
+    if (cur == kDone) break;
+    const uint32_t v = ~(uint32_t)cur;
+    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+    if (first + cnt > (uint32_t)dom.num_tris) {
       raise(ctr, kErrBadNode);
       return false;
     }
-    float tn[4];
-    ++nnodes;
-    int mask = testChildren(nodes, node, r, kRayEpsilon, tfar, tn);
-    int4 ch = loadChildren(nodes, node);
-    for (int c = 0; c < 4; ++c) {
-      if (!(mask & (1 << c))) continue;
-      int ref = childAt(ch, c);
-      if (ref == kEmptyChild) continue;
-      if (ref < 0) {
-        uint32_t v = ~(uint32_t)ref;
-        uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
-        if (first + cnt > (uint32_t)dom.num_tris) {
-          raise(ctr, kErrBadNode);
-          continue;
-        }
-        ntris += cnt;
-        for (uint32_t q = 0; q < cnt; ++q) {
-          const float4* tp = tris + 3 * (size_t)(first + q);
-          float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
-          float t, u, vv;
-          if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z),
-                                v3(cc.x, cc.y, cc.z), kRayEpsilon, tfar, &t, &u, &vv))
-            return true;
-        }
-      } else if (sp < kStack) {
-        stack[sp++] = ref;
-      }
+    ntris += cnt;
+    for (uint32_t q = 0; q < cnt; ++q) {
+      const float4* tp = tris + 3 * (size_t)(first + q);
+      const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+      float t, u, vv;
+      if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
+                            kRayEpsilon, tfar, &t, &u, &vv))
+        return true;
     }
-    if (sp == 0) return false;
-    node = stack[--sp];
+    cur = sp > 0 ? stack[--sp] : kDone;
   }
+  return false;
 }
 
 __device__ __forceinline__ int findKey(const uint32_t* ks, int nkeys, uint32_t e) {
