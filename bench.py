@@ -178,6 +178,9 @@ def main():
     ap.add_argument("--policy", default="plain", choices=list(POLICIES),
                     help="out-of-core domain order (plain: the reference's DomainStats order)")
     ap.add_argument("--ooc-batch", type=int, default=0, help="domains per batch under --policy batched")
+    ap.add_argument("--graphs", type=int, default=1, choices=[0, 1],
+                    help="1: replay the in-core frame as a captured CUDA graph; 0: direct launches "
+                         "(kernel profilers)")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide the image size (profiling captures on a small frame only)")
     args = ap.parse_args()
@@ -233,6 +236,7 @@ def main():
     if args.scale > 1:
         cfg["image_w"] = max(8, cfg["image_w"] // args.scale)
         cfg["image_h"] = max(8, cfg["image_h"] // args.scale)
+    cfg["graphs"] = args.graphs
     cfg["schedule_policy"] = POLICIES[args.policy][0]
     cfg["ooc_batch"] = args.ooc_batch
     if args.policy == "learned":

@@ -90,6 +90,29 @@ __device__ __forceinline__ void raise(Counters* ctr, unsigned long long bit) {
 
 // Marks the end of a traversal (never a child reference: empty slots are skipped).
 constexpr int kDone = (int)kEmptyChild;
+// Inner-node expansions a lane runs before its warp checks for idle lanes.
+constexpr int kNodeBudget = 8;
+
+// Traversal state of one (ray, domain) entry, kept across the rounds of the
+// persistent loop so that a lane can be refilled as soon as its entry ends.
+struct Walk {
+  const BvhNode4* nodes;
+  const float4* tris;
+  int num_nodes, num_tris;
+  int cur, sp, steps;
+};
+
+__device__ __forceinline__ Walk startWalk(const SceneDev& sc, const DomainDev& dom) {
+  Walk w;
+  w.nodes = sc.nodes + dom.node_base;
+  w.tris = sc.tris + 3 * (size_t)dom.tri_base;
+  w.num_nodes = dom.num_nodes;
+  w.num_tris = dom.num_tris;
+  w.cur = 0;
+  w.sp = 0;
+  w.steps = 0;
+  return w;
+}
 
 // Closest hit in one domain.  best_key enters as the key to beat and leaves as
 // the best found; returns true when this domain improved it.
@@ -188,60 +211,58 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
   return found;
 }
 
-// Any hit in (tnear, tfar) in one domain, with the same while-while loop.
-__device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar,
-                            Counters* ctr, unsigned long long& nnodes, unsigned long long& ntris) {
-  const BvhNode4* nodes = sc.nodes + dom.node_base;
-  const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
-  int stack[kStack];
-  int sp = 0;
-  int steps = 0;
-  int cur = 0;
-  while (cur != kDone) {
-    while (cur >= 0) {
-      if (++steps > kMaxSteps) {
-        raise(ctr, kErrTraversalBound);
-        return false;
-      }
-      if ((unsigned)cur >= (unsigned)dom.num_nodes) {
-        raise(ctr, kErrBadNode);
-        return false;
-      }
-      float tn[4];
-      ++nnodes;
-      const int mask = testChildren(nodes, cur, r, kRayEpsilon, tfar, tn);
-      const int4 ch = loadChildren(nodes, cur);
-      for (int c = 0; c < 4; ++c) {
-        if (!(mask & (1 << c))) continue;
-        const int ref = childAt(ch, c);
-        if (ref == kEmptyChild) continue;
-        if (sp == kStack) {
-          raise(ctr, kErrTraversalBound);
-          return false;
-        }
-        stack[sp++] = ref;
-      }
-      cur = sp > 0 ? stack[--sp] : kDone;
+// Any hit in (tnear, tfar), the same rounds.  Returns true when the walk has
+// ended; *hit tells whether it ended on a hit.
+__device__ __forceinline__ bool anyRound(Walk& w, int* stack, const TravRay& r, float tfar, bool* hit,
+                                         Counters* ctr, unsigned long long& nnodes,
+                                         unsigned long long& ntris) {
+  *hit = false;
+  for (int k = 0; w.cur >= 0; ++k) {
+    if (k == kNodeBudget) return false;
+    if (++w.steps > kMaxSteps) {
+      raise(ctr, kErrTraversalBound);
+      return true;
     }
-    if (cur == kDone) break;
-    const uint32_t v = ~(uint32_t)cur;
-    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
-    if (first + cnt > (uint32_t)dom.num_tris) {
+    if ((unsigned)w.cur >= (unsigned)w.num_nodes) {
       raise(ctr, kErrBadNode);
-      return false;
+      return true;
     }
-    ntris += cnt;
-    for (uint32_t q = 0; q < cnt; ++q) {
-      const float4* tp = tris + 3 * (size_t)(first + q);
-      const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
-      float t, u, vv;
-      if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
-                            kRayEpsilon, tfar, &t, &u, &vv))
+    float tn[4];
+    ++nnodes;
+    const int mask = testChildren(w.nodes, w.cur, r, kRayEpsilon, tfar, tn);
+    const int4 ch = loadChildren(w.nodes, w.cur);
+    for (int c = 0; c < 4; ++c) {
+      if (!(mask & (1 << c))) continue;
+      const int ref = childAt(ch, c);
+      if (ref == kEmptyChild) continue;
+      if (w.sp == kStack) {
+        raise(ctr, kErrTraversalBound);
         return true;
+      }
+      stack[w.sp++] = ref;
     }
-    cur = sp > 0 ? stack[--sp] : kDone;
+    w.cur = w.sp > 0 ? stack[--w.sp] : kDone;
   }
-  return false;
+  if (w.cur == kDone) return true;
+  const uint32_t v = ~(uint32_t)w.cur;
+  const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+  if (first + cnt > (uint32_t)w.num_tris) {
+    raise(ctr, kErrBadNode);
+    return true;
+  }
+  ntris += cnt;
+  for (uint32_t q = 0; q < cnt; ++q) {
+    const float4* tp = w.tris + 3 * (size_t)(first + q);
+    const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+    float t, u, vv;
+    if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
+                          kRayEpsilon, tfar, &t, &u, &vv)) {
+      *hit = true;
+      return true;
+    }
+  }
+  w.cur = w.sp > 0 ? stack[--w.sp] : kDone;
+  return w.cur == kDone;
 }
 
 __device__ __forceinline__ int findKey(const uint32_t* ks, int nkeys, uint32_t e) {
@@ -281,6 +302,14 @@ __device__ __forceinline__ uint32_t entryOf(const TraceArgs& a, const uint32_t* 
 
 }  // namespace
 
+__device__ __forceinline__ uint32_t lanesBelow() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Closest hits: warps take 32 consecutive entries at a time, so the lanes of a
+// warp walk coherent rays (consecutive samples of the same domain queue).
 __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
@@ -379,6 +408,11 @@ void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nbloc
   kResolve<<<nblocks, 256, 0, s>>>(a, hit_ns);
 }
 
+// Occlusion with persistent, refilling warps: each round, the lanes whose
+// entry has ended take the next entries (one warp-aggregated atomic), then
+// every busy lane advances its walk by one while-while round.  Any-hit walks
+// end early and unevenly, so refilling keeps lanes busy; closest-hit walks do
+// better with the coherence of consecutive entries.
 __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
@@ -387,25 +421,47 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(Tr
   loadTables(a, skeys, sbeg, spre);
   const uint32_t E = a.nseg > 0 ? spre[a.nseg] : *a.num_entries;
   const int lane = threadIdx.x & 31;
+  const uint32_t below = lanesBelow();
   unsigned long long visits = 0, nnodes = 0, ntris = 0;
+  int stack[kStack];
+  Walk w{};
+  TravRay r{};
+  float tfar = 0.0f;
+  uint32_t ray = 0;
+  bool has = false, exhausted = false;
   while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(a.work, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= E) break;
-    const uint32_t w = base + lane;
-    if (w >= E) continue;
-    const uint32_t e = entryOf(a, sbeg, spre, w);
-    const uint2 ent = a.entries[e];
-    const uint32_t ray = ent.x & kRayIdMask;
-    if (*((volatile uint8_t*)&a.sh.occluded[ray])) continue;
-    const int d = findKey(skeys, a.nkeys, e) % D;
-    const DomainDev dom = a.scene.domains[d];
-    ++visits;
-    const float4 hp = a.sh.hitpos[ray / a.slots];
-    const float4 dd = a.sh.dir[ray];
-    TravRay r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
-    if (traverseAny(a.scene, dom, r, dd.w, a.ctr, nnodes, ntris)) a.sh.occluded[ray] = 1;
+    const unsigned idle = __ballot_sync(0xffffffffu, !has);
+    if (idle && !exhausted) {
+      const uint32_t need = __popc(idle);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(a.work, need);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + need >= E) exhausted = true;
+      const uint32_t wi = base + __popc(idle & below);
+      if (!has && wi < E) {
+        const uint32_t e = entryOf(a, sbeg, spre, wi);
+        ray = a.entries[e].x & kRayIdMask;
+        if (!*((volatile uint8_t*)&a.sh.occluded[ray])) {
+          const int d = findKey(skeys, a.nkeys, e) % D;
+          ++visits;
+          const float4 hp = a.sh.hitpos[ray / a.slots];
+          const float4 dd = a.sh.dir[ray];
+          r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
+          tfar = dd.w;
+          w = startWalk(a.scene, a.scene.domains[d]);
+          has = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, has)) {
+      if (exhausted) break;
+      continue;
+    }
+    bool hit = false;
+    if (has && anyRound(w, stack, r, tfar, &hit, a.ctr, nnodes, ntris)) {
+      has = false;
+      if (hit) a.sh.occluded[ray] = 1;
+    }
   }
   for (int o = 16; o; o >>= 1) {
     visits += __shfl_down_sync(0xffffffffu, visits, o);
