@@ -178,6 +178,9 @@ def main():
     ap.add_argument("--policy", default="plain", choices=list(POLICIES),
                     help="out-of-core domain order (plain: the reference's DomainStats order)")
     ap.add_argument("--ooc-batch", type=int, default=0, help="domains per batch under --policy batched")
+    ap.add_argument("--ooc-inplace", type=int, default=16384,
+                    help="trace a non-resident domain in place from host memory when a batch holds at "
+                         "most this many of its live entries (batched and learned policies)")
     ap.add_argument("--graphs", type=int, default=1, choices=[0, 1],
                     help="1: replay the in-core frame as a captured CUDA graph; 0: direct launches "
                          "(kernel profilers)")
@@ -239,6 +242,7 @@ def main():
     cfg["graphs"] = args.graphs
     cfg["schedule_policy"] = POLICIES[args.policy][0]
     cfg["ooc_batch"] = args.ooc_batch
+    cfg["ooc_inplace"] = args.ooc_inplace
     if args.policy == "learned":
         cfg["learn_frames"] = 1  # collect during the first warm-up frame, train after it
     tracer = sg.Tracer(cfg, device=local)
@@ -334,6 +338,7 @@ def main():
         "visits_per_ray": (s0["visits_radiance"] + s0["visits_shadow"]) / max(nrays, 1),
         "visits_culled": s0["visits_culled"],
         "domain_loads_per_frame": s0["domain_loads"],
+        "inplace_domains_per_frame": s0["inplace_domains"],
         "breakdown_ms_per_frame": {k: s0[f"{k}_ms"] for k in ("frame", "schedule", "trace", "occlude", "h2d")},
         "h2d_bytes_per_frame": s0["h2d_bytes"],
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),

@@ -94,6 +94,10 @@ typedef struct spray_gpu_config {
                                    were collected (4) */
   int32_t graphs;               /* in core: capture the frame's launches once into a CUDA graph and
                                    replay it while the buffers stay the same (1) */
+  int32_t ooc_inplace;          /* out-of-core, policies 2 and 3: a domain that is not resident and
+                                   has at most this many live entries in a batch is traced in place
+                                   from pinned host memory (read over the host link) instead of
+                                   being copied into the cache; 0 = always copy (16384) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as
@@ -154,6 +158,7 @@ typedef struct spray_gpu_stats {
   int64_t learn_trained;    /* policy 3: 1 once the proposal has been trained */
   double learn_ms;          /* policy 3: device time spent training after this frame */
   double learn_loss;        /* policy 3: mean loss of the last training batch */
+  int64_t inplace_domains;  /* out of core: (domain, batch) pairs traced in place from host memory */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

@@ -41,7 +41,7 @@ class ConfigC(C.Structure):
         ("schedule_policy", C.c_int32),
         ("ooc_batch", C.c_int32), ("learn_samples", C.c_int64), ("learn_batch", C.c_int32),
         ("learn_epochs", C.c_int32), ("learn_lr", C.c_float), ("learn_seed", C.c_int32),
-        ("learn_frames", C.c_int32), ("graphs", C.c_int32),
+        ("learn_frames", C.c_int32), ("graphs", C.c_int32), ("ooc_inplace", C.c_int32),
     ]
 
 
@@ -69,7 +69,7 @@ class StatsC(C.Structure):
         ("nodes_radiance", C.c_int64), ("tris_radiance", C.c_int64), ("nodes_shadow", C.c_int64),
         ("tris_shadow", C.c_int64), ("scene_triangles", C.c_int64), ("scene_bytes", C.c_int64),
         ("h2d_ms", C.c_double), ("learn_pairs", C.c_int64), ("learn_trained", C.c_int64),
-        ("learn_ms", C.c_double), ("learn_loss", C.c_double),
+        ("learn_ms", C.c_double), ("learn_loss", C.c_double), ("inplace_domains", C.c_int64),
     ]
 
     def asdict(self) -> dict:

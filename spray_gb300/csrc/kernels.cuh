@@ -42,9 +42,17 @@ struct DomainDev {
   int32_t face_base;       // first index triple (original face order)
   int32_t bsdf;
   float bsdf_p[3];
-  int32_t resident;        // 1 when the geometry is in device memory
+  int32_t resident;        // 1: geometry in a device slot (the *_base offsets); 2: traced in
+                           // place from pinned host memory (the src_* pointers); 0: neither
   int32_t num_nodes;       // BVH nodes of the domain
   int32_t num_tris;        // triangles of the domain
+  // out of core: the domain's arrays in mapped pinned host memory, read over
+  // the host link when the domain is traced in place
+  const BvhNode4* src_nodes;
+  const float4* src_tris;
+  const uint32_t* src_faces;
+  const uint32_t* src_colors;
+  const float* src_normals;
 };
 
 // Bits of Counters::error_flags.
@@ -61,6 +69,33 @@ struct SceneDev {
   const uint32_t* colors;   // per vertex
   const float* normals;     // 3 per vertex
 };
+
+// A domain's geometry, wherever it is: its device slot, or pinned host memory.
+struct DomArrays {
+  const BvhNode4* nodes;
+  const float4* tris;        // 3 per triangle, leaf order
+  const uint32_t* faces;     // 3 per face, original order; indices into colors / normals
+  const uint32_t* colors;
+  const float* normals;      // 3 per vertex
+};
+
+__device__ __forceinline__ DomArrays domArrays(const SceneDev& sc, const DomainDev& d) {
+  DomArrays a;
+  if (d.resident == 2) {
+    a.nodes = d.src_nodes;
+    a.tris = d.src_tris;
+    a.faces = d.src_faces;
+    a.colors = d.src_colors;
+    a.normals = d.src_normals;
+  } else {
+    a.nodes = sc.nodes + d.node_base;
+    a.tris = sc.tris + 3 * (size_t)d.tri_base;
+    a.faces = sc.faces + 3 * (size_t)d.face_base;
+    a.colors = sc.colors + d.vert_base;
+    a.normals = sc.normals + 3 * (size_t)d.vert_base;
+  }
+  return a;
+}
 
 struct Counters {
   unsigned long long rays_primary;

@@ -104,8 +104,9 @@ struct Walk {
 
 __device__ __forceinline__ Walk startWalk(const SceneDev& sc, const DomainDev& dom) {
   Walk w;
-  w.nodes = sc.nodes + dom.node_base;
-  w.tris = sc.tris + 3 * (size_t)dom.tri_base;
+  const DomArrays g = domArrays(sc, dom);
+  w.nodes = g.nodes;
+  w.tris = g.tris;
   w.num_nodes = dom.num_nodes;
   w.num_tris = dom.num_tris;
   w.cur = 0;
@@ -129,8 +130,9 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
                                 uint64_t& best_key, float& best_t, uint32_t& best_prim,
                                 float& best_u, float& best_v, Counters* ctr,
                                 unsigned long long& nnodes, unsigned long long& ntris) {
-  const BvhNode4* nodes = sc.nodes + dom.node_base;
-  const float4* tris = sc.tris + 3 * (size_t)dom.tri_base;
+  const DomArrays g = domArrays(sc, dom);
+  const BvhNode4* nodes = g.nodes;
+  const float4* tris = g.tris;
   uint2 stack[kStack];
   int sp = 0;
   bool found = false;
@@ -359,10 +361,11 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
     float u = 0.f, v = 0.f;
     if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v, a.ctr, nnodes, ntris)) {
       atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
-      const uint32_t* f = a.scene.faces + 3 * ((size_t)dom.face_base + prim);
-      uint32_t i0 = dom.vert_base + f[0], i1 = dom.vert_base + f[1], i2 = dom.vert_base + f[2];
-      uint32_t col = interpolateColor(a.scene.colors[i0], a.scene.colors[i1], a.scene.colors[i2], u, v);
-      const float* nb = a.scene.normals;
+      const DomArrays g = domArrays(a.scene, dom);
+      const uint32_t* f = g.faces + 3 * (size_t)prim;
+      const uint32_t i0 = f[0], i1 = f[1], i2 = f[2];
+      uint32_t col = interpolateColor(g.colors[i0], g.colors[i1], g.colors[i2], u, v);
+      const float* nb = g.normals;
       V3 ns = interpolateNormal(v3(nb[3 * (size_t)i0], nb[3 * (size_t)i0 + 1], nb[3 * (size_t)i0 + 2]),
                                 v3(nb[3 * (size_t)i1], nb[3 * (size_t)i1 + 1], nb[3 * (size_t)i1 + 2]),
                                 v3(nb[3 * (size_t)i2], nb[3 * (size_t)i2 + 1], nb[3 * (size_t)i2 + 2]),

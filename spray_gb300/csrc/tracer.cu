@@ -148,6 +148,7 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
         "learned proposal needs learn_samples >= 0, learn_batch > 0, learn_epochs >= 0, learn_lr > 0, "
         "learn_frames >= 1");
   if (cfg.ooc_batch < 0) throw std::invalid_argument("ooc_batch must be >= 0");
+  if (cfg.ooc_inplace < 0) throw std::invalid_argument("ooc_inplace must be >= 0");
   int ndev = 0;
   CK(cudaGetDeviceCount(&ndev));
   if (cfg.device < 0 || cfg.device >= ndev) throw CudaError("no CUDA device " + std::to_string(cfg.device));
@@ -444,21 +445,27 @@ void Tracer::setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t
              p.colors.size() * 4 + p.normals.size() * 4;
     total = (total + 255) & ~(size_t)255;
   }
-  CK(cudaHostAlloc((void**)&h_pinned, std::max<size_t>(total, 256), cudaHostAllocDefault));
+  // mapped, so that a domain can also be traced in place over the host link
+  CK(cudaHostAlloc((void**)&h_pinned, std::max<size_t>(total, 256), cudaHostAllocMapped));
+  char* dev_pinned = nullptr;
+  CK(cudaHostGetDevicePointer((void**)&dev_pinned, h_pinned, 0));
   for (int d = 0; d < D; ++d) {
     const DomainPack& p = packs[d];
     char* q = h_pinned + host_off[d];
+    DomainDev& dd = hdoms[d];
     auto put = [&](const void* src, size_t n) {
+      const char* at = dev_pinned + (q - h_pinned);
       std::memcpy(q, src, n);
       q += n;
+      return at;
     };
-    put(p.nodes.data(), p.nodes.size() * sizeof(BvhNode4));
-    put(p.tris.data(), p.tris.size() * sizeof(float4));
-    put(p.faces.data(), p.faces.size() * 4);
-    put(p.colors.data(), p.colors.size() * 4);
-    put(p.normals.data(), p.normals.size() * 4);
-    hdoms[d].resident = 0;
-    hdoms[d].node_base = hdoms[d].tri_base = hdoms[d].vert_base = hdoms[d].face_base = 0;
+    dd.src_nodes = reinterpret_cast<const BvhNode4*>(put(p.nodes.data(), p.nodes.size() * sizeof(BvhNode4)));
+    dd.src_tris = reinterpret_cast<const float4*>(put(p.tris.data(), p.tris.size() * sizeof(float4)));
+    dd.src_faces = reinterpret_cast<const uint32_t*>(put(p.faces.data(), p.faces.size() * 4));
+    dd.src_colors = reinterpret_cast<const uint32_t*>(put(p.colors.data(), p.colors.size() * 4));
+    dd.src_normals = reinterpret_cast<const float*>(put(p.normals.data(), p.normals.size() * 4));
+    dd.resident = 0;
+    dd.node_base = dd.tri_base = dd.vert_base = dd.face_base = 0;
   }
   devAlloc(&d_domains, D);
   devAlloc(&d_nodes, (size_t)capacity * max_nodes);
@@ -1026,6 +1033,9 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
   // the running trace reads (and the batch before it has finished)
   const int half = std::max(1, cache_capacity / 2);
   const int B = std::min(cfg.ooc_batch > 0 ? cfg.ooc_batch : half, half);
+  // domains whose live entries are counted before a batch is chosen: enough to
+  // fill it after drops; with in-place tracing every remaining domain may join
+  const int window_n = cfg.ooc_inplace > 0 ? D : 2 * B;
   int32_t* hdoms_list = reinterpret_cast<int32_t*>(h_live);
   uint32_t* hlive = h_live + D;
   // live counts of `doms`, written to hlive when `done` has completed
@@ -1055,17 +1065,30 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
   };
   // the next batch: the first B domains of `remaining` with live entries; the
   // rest stay in `remaining`, domains without live entries are dropped
+  // traced in place: not resident, and few live entries (by the counts in hlive)
+  auto inPlace = [&](int d) {
+    return hdoms[d].resident != 1 && cfg.ooc_inplace > 0 &&
+           (uint64_t)(with_r ? hlive[d] : 0) + (with_s ? hlive[D + d] : 0) <= (uint64_t)cfg.ooc_inplace;
+  };
+  // B bounds the domains that go through the cache (resident or copied); those
+  // traced in place take no slot and join the batch freely
   auto select = [&](std::vector<int>& remaining, std::vector<int>& batch) {
     std::vector<int> rest;
     batch.clear();
-    const size_t counted_n = std::min(remaining.size(), (size_t)2 * B);
+    int cached = 0;
+    const size_t counted_n = std::min(remaining.size(), (size_t)window_n);
     for (size_t k = 0; k < remaining.size(); ++k) {
       const int d = remaining[k];
       if (k < counted_n) {
         const bool lr = with_r && hlive[d] > 0, ls = with_s && hlive[D + d] > 0;
         if (!lr && !ls) continue;  // nothing left to trace here: not loaded
-        if ((int)batch.size() < B) {
+        if (inPlace(d)) {
           batch.push_back(d);
+          continue;
+        }
+        if (cached < B) {
+          batch.push_back(d);
+          ++cached;
           continue;
         }
       }
@@ -1073,10 +1096,19 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
     }
     remaining.swap(rest);
   };
+  // a domain that is not resident and has at most ooc_inplace live entries in
+  // this batch is traced in place from pinned host memory instead of copied
+  std::vector<int> inplace;
   auto issueLoads = [&](const std::vector<int>& batch, cudaEvent_t loaded) {
     cudaEvent_t c0 = poolEvent();
     CK(cudaEventRecord(c0, cstream));
+    inplace.clear();
     for (int d : batch) {
+      if (inPlace(d)) {
+        hdoms[d].resident = 2;
+        inplace.push_back(d);
+        continue;
+      }
       int slot, evicted;
       if (!lru.load(d, &slot, &evicted)) {
         if (evicted >= 0) hdoms[evicted].resident = 0;
@@ -1089,7 +1121,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
   // live counts cover a window of the next 2 B remaining domains: enough to
   // fill a batch after drops, and each domain is counted about once
   auto window = [&](const std::vector<int>& rem) {
-    return std::vector<int>(rem.begin(), rem.begin() + std::min(rem.size(), (size_t)2 * B));
+    return std::vector<int>(rem.begin(), rem.begin() + std::min(rem.size(), (size_t)window_n));
   };
   // after a count: select, and while a whole window was dropped, count on
   auto nextBatch = [&](std::vector<int>& batch) {
@@ -1113,6 +1145,9 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
     // domain table, then segment tables: radiance bucket 0..rb-1, shadows
     DomainDev* sd = reinterpret_cast<DomainDev*>(h_stage);
     std::memcpy(sd, hdoms.data(), D * sizeof(DomainDev));
+    // the device table of this batch marks them in place; later batches decide anew
+    inplace_domains += (int64_t)inplace.size();
+    for (int d : inplace) hdoms[d].resident = 0;
     uint32_t* seg = reinterpret_cast<uint32_t*>(h_stage + D * sizeof(DomainDev));
     std::vector<int> nseg(rb + 1, 0);
     for (int q = 0; q <= rb; ++q) {
@@ -1530,6 +1565,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     h2d_bytes = 0;
     d2h_bytes = 0;
     domain_loads = 0;
+    inplace_domains = 0;
     ev_used = 0;
     sched_events.clear();
     trace_events.clear();
@@ -1630,6 +1666,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->learn_trained = proposal_trained ? 1 : 0;
       st->learn_ms = learn_ms;
       st->learn_loss = learn_loss;
+      st->inplace_domains = inplace_domains;
     }
     return;
   }
@@ -1844,6 +1881,7 @@ void spray_gpu_config_defaults(spray_gpu_config* c) {
   c->learn_seed = 1;
   c->learn_frames = 4;
   c->graphs = 1;
+  c->ooc_inplace = 16384;
 }
 
 const char* spray_gpu_last_error(void) { return spray::g_last_error.c_str(); }

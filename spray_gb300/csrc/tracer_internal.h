@@ -244,6 +244,7 @@ class Tracer {
   // frame accounting
   int64_t launches = 0;
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
+  int64_t inplace_domains = 0;  // (domain, batch) pairs traced in place this frame
   std::map<std::pair<int, int>, std::vector<char>> dbg;
 };
 

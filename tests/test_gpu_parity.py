@@ -304,10 +304,13 @@ def test_scene_file_path(lib_built, oracle_mod, tmp_path):
 
 @pytest.mark.parametrize("kw", [dict(cache_size=16), dict(cache_size=5), dict(cache_bytes=3 << 20),
                                 dict(cache_size=16, schedule_policy=1),
-                                dict(cache_size=16, schedule_policy=2),
-                                dict(cache_size=5, schedule_policy=2, ooc_batch=1),
-                                dict(cache_size=1, schedule_policy=2),
-                                dict(cache_bytes=3 << 20, schedule_policy=2, ooc_batch=3)])
+                                dict(cache_size=16, schedule_policy=2, ooc_inplace=0),
+                                dict(cache_size=5, schedule_policy=2, ooc_batch=1, ooc_inplace=0),
+                                dict(cache_size=1, schedule_policy=2, ooc_inplace=0),
+                                dict(cache_bytes=3 << 20, schedule_policy=2, ooc_batch=3, ooc_inplace=0),
+                                dict(cache_size=16, schedule_policy=2, ooc_inplace=200),
+                                dict(cache_size=16, schedule_policy=2, ooc_inplace=1 << 30),
+                                dict(cache_size=16, schedule_policy=2)])
 def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     """Streaming domains through a small LRU cache changes loads, never the image."""
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
@@ -322,7 +325,15 @@ def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     t.set_camera(*cam)
     got, st = t.trace()
     assert np.array_equal(bits(got), bits(want))
-    assert st["domain_loads"] > 0 and st["h2d_bytes"] > 0
+    inplace = kw.get("ooc_inplace", 16384) if kw.get("schedule_policy", 0) >= 2 else 0
+    if inplace >= 1 << 30:
+        assert st["domain_loads"] == 0 and st["inplace_domains"] > 0  # every domain read in place
+    elif inplace == 0:
+        assert st["domain_loads"] > 0 and st["h2d_bytes"] > 0 and st["inplace_domains"] == 0
+    else:
+        assert st["domain_loads"] + st["inplace_domains"] > 0
+    if 0 < inplace < 1 << 30 and "ooc_inplace" in kw:
+        assert st["inplace_domains"] > 0 and st["domain_loads"] > 0
     assert st["rays_shadow"] == st0["rays_shadow"] and st["visits_radiance"] >= st0["visits_radiance"] - st0["visits_culled"]
     got2, st2 = t.trace()  # the cache stays warm across frames
     assert np.array_equal(bits(got2), bits(want))
@@ -345,7 +356,7 @@ def test_cache_aware_order_needs_fewer_loads(lib_built, scene64):
     cam = scenes.orbit_camera(scene64)
     loads = []
     for pol in (0, 1, 2):
-        t = sg.Tracer(cfg, schedule_policy=pol)
+        t = sg.Tracer(cfg, schedule_policy=pol, ooc_inplace=0)
         t.set_scene(scene64)
         t.set_camera(*cam)
         t.trace()
@@ -362,7 +373,7 @@ def test_batched_pass_skips_fully_culled_domains(lib_built, scene64):
     cam = scenes.orbit_camera(scene64)
     out = {}
     for pol, batch in ((0, 0), (2, 2)):
-        t = sg.Tracer(cfg, schedule_policy=pol, ooc_batch=batch)
+        t = sg.Tracer(cfg, schedule_policy=pol, ooc_batch=batch, ooc_inplace=0)
         t.set_scene(scene64)
         t.set_camera(*cam)
         out[pol] = t.trace()
@@ -406,7 +417,7 @@ def test_trained_proposal_gains_over_untrained(lib_built):
     the same method with the untrained (randomly initialised) network."""
     scene = scenes.wavelet_grid(4, 32, colors="albedo", light="quad")
     cfg = small_config(image_w=320, image_h=240, ao_mode=0, pixel_samples=4, bounces=4, rr_depth=3,
-                       cache_size=16)
+                       cache_size=16, ooc_inplace=0)
     cam = scenes.orbit_camera(scene)
     out = {}
     for name, epochs in (("untrained", 0), ("trained", 8)):
