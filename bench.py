@@ -99,7 +99,7 @@ def hbm_peak():
 
 
 def load_profile_traffic(name: str):
-    """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu summary."""
+    """DRAM bytes per algorithmic byte of the closest-hit kernel, from the committed ncu summary."""
     p = ROOT / "profiles" / f"trace_closest_{name}.json"
     try:
         d = json.loads(p.read_text())
@@ -317,8 +317,9 @@ def main():
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
     prof = load_profile_traffic(args.config)
     traffic = None
-    if prof and prof.get("kernel") == kname:
-        traffic = prof.get("dram_bytes_per_frame")
+    if prof and prof.get("kernel") == kname and "dram_bytes_per_algorithmic_byte" in prof:
+        # ncu DRAM bytes of a small frame, scaled by the units processed
+        traffic = prof["dram_bytes_per_algorithmic_byte"] * kbytes
 
     nrays = s0["rays_primary"] + s0["rays_shadow"] + s0["rays_bounce"]
     out = {
