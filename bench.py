@@ -37,7 +37,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mrays/s at <=1e-3 image RMSE, learned vs plain scheduler; domain loads/frame"
 POLICIES = {"plain": (0, "plain speculative"), "resident": (1, "resident domains first"),
             "batched": (2, "batched passes (shadow b + radiance b+1), culled domains not loaded"),
-            "learned": (3, "learned domain-order proposal (online-trained MLP) + batched passes")}
+            "learned": (3, "learned domain-order proposal (online-trained MLP) + batched passes"),
+            "nonspec": (4, "non-speculative LoadAnyOnce: one pass per list position, most pending rays first")}
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24

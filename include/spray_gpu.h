@@ -81,7 +81,11 @@ typedef struct spray_gpu_config {
                                    (ray, winning domain) pairs) orders the work: in core, each
                                    ray's entries up to its predicted domain are traced first and
                                    the later ones front to back; out of core, domains holding
-                                   more predicted hits go first.  Images are unchanged (0) */
+                                   more predicted hits go first; 4 non-speculative: the
+                                   LoadAnyOnce baseline (src/baseline/baseline_schedulers.cc) --
+                                   one pass per list position, a ray waits only in the queue of its
+                                   next domain, domains with the most pending rays first.  Images
+                                   are unchanged (0) */
   int32_t ooc_batch;            /* out-of-core, policy 2: domains made resident per traced batch,
                                    at most half the cache capacity so that the next batch's copies
                                    overlap this batch's traces; 0 = half the capacity (0) */
@@ -173,6 +177,18 @@ int spray_gpu_destroy(spray_gpu_tracer* t);
  * each domain's BVH and uploads every domain when the cache holds them all. */
 int spray_gpu_set_scene(spray_gpu_tracer* t, const spray_gpu_domain* domains, int32_t num_domains,
                         const spray_gpu_light* lights, int32_t num_lights);
+
+/* Prepared-domain blobs (the on-disk side of the out-of-core path): what
+ * set_scene builds per domain -- vertex normals (TriMeshBuffer::computeNormals,
+ * src/render/trimesh_buffer.cc:267-326), the BVH and the leaf-ordered
+ * triangles that replace SpRay's per-load PLY parse and Embree build
+ * (TriMeshBuffer::load, trimesh_buffer.cc:117-169) -- written once, one file
+ * `dir/domain_NNNNN.sdom` per domain.  spray_scene_prepare needs no GPU. */
+int spray_scene_prepare(const spray_gpu_domain* domains, int32_t num_domains, const char* dir);
+/* set_scene from blobs in `dir` (domains 0..num_domains-1): no normal or BVH
+ * build; SPRAY_GPU_EIO for a missing, truncated or foreign file. */
+int spray_gpu_set_scene_prepared(spray_gpu_tracer* t, const char* dir, int32_t num_domains,
+                                 const spray_gpu_light* lights, int32_t num_lights);
 
 /* Camera::init (src/render/camera.h:128-166); vfov in degrees. */
 int spray_gpu_set_camera(spray_gpu_tracer* t, const float pos[3], const float lookat[3],

@@ -131,6 +131,8 @@ def lib() -> C.CDLL:
                                              P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.spray_gpu_schedule_static.argtypes = [P, C.c_int32, P, P, C.c_int32, C.c_int32, P, C.c_int64, P,
                                                 C.POINTER(C.c_int64), P]
+        L.spray_scene_prepare.argtypes = [C.POINTER(DomainC), C.c_int32, C.c_char_p]
+        L.spray_gpu_set_scene_prepared.argtypes = [P, C.c_char_p, C.c_int32, C.POINTER(LightC), C.c_int32]
         F4 = C.POINTER(C.c_float)
         L.spray_mlp_param_count.restype = C.c_int32
         L.spray_mlp_forward_dev.argtypes = [P, P, F4, P, C.c_int64, P, P, C.c_int32]
@@ -288,6 +290,12 @@ class Tracer:
         self._scene_ref = scene
         _check(lib().spray_gpu_set_scene(self._h, doms, len(scene.domains), lts, len(scene.lights)))
 
+    def set_scene_prepared(self, directory, num_domains: int, lights=()) -> None:
+        """set_scene from prepared-domain blobs (see prepare_scene)."""
+        lts = Scene([], list(lights)).light_structs()
+        _check(lib().spray_gpu_set_scene_prepared(self._h, str(directory).encode(), num_domains, lts,
+                                                  len(lights)))
+
     def set_camera(self, pos, lookat, up=(0, 1, 0), vfov=None) -> None:
         f3 = lambda x: (C.c_float * 3)(*[float(v) for v in x])
         fov = self.config["fov"] if vfov is None else vfov
@@ -330,6 +338,13 @@ def schedule_static(domain_bounds_ptr: int, num_domains: int, org_ptr: int, dir_
                                            C.c_void_p(domain_start_ptr), C.byref(n),
                                            C.c_void_p(stream) if stream else None))
     return n.value
+
+
+def prepare_scene(scene: "Scene", directory) -> None:
+    """Writes one prepared-domain blob per domain (normals, BVH, leaf-ordered
+    triangles) into `directory`; needs no GPU."""
+    Path(directory).mkdir(parents=True, exist_ok=True)
+    _check(lib().spray_scene_prepare(scene.domain_structs(), len(scene.domains), str(directory).encode()))
 
 
 # spray_mlp_sample

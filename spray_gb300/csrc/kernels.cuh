@@ -277,8 +277,8 @@ void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int lis
 // radiance entries and live[D + d] shadow entries.  Either queue may be null.
 struct LiveArgs {
   const uint2* rentries;
-  const uint32_t* rkey_start;  // [rbuckets * D + 1]: key = bucket * D + domain
-  int rbuckets;
+  const uint32_t* rkey_start;  // key = bucket * D + domain
+  int rbucket0, rbuckets;      // the radiance buckets counted: [rbucket0, rbucket0 + rbuckets)
   const uint64_t* ray_key;
   uint64_t* rec_key;
   const uint2* sentries;

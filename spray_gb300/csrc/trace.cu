@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(256) kCountLive(LiveArgs a) {
   __shared__ uint32_t wsum[2][8];
   const int d = a.domains[blockIdx.x];
   uint32_t nr = 0, ns = 0;
-  for (int b = 0; a.rentries && b < a.rbuckets; ++b) {
+  for (int b = a.rbucket0; a.rentries && b < a.rbucket0 + a.rbuckets; ++b) {
     const uint32_t e0 = a.rkey_start[b * a.D + d], e1 = a.rkey_start[b * a.D + d + 1];
     for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
       const uint2 ent = a.rentries[e];

@@ -128,6 +128,180 @@ CameraDev makeCamera(const float p[3], const float l[3], const float up[3], floa
   return c;
 }
 
+// ---------------------------------------------------------------- domain preparation
+void buildPack(const spray_gpu_domain& src, int d, DomainPack& p) {
+  if (src.num_faces <= 0 || src.num_vertices <= 0 || !src.vertices || !src.faces)
+    throw std::invalid_argument("domain " + std::to_string(d) + " has no geometry");
+  if (src.num_faces >= (1ll << 28)) throw std::invalid_argument("domain too large");
+  for (int64_t i = 0; i < 3 * src.num_faces; ++i)
+    if ((int64_t)src.faces[i] >= src.num_vertices)
+      throw std::invalid_argument("domain " + std::to_string(d) + ": face index out of range");
+  p.nv = src.num_vertices;
+  p.nf = src.num_faces;
+  p.normals.resize(3 * (size_t)p.nv);
+  computeVertexNormals(src.vertices, p.nv, src.faces, p.nf, p.normals.data());
+  BvhBuildResult bvh;
+  buildBvh4(src.vertices, src.faces, (uint32_t)p.nf, &bvh);
+  p.nodes = std::move(bvh.nodes);
+  p.bvh_depth = bvh.depth;
+  p.tris.resize(3 * (size_t)p.nf);
+  for (size_t k = 0; k < bvh.tri_order.size(); ++k) {
+    uint32_t prim = bvh.tri_order[k];
+    const uint32_t* fi = src.faces + 3 * (size_t)prim;
+    for (int c = 0; c < 3; ++c) {
+      const float* vp = src.vertices + 3 * (size_t)fi[c];
+      float w = 0.f;
+      if (c == 0) std::memcpy(&w, &prim, 4);
+      p.tris[3 * k + c] = make_float4(vp[0], vp[1], vp[2], w);
+    }
+  }
+  p.faces.assign(src.faces, src.faces + 3 * p.nf);
+  if (src.colors) p.colors.assign(src.colors, src.colors + p.nv);
+  else p.colors.assign(p.nv, 0u);
+  for (int c = 0; c < 6; ++c) p.bounds[c] = src.world_bounds[c];
+  p.bsdf = src.bsdf_type;
+  for (int c = 0; c < 3; ++c) p.bsdf_p[c] = src.bsdf_params[c];
+}
+
+// Blob layout (little-endian, version 1): a 128-byte header, then the arrays
+// at the 256-byte-aligned offsets it records: BVH nodes (128 B each),
+// leaf-ordered triangles (3 float4 each), faces (3 uint32 each), colours (one
+// uint32 per vertex), normals (3 floats per vertex).
+namespace {
+struct BlobHeader {
+  char magic[8];
+  uint32_t version;
+  int32_t bsdf_type;
+  float world_bounds[6];
+  float bsdf_params[3];
+  int32_t bvh_depth;
+  int64_t num_vertices, num_faces, num_nodes;
+  uint64_t off_nodes, off_tris, off_faces, off_colors, off_normals, file_bytes;
+};
+static_assert(sizeof(BlobHeader) <= 128, "blob header");
+constexpr char kBlobMagic[8] = {'S', 'P', 'R', 'A', 'Y', 'D', 'O', 'M'};
+
+uint64_t align256(uint64_t x) { return (x + 255) & ~(uint64_t)255; }
+}  // namespace
+
+std::string domainBlobPath(const std::string& dir, int d) {
+  char name[32];
+  std::snprintf(name, sizeof(name), "domain_%05d.sdom", d);
+  return dir + "/" + name;
+}
+
+void writeDomainBlob(const std::string& path, const DomainPack& p) {
+  BlobHeader h{};
+  std::memcpy(h.magic, kBlobMagic, 8);
+  h.version = 1;
+  h.bsdf_type = p.bsdf;
+  for (int c = 0; c < 6; ++c) h.world_bounds[c] = p.bounds[c];
+  for (int c = 0; c < 3; ++c) h.bsdf_params[c] = p.bsdf_p[c];
+  h.bvh_depth = p.bvh_depth;
+  h.num_vertices = p.nv;
+  h.num_faces = p.nf;
+  h.num_nodes = (int64_t)p.nodes.size();
+  uint64_t at = 256;
+  h.off_nodes = at;
+  at = align256(at + p.nodes.size() * sizeof(BvhNode4));
+  h.off_tris = at;
+  at = align256(at + p.tris.size() * sizeof(float4));
+  h.off_faces = at;
+  at = align256(at + p.faces.size() * 4);
+  h.off_colors = at;
+  at = align256(at + p.colors.size() * 4);
+  h.off_normals = at;
+  at += p.normals.size() * 4;
+  h.file_bytes = at;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw IoError("cannot write " + path);
+  bool ok = true;
+  auto put = [&](uint64_t off, const void* src, size_t n) {
+    ok = ok && std::fseek(f, (long)off, SEEK_SET) == 0 && (n == 0 || std::fwrite(src, 1, n, f) == n);
+  };
+  unsigned char head[256] = {0};
+  std::memcpy(head, &h, sizeof(h));
+  put(0, head, sizeof(head));
+  put(h.off_nodes, p.nodes.data(), p.nodes.size() * sizeof(BvhNode4));
+  put(h.off_tris, p.tris.data(), p.tris.size() * sizeof(float4));
+  put(h.off_faces, p.faces.data(), p.faces.size() * 4);
+  put(h.off_colors, p.colors.data(), p.colors.size() * 4);
+  put(h.off_normals, p.normals.data(), p.normals.size() * 4);
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) throw IoError("short write to " + path);
+}
+
+void readDomainBlob(const std::string& path, DomainPack* p) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) throw IoError("cannot open " + path);
+  BlobHeader h{};
+  bool ok = std::fread(&h, 1, sizeof(h), f) == sizeof(h);
+  std::fseek(f, 0, SEEK_END);
+  const long size = std::ftell(f);
+  auto fail_io = [&](const std::string& why) {
+    std::fclose(f);
+    throw IoError(path + ": " + why);
+  };
+  if (!ok || std::memcmp(h.magic, kBlobMagic, 8) != 0) fail_io("not a prepared-domain blob");
+  if (h.version != 1) fail_io("unsupported blob version " + std::to_string(h.version));
+  if (h.num_vertices <= 0 || h.num_faces <= 0 || h.num_faces >= (1ll << 28) || h.num_nodes <= 0 ||
+      h.num_nodes >= (1ll << 31))
+    fail_io("bad counts");
+  const uint64_t nv = (uint64_t)h.num_vertices, nf = (uint64_t)h.num_faces, nn = (uint64_t)h.num_nodes;
+  if (h.off_nodes < 256 || h.off_tris < h.off_nodes + nn * sizeof(BvhNode4) ||
+      h.off_faces < h.off_tris + 3 * nf * sizeof(float4) || h.off_colors < h.off_faces + 3 * nf * 4 ||
+      h.off_normals < h.off_colors + nv * 4 || h.file_bytes != h.off_normals + 3 * nv * 4 ||
+      (uint64_t)size != h.file_bytes)
+    fail_io("inconsistent layout or truncated file");
+  p->nv = (int64_t)nv;
+  p->nf = (int64_t)nf;
+  p->bsdf = h.bsdf_type;
+  for (int c = 0; c < 6; ++c) p->bounds[c] = h.world_bounds[c];
+  for (int c = 0; c < 3; ++c) p->bsdf_p[c] = h.bsdf_params[c];
+  p->bvh_depth = h.bvh_depth;
+  p->nodes.resize(nn);
+  p->tris.resize(3 * nf);
+  p->faces.resize(3 * nf);
+  p->colors.resize(nv);
+  p->normals.resize(3 * nv);
+  auto get = [&](uint64_t off, void* dst, size_t n) {
+    ok = ok && std::fseek(f, (long)off, SEEK_SET) == 0 && std::fread(dst, 1, n, f) == n;
+  };
+  get(h.off_nodes, p->nodes.data(), nn * sizeof(BvhNode4));
+  get(h.off_tris, p->tris.data(), 3 * nf * sizeof(float4));
+  get(h.off_faces, p->faces.data(), 3 * nf * 4);
+  get(h.off_colors, p->colors.data(), nv * 4);
+  get(h.off_normals, p->normals.data(), 3 * nv * 4);
+  std::fclose(f);
+  if (!ok) throw IoError(path + ": read failed");
+  for (uint64_t i = 0; i < 3 * nf; ++i)
+    if (p->faces[i] >= nv) throw IoError(path + ": face index out of range");
+}
+
+// Builds and writes every domain's blob (domains in parallel).
+void prepareScene(const spray_gpu_domain* domains, int nd, const std::string& dir) {
+  std::vector<std::string> errors(nd);
+  std::vector<char> io(nd, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int d = 0; d < nd; ++d) {
+    try {
+      DomainPack p;
+      buildPack(domains[d], d, p);
+      writeDomainBlob(domainBlobPath(dir, d), p);
+    } catch (const IoError& e) {
+      errors[d] = e.what();
+      io[d] = 1;
+    } catch (const std::exception& e) {
+      errors[d] = e.what();
+    }
+  }
+  for (int d = 0; d < nd; ++d) {
+    if (errors[d].empty()) continue;
+    if (io[d]) throw IoError(errors[d]);
+    throw std::invalid_argument(errors[d]);
+  }
+}
+
 // ---------------------------------------------------------------- tracer
 Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   if (cfg.image_w <= 0 || cfg.image_h <= 0) throw std::invalid_argument("image size must be positive");
@@ -139,8 +313,8 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   if (cfg.max_samples_per_rank <= 0) throw std::invalid_argument("max_samples_per_rank must be positive");
   if (cfg.num_ranks <= 0 || cfg.rank < 0 || cfg.rank >= cfg.num_ranks)
     throw std::invalid_argument("rank must be in [0, num_ranks)");
-  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 3)
-    throw std::invalid_argument("schedule_policy must be 0, 1, 2 or 3");
+  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 4)
+    throw std::invalid_argument("schedule_policy must be 0, 1, 2, 3 or 4");
   if (cfg.schedule_policy == 3 &&
       (cfg.learn_samples < 0 || cfg.learn_batch <= 0 || cfg.learn_epochs < 0 || !(cfg.learn_lr > 0.0f) ||
        cfg.learn_frames < 1))
@@ -282,42 +456,41 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
 #pragma omp parallel for schedule(dynamic, 1)
   for (int d = 0; d < nd; ++d) {
     try {
-      const spray_gpu_domain& src = doms[d];
-      if (src.num_faces <= 0 || src.num_vertices <= 0 || !src.vertices || !src.faces)
-        throw std::invalid_argument("domain " + std::to_string(d) + " has no geometry");
-      if (src.num_faces >= (1ll << 28)) throw std::invalid_argument("domain too large");
-      for (int64_t i = 0; i < 3 * src.num_faces; ++i)
-        if ((int64_t)src.faces[i] >= src.num_vertices)
-          throw std::invalid_argument("domain " + std::to_string(d) + ": face index out of range");
-      DomainPack& p = packs[d];
-      p.nv = src.num_vertices;
-      p.nf = src.num_faces;
-      p.normals.resize(3 * (size_t)p.nv);
-      computeVertexNormals(src.vertices, p.nv, src.faces, p.nf, p.normals.data());
-      BvhBuildResult bvh;
-      buildBvh4(src.vertices, src.faces, (uint32_t)p.nf, &bvh);
-      p.nodes = std::move(bvh.nodes);
-      p.bvh_depth = bvh.depth;
-      p.tris.resize(3 * (size_t)p.nf);
-      for (size_t k = 0; k < bvh.tri_order.size(); ++k) {
-        uint32_t prim = bvh.tri_order[k];
-        const uint32_t* fi = src.faces + 3 * (size_t)prim;
-        for (int c = 0; c < 3; ++c) {
-          const float* vp = src.vertices + 3 * (size_t)fi[c];
-          float w = 0.f;
-          if (c == 0) std::memcpy(&w, &prim, 4);
-          p.tris[3 * k + c] = make_float4(vp[0], vp[1], vp[2], w);
-        }
-      }
-      p.faces.assign(src.faces, src.faces + 3 * p.nf);
-      if (src.colors) p.colors.assign(src.colors, src.colors + p.nv);
-      else p.colors.assign(p.nv, 0u);
+      buildPack(doms[d], d, packs[d]);
     } catch (const std::exception& e) {
       errors[d] = e.what();
     }
   }
   for (int d = 0; d < nd; ++d)
     if (!errors[d].empty()) throw std::invalid_argument(errors[d]);
+  installScene(packs, ls, nl);
+}
+
+void Tracer::setScenePrepared(const std::string& dir, int nd, const spray_gpu_light* ls, int nl) {
+  if (nd <= 0) throw std::invalid_argument("a scene needs at least one domain");
+  freeScene();
+  D = nd;
+  lights.assign(ls, ls + nl);
+  if (slots() > kMaxSlots) throw std::invalid_argument("too many shadow rays per hit (max 64)");
+  std::vector<DomainPack> packs(nd);
+  std::vector<std::string> errors(nd);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int d = 0; d < nd; ++d) {
+    try {
+      readDomainBlob(domainBlobPath(dir, d), &packs[d]);
+    } catch (const std::exception& e) {
+      errors[d] = e.what();
+    }
+  }
+  for (int d = 0; d < nd; ++d)
+    if (!errors[d].empty()) throw IoError(errors[d]);
+  installScene(packs, ls, nl);
+}
+
+// Concatenates the prepared domains (in-core) or moves them to the pinned
+// arena (out of core), then builds the domain hierarchy and the light table.
+void Tracer::installScene(std::vector<DomainPack>& packs, const spray_gpu_light* ls, int nl) {
+  const int nd = (int)packs.size();
   domain_verts.assign(nd, 0);
   for (int d = 0; d < nd; ++d) domain_verts[d] = (size_t)packs[d].nv;
   // concatenate in domain order
@@ -328,16 +501,16 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   for (int d = 0; d < nd; ++d) {
     DomainDev& dd = hdoms[d];
     for (int c = 0; c < 3; ++c) {
-      dd.bmin[c] = doms[d].world_bounds[c];
-      dd.bmax[c] = doms[d].world_bounds[3 + c];
+      dd.bmin[c] = packs[d].bounds[c];
+      dd.bmax[c] = packs[d].bounds[3 + c];
     }
     dd.node_base = (int32_t)nn;
     dd.tri_base = (int32_t)nt;
     dd.gprim_base = (uint32_t)gp;
     dd.vert_base = (int32_t)nvv;
     dd.face_base = (int32_t)nt;
-    dd.bsdf = doms[d].bsdf_type;
-    for (int c = 0; c < 3; ++c) dd.bsdf_p[c] = doms[d].bsdf_params[c];
+    dd.bsdf = packs[d].bsdf;
+    for (int c = 0; c < 3; ++c) dd.bsdf_p[c] = packs[d].bsdf_p[c];
     dd.resident = 1;
     dd.num_nodes = (int32_t)packs[d].nodes.size();
     dd.num_tris = (int32_t)packs[d].nf;
@@ -880,7 +1053,10 @@ void Tracer::traceWave(const Wave& w, bool capture) {
   const int S = std::max(slots(), 1);
   const int spp = cfg.pixel_samples;
   beginWave(w);
-  const int order_by_depth = (cfg.cull && !ooc) ? 1 : 0;
+  // non-speculative (policy 4): one pass per list position, so radiance
+  // queues are keyed by depth bucket out of core as well
+  const bool nonspec = ooc && cfg.schedule_policy == 4;
+  const int order_by_depth = (cfg.cull && (!ooc || nonspec)) ? 1 : 0;
   const int nblk = num_sms * 4;
   for (int b = 0; b < cfg.bounces; ++b) {
     if (capture) captureRays(b);
@@ -904,7 +1080,14 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     // entry sees the hits of all nearer domain lists (front-to-back waves)
     TraceArgs ta = traceArgs(order_by_depth, S);
     std::vector<int> order;
-    if (ooc) {
+    if (nonspec) {
+      // LoadAnyOnce restated: a ray waits in the queue of its next domain only
+      // (list position k in pass k), and continues only when no hit lies in
+      // front of that domain; each pass takes the domains with the most
+      // pending rays first
+      const int rb = order_by_depth ? kDepthBuckets : 1;
+      for (int k = 0; k < rb; ++k) oocPass(true, false, S, rb, k, 1, true);
+    } else if (ooc) {
       order = scoreOrder();
       if (cfg.schedule_policy == 1) {
         traceOutOfCore(false, residentFirst(order), S);
@@ -937,9 +1120,11 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
                   nullptr, d_block_tmp, compact_blocks);
     launches += 3;
-    schedule(true, 0, d_shadow_count, d_shadow_list, S);
+    schedule(true, 0, d_shadow_count, d_shadow_list, S, false, nonspec);
     if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, 0);
-    if (ooc && cfg.schedule_policy == 0) {
+    if (nonspec) {
+      oocPass(false, true, S, 1, 0, 0, true);
+    } else if (ooc && cfg.schedule_policy == 0) {
       traceOutOfCore(true, order, S);
     } else if (ooc) {
       traceOutOfCore(true, residentFirst(order), S);
@@ -989,7 +1174,9 @@ std::vector<int> Tracer::residentFirst(const std::vector<int>& order) const {
 // all of its shadow rays already occluded) is dropped without being loaded.
 // Dropping changes neither hit nor occlusion: a culled entry cannot beat its
 // ray's hit, and an occluded shadow ray stays occluded.
-void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
+void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int rb_count, bool by_live) {
+  if (rb_count < 0) rb_count = rb - rb_first;
+  const int rb_end = rb_first + rb_count;
   const int nrk = rb * D;  // radiance keys: bucket * D + domain
   std::vector<uint32_t> rk(nrk + 1, 0), sk(D + 1, 0);
   uint32_t rn = 0, sn = 0;
@@ -1008,7 +1195,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
   if (!with_r && !with_s) return;
   auto rcount = [&](int d) {
     uint32_t c = 0;
-    for (int b = 0; b < rb; ++b) c += rk[b * D + d + 1] - rk[b * D + d];
+    for (int b = rb_first; b < rb_end; ++b) c += rk[b * D + d + 1] - rk[b * D + d];
     return c;
   };
   std::vector<int> order = scoreOrder();
@@ -1035,7 +1222,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
   const int B = std::min(cfg.ooc_batch > 0 ? cfg.ooc_batch : half, half);
   // domains whose live entries are counted before a batch is chosen: enough to
   // fill it after drops; with in-place tracing every remaining domain may join
-  const int window_n = cfg.ooc_inplace > 0 ? D : 2 * B;
+  const int window_n = (cfg.ooc_inplace > 0 || by_live) ? D : 2 * B;
   int32_t* hdoms_list = reinterpret_cast<int32_t*>(h_live);
   uint32_t* hlive = h_live + D;
   // live counts of `doms`, written to hlive when `done` has completed
@@ -1046,7 +1233,8 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
       LiveArgs la{};
       la.rentries = with_r ? d_entries : nullptr;
       la.rkey_start = d_key_start;
-      la.rbuckets = rb;
+      la.rbucket0 = rb_first;
+      la.rbuckets = rb_count;
       la.ray_key = d_ray_key;
       la.rec_key = d_rec_key;
       la.sentries = with_s ? d_sentries : nullptr;
@@ -1137,6 +1325,13 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
   cudaEvent_t counted = poolEvent();
   countLive(window(remaining), counted);
   CK(cudaEventSynchronize(counted));
+  if (by_live) {
+    // LoadAnyOnceImageSched::schedule (src/baseline/baseline_schedulers.cc): the
+    // domain holding the most pending rays first
+    std::stable_sort(remaining.begin(), remaining.end(), [&](int x, int y) {
+      return (uint64_t)hlive[x] + hlive[D + x] > (uint64_t)hlive[y] + hlive[D + y];
+    });
+  }
   nextBatch(batch);
   cudaEvent_t loaded = poolEvent();
   if (!batch.empty()) issueLoads(batch, loaded);
@@ -1152,7 +1347,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb) {
     std::vector<int> nseg(rb + 1, 0);
     for (int q = 0; q <= rb; ++q) {
       const bool shadow = q == rb;
-      const bool on = shadow ? with_s : with_r;
+      const bool on = shadow ? with_s : (with_r && q >= rb_first && q < rb_end);
       uint32_t* beg = seg + q * tbl;
       uint32_t* pre = beg + D + 1;
       uint32_t run = 0;
@@ -1592,7 +1787,8 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
       for (size_t k = 0; k < waves.size(); ++k) {
         const bool capture = cfg.debug_capture && k == 0;
-        if (ooc && cfg.schedule_policy >= 2 && !capture) traceWaveBatched(waves[k]);
+        if (ooc && (cfg.schedule_policy == 2 || cfg.schedule_policy == 3) && !capture)
+        traceWaveBatched(waves[k]);
         else traceWave(waves[k], capture);
       }
     }
@@ -1842,6 +2038,8 @@ using spray::fail;
     return fail(SPRAY_GPU_ESTATE, e.what());                             \
   } catch (const spray::OverflowError& e) {                              \
     return fail(SPRAY_GPU_EOVERFLOW, e.what());                          \
+  } catch (const spray::IoError& e) {                                    \
+    return fail(SPRAY_GPU_EIO, e.what());                                \
   } catch (const std::invalid_argument& e) {                             \
     return fail(SPRAY_GPU_EINVAL, e.what());                             \
   } catch (const std::bad_alloc&) {                                      \
@@ -1908,6 +2106,24 @@ int spray_gpu_set_scene(spray_gpu_tracer* t, const spray_gpu_domain* domains, in
   if (!t || !domains || (num_lights > 0 && !lights)) return fail(SPRAY_GPU_EINVAL, "null argument");
   API_GUARD({
     t->impl->setScene(domains, num_domains, lights, num_lights);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_set_scene_prepared(spray_gpu_tracer* t, const char* dir, int32_t num_domains,
+                                 const spray_gpu_light* lights, int32_t num_lights) {
+  if (!t || !dir || (num_lights > 0 && !lights)) return fail(SPRAY_GPU_EINVAL, "null argument");
+  API_GUARD({
+    t->impl->setScenePrepared(dir, num_domains, lights, num_lights);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_scene_prepare(const spray_gpu_domain* domains, int32_t num_domains, const char* dir) {
+  if (!domains || !dir) return fail(SPRAY_GPU_EINVAL, "null argument");
+  if (num_domains <= 0) return fail(SPRAY_GPU_EINVAL, "a scene needs at least one domain");
+  API_GUARD({
+    spray::prepareScene(domains, num_domains, dir);
     return SPRAY_GPU_OK;
   })
 }

@@ -22,6 +22,9 @@ struct StateError : std::runtime_error {
 struct OverflowError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
+struct IoError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
 
 int fail(int code, const std::string& msg);
 
@@ -38,6 +41,9 @@ struct Wave {
 // A domain prepared for the device: BVH, leaf-ordered triangles and the
 // per-vertex shading data.
 struct DomainPack {
+  float bounds[6] = {0, 0, 0, 0, 0, 0};  // world AABB: min xyz, max xyz
+  int32_t bsdf = 0;
+  float bsdf_p[3] = {0, 0, 0};
   int64_t nv = 0, nf = 0;
   std::vector<BvhNode4> nodes;
   std::vector<float4> tris;
@@ -58,6 +64,16 @@ struct LruSlots {
   bool load(int domain, int* slot, int* evicted);
 };
 
+// Normals, BVH and leaf-ordered triangles of one domain (TriMeshBuffer::load
+// and its Embree build, src/render/trimesh_buffer.cc:117-326).
+void buildPack(const spray_gpu_domain& src, int d, DomainPack& p);
+// Prepared-domain blobs: one file per domain holding everything buildPack
+// makes, so that a scene is prepared once and loaded without rebuilding.
+std::string domainBlobPath(const std::string& dir, int d);
+void writeDomainBlob(const std::string& path, const DomainPack& p);
+void readDomainBlob(const std::string& path, DomainPack* p);
+void prepareScene(const spray_gpu_domain* domains, int nd, const std::string& dir);
+
 std::vector<HostTile> makeTiles(int W, int H, int spp, int num_ranks, int rank, int64_t max_samples);
 void computeVertexNormals(const float* v, int64_t nv, const uint32_t* f, int64_t nf, float* n);
 CameraDev makeCamera(const float p[3], const float l[3], const float up[3], float vfov, int W, int H);
@@ -67,6 +83,8 @@ class Tracer {
   explicit Tracer(const spray_gpu_config& c);
   ~Tracer();
   void setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_light* ls, int nl);
+  // the same from blobs written by writeDomainBlob (no normal or BVH build)
+  void setScenePrepared(const std::string& dir, int nd, const spray_gpu_light* ls, int nl);
   void setCamera(const float p[3], const float l[3], const float up[3], float vfov);
   void trace(float* out, bool out_is_device, spray_gpu_stats* st);
   int64_t debugCount(int what, int bounce) const;
@@ -102,11 +120,16 @@ class Tracer {
   void captureScores(int b);
   void captureHits(int b);
   void captureShadows(int b, int S);
+  void installScene(std::vector<DomainPack>& packs, const spray_gpu_light* ls, int nl);
   void setupOutOfCore(std::vector<DomainPack>& packs, int capacity, size_t max_nodes, size_t max_tris,
                       size_t max_verts, size_t slot_bytes);
   void loadDomain(int d, int slot, cudaStream_t s);
   void traceOutOfCore(bool shadow, const std::vector<int>& order, int S);
-  void oocPass(bool with_radiance, bool with_shadow, int S, int rbuckets);
+  // One pass over the domains for the radiance queues (buckets [rb_first,
+  // rb_first + rb_count) of rbuckets) and/or the shadow queues; by_live orders
+  // the domains by live entries, most first, instead of resident-first.
+  void oocPass(bool with_radiance, bool with_shadow, int S, int rbuckets, int rb_first = 0,
+               int rb_count = -1, bool by_live = false);
   std::vector<int> residentFirst(const std::vector<int>& order) const;
   std::vector<int> scoreOrder();
 

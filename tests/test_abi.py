@@ -60,7 +60,7 @@ def test_invalid_config_rejected(lib_built):
     assert e.value.code in (sg.EINVAL, sg.ECUDA)
 
 
-@pytest.mark.parametrize("kw", [dict(schedule_policy=4), dict(schedule_policy=-1), dict(ooc_batch=-1),
+@pytest.mark.parametrize("kw", [dict(schedule_policy=5), dict(schedule_policy=-1), dict(ooc_batch=-1),
                                 dict(schedule_policy=3, learn_batch=0), dict(schedule_policy=3, learn_lr=0.0),
                                 dict(schedule_policy=3, learn_frames=0), dict(ooc_inplace=-1)])
 def test_out_of_core_options_validated(lib_built, kw):

@@ -310,7 +310,9 @@ def test_scene_file_path(lib_built, oracle_mod, tmp_path):
                                 dict(cache_bytes=3 << 20, schedule_policy=2, ooc_batch=3, ooc_inplace=0),
                                 dict(cache_size=16, schedule_policy=2, ooc_inplace=200),
                                 dict(cache_size=16, schedule_policy=2, ooc_inplace=1 << 30),
-                                dict(cache_size=16, schedule_policy=2)])
+                                dict(cache_size=16, schedule_policy=2),
+                                dict(cache_size=16, schedule_policy=4, ooc_inplace=0),
+                                dict(cache_size=5, schedule_policy=4, ooc_batch=2)])
 def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     """Streaming domains through a small LRU cache changes loads, never the image."""
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
@@ -325,7 +327,7 @@ def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     t.set_camera(*cam)
     got, st = t.trace()
     assert np.array_equal(bits(got), bits(want))
-    inplace = kw.get("ooc_inplace", 16384) if kw.get("schedule_policy", 0) >= 2 else 0
+    inplace = kw.get("ooc_inplace", 16384) if kw.get("schedule_policy", 0) in (2, 3, 4) else 0
     if inplace >= 1 << 30:
         assert st["domain_loads"] == 0 and st["inplace_domains"] > 0  # every domain read in place
     elif inplace == 0:
@@ -454,3 +456,40 @@ def test_graph_replay_follows_camera_and_matches_direct_launches(lib_built, scen
                   "kernel_launches", "trace_launches"):
             assert sgr[k] == sd[k], (frame, k)
         assert sgr["trace_ms"] > 0 and sgr["frame_ms"] > 0
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(cache_size=3, schedule_policy=2)])
+def test_prepared_blobs_render_the_same_image(lib_built, scene64, tmp_path, kw):
+    """A scene set from prepared-domain blobs renders bit-identically to set_scene."""
+    sg.prepare_scene(scene64, tmp_path)
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
+    cam = scenes.orbit_camera(scene64)
+    imgs = []
+    for prepared in (False, True):
+        t = sg.Tracer(cfg, **kw)
+        if prepared:
+            t.set_scene_prepared(tmp_path, len(scene64.domains), scene64.lights)
+        else:
+            t.set_scene(scene64)
+        t.set_camera(*cam)
+        img, st = t.trace()
+        imgs.append((img, st))
+    assert np.array_equal(bits(imgs[0][0]), bits(imgs[1][0]))
+    assert imgs[0][1]["scene_triangles"] == imgs[1][1]["scene_triangles"]
+
+
+def test_non_speculative_order_visits_least(lib_built, scene64):
+    """The LoadAnyOnce restatement traces each ray only in domains it reaches
+    without a nearer hit: no more radiance visits than the speculative passes."""
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3, cache_size=16,
+                       ooc_inplace=0)
+    cam = scenes.orbit_camera(scene64)
+    out = {}
+    for pol in (0, 4):
+        t = sg.Tracer(cfg, schedule_policy=pol)
+        t.set_scene(scene64)
+        t.set_camera(*cam)
+        out[pol] = t.trace()
+    (i0, s0), (i4, s4) = out[0], out[4]
+    assert np.array_equal(bits(i0), bits(i4))
+    assert s4["visits_radiance"] <= s0["visits_radiance"]

@@ -129,3 +129,40 @@ def test_ppm_writer_semantics(tmp_path):
     assert data[3 + 2] == "1 1022 1023"
     assert data[3 + 3] == "511 1023 0"
     assert np.array_equal(image.read_ppm_bytes(image.ppm_bytes(img))[0, 0], [511, 1023, 0])
+
+
+def test_prepared_domain_blobs_round_trip(lib_built, tmp_path):
+    """spray_scene_prepare writes one self-describing blob per domain (no GPU)."""
+    import struct
+    import spray_gb300 as sg
+    from spray_gb300 import scenes
+    scene = scenes.wavelet_grid(2, 16, colors="albedo", light="point")
+    sg.prepare_scene(scene, tmp_path)
+    files = sorted(tmp_path.glob("domain_*.sdom"))
+    assert len(files) == len(scene.domains)
+    for d, f in enumerate(files):
+        raw = f.read_bytes()
+        assert raw[:8] == b"SPRAYDOM"
+        version, bsdf = struct.unpack_from("<Ii", raw, 8)
+        bounds = struct.unpack_from("<6f", raw, 16)
+        nv, nf, nn = struct.unpack_from("<3q", raw, 16 + 24 + 12 + 4)
+        offs = struct.unpack_from("<6Q", raw, 16 + 24 + 12 + 4 + 24)
+        dom = scene.domains[d]
+        assert version == 1 and nv == len(dom.vertices) and nf == len(dom.faces) and nn > 0
+        assert np.array_equal(np.float32(bounds), dom.bounds)
+        assert offs[-1] == len(raw)
+        faces = np.frombuffer(raw, np.uint32, 3 * nf, offs[2]).reshape(-1, 3)
+        assert np.array_equal(faces, dom.faces)
+
+
+def test_prepared_blob_errors(lib_built, tmp_path):
+    import spray_gb300 as sg
+    bad = tmp_path / "domain_00000.sdom"
+    bad.write_bytes(b"not a blob" * 40)
+    try:
+        t = sg.Tracer(image_w=8, image_h=8)
+    except sg.SprayError:
+        pytest.skip("no GPU: the loader runs inside a tracer")
+    with pytest.raises(sg.SprayError) as e:
+        t.set_scene_prepared(tmp_path, 1)
+    assert e.value.code == sg.EIO
