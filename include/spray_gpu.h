@@ -131,6 +131,26 @@ typedef struct spray_gpu_light {
   float edge2[3];
 } spray_gpu_light;
 
+/* One view of a multi-view batch: camera (Camera::init, src/render/camera.h:
+ * 128-166), image size, samples and shader settings (the matching
+ * spray_gpu_config fields).  Views of one call share the scene, the lights,
+ * ks/shininess and every queue of the wavefront. */
+typedef struct spray_gpu_view {
+  float position[3];
+  float lookat[3];
+  float up[3];
+  float vfov;
+  int32_t image_w;
+  int32_t image_h;
+  int32_t pixel_samples;
+  int32_t ao_mode;
+  int32_t ao_samples;
+  int32_t bounces;
+  int32_t rr_depth;
+  int32_t ao_light_shadow;
+  float ao_max_distance;
+} spray_gpu_view;
+
 /* Per-frame counters.  A "ray" is one logical ray counted once, whatever the
  * number of domains it visits; a "visit" is one (ray, domain) pair traced. */
 typedef struct spray_gpu_stats {
@@ -203,6 +223,16 @@ int spray_gpu_trace(spray_gpu_tracer* t, float* rgba_out, spray_gpu_stats* stats
 /* Same frame, result left in device memory (W*H*4 floats at rgba_dev), for
  * callers that keep the image on the GPU.  No host copy. */
 int spray_gpu_trace_device(spray_gpu_tracer* t, float* rgba_dev, spray_gpu_stats* stats);
+
+/* Several views traced in the same wavefronts (no counterpart in SpRay,
+ * which renders one camera per run): each view's float4 image, view after
+ * view, into `images` (host memory, sum of W*H*4 floats); the _device
+ * variant writes device memory.  Each view's image equals what a tracer
+ * configured with that view's settings renders. */
+int spray_gpu_trace_views(spray_gpu_tracer* t, const spray_gpu_view* views, int32_t num_views, float* images,
+                          spray_gpu_stats* stats);
+int spray_gpu_trace_views_device(spray_gpu_tracer* t, const spray_gpu_view* views, int32_t num_views,
+                                 float* images, spray_gpu_stats* stats);
 
 /* ---------------------------------------------------------------- host scene
  * SceneLoader::load + PlyLoader (src/io/scene_loader.cc:315-358,

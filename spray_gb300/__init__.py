@@ -58,6 +58,14 @@ class LightC(C.Structure):
                 ("edge1", C.c_float * 3), ("edge2", C.c_float * 3)]
 
 
+class ViewC(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("lookat", C.c_float * 3), ("up", C.c_float * 3),
+                ("vfov", C.c_float), ("image_w", C.c_int32), ("image_h", C.c_int32),
+                ("pixel_samples", C.c_int32), ("ao_mode", C.c_int32), ("ao_samples", C.c_int32),
+                ("bounces", C.c_int32), ("rr_depth", C.c_int32), ("ao_light_shadow", C.c_int32),
+                ("ao_max_distance", C.c_float)]
+
+
 class StatsC(C.Structure):
     _fields_ = [
         ("rays_primary", C.c_int64), ("rays_shadow", C.c_int64), ("rays_bounce", C.c_int64),
@@ -131,6 +139,8 @@ def lib() -> C.CDLL:
                                              P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.spray_gpu_schedule_static.argtypes = [P, C.c_int32, P, P, C.c_int32, C.c_int32, P, C.c_int64, P,
                                                 C.POINTER(C.c_int64), P]
+        L.spray_gpu_trace_views.argtypes = [P, C.POINTER(ViewC), C.c_int32, P, C.POINTER(StatsC)]
+        L.spray_gpu_trace_views_device.argtypes = [P, C.POINTER(ViewC), C.c_int32, P, C.POINTER(StatsC)]
         L.spray_scene_prepare.argtypes = [C.POINTER(DomainC), C.c_int32, C.c_char_p]
         L.spray_gpu_set_scene_prepared.argtypes = [P, C.c_char_p, C.c_int32, C.POINTER(LightC), C.c_int32]
         F4 = C.POINTER(C.c_float)
@@ -310,6 +320,34 @@ class Tracer:
         st = StatsC()
         _check(lib().spray_gpu_trace(self._h, out.ctypes.data_as(C.c_void_p), C.byref(st)))
         return out, st.asdict()
+
+    def trace_views(self, views: list[dict]) -> tuple[list[np.ndarray], dict]:
+        """Several views in one frame (multi-view batch).  Each view is a dict with
+        position, lookat, up, vfov and any of image_w, image_h, pixel_samples,
+        ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow, ao_max_distance
+        (defaults: this tracer's configuration).  Returns one (H, W, 4) image per
+        view and the frame's stats."""
+        arr = (ViewC * len(views))()
+        shapes = []
+        for i, v in enumerate(views):
+            c = arr[i]
+            c.position = (C.c_float * 3)(*[float(x) for x in v["position"]])
+            c.lookat = (C.c_float * 3)(*[float(x) for x in v["lookat"]])
+            c.up = (C.c_float * 3)(*[float(x) for x in v.get("up", (0, 1, 0))])
+            c.vfov = float(v.get("vfov", self.config["fov"]))
+            for k in ("image_w", "image_h", "pixel_samples", "ao_mode", "ao_samples", "bounces", "rr_depth",
+                      "ao_light_shadow"):
+                setattr(c, k, int(v.get(k, self.config[k])))
+            c.ao_max_distance = float(v.get("ao_max_distance", self.config["ao_max_distance"]))
+            shapes.append((c.image_h, c.image_w))
+        out = np.empty(sum(h * w for h, w in shapes) * 4, np.float32)
+        st = StatsC()
+        _check(lib().spray_gpu_trace_views(self._h, arr, len(views), out.ctypes.data_as(C.c_void_p), C.byref(st)))
+        imgs, off = [], 0
+        for h, w in shapes:
+            imgs.append(out[off:off + h * w * 4].reshape(h, w, 4))
+            off += h * w * 4
+        return imgs, st.asdict()
 
     def trace_device(self, dev_ptr: int) -> dict:
         """One frame into device memory at dev_ptr (W*H*4 floats)."""

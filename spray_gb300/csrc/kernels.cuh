@@ -119,8 +119,9 @@ struct RayBuf {
   float4* org;
   float4* dir;
   float4* wgt;
-  int32_t* pixid;
+  int32_t* pixid;   // pixel inside the sample's view (y * width + x)
   int32_t* samid;
+  uint16_t* view;   // view of the sample
 };
 
 // Shadow rays of a bounce, indexed by alive_index * slots + slot.
@@ -142,6 +143,21 @@ struct CameraDev {
 struct TileDev {
   int32_t x, y, w, h;
   int64_t sample_base;  // first sample of the tile inside the wave
+  int64_t pix_base;     // first pixel of the tile among the wave's pixels
+  int32_t view;         // view the tile belongs to
+  int32_t spp;          // samples per pixel of that view
+};
+
+// One view of a frame: camera, image and shader settings.  A frame may trace
+// several views in the same wavefronts (multi-view batches); every sample
+// carries its view.
+struct ViewDev {
+  CameraDev cam;
+  int32_t image_w, image_h, spp;
+  int32_t ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow;
+  float ao_max_distance;
+  int64_t pixel_base;   // first pixel of the view in the frame's image buffer
+  double scale;         // retire weight scale, 1 / spp
 };
 
 // Scheduling of one ray set into per-domain queues.
@@ -230,9 +246,8 @@ struct ShadeArgs {
   uint8_t* shadow_flag;       // per shadow id
   int slots;
   int depth;                  // actual depth of the rays being shaded
-  // shader configuration
-  int ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow;
-  float ao_max_distance;
+  // shader configuration: per view (AO or PT, samples, bounces, ...) and shared
+  const ViewDev* views;
   float ks[3], shininess;
   const float* lights;        // 13 floats per light: type, pos, radiance, e1, e2
   int num_lights;
@@ -240,10 +255,11 @@ struct ShadeArgs {
 };
 
 // ---------------------------------------------------------------- launchers
-// The camera is read from device memory, so a captured frame follows camera changes.
-void launchGenPrimary(cudaStream_t s, const CameraDev* cam, const TileDev* tiles, int ntiles,
-                      int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
-                      uint32_t* alive_count, int32_t* alive_idx, Counters* ctr);
+// Views (cameras) and tiles are read from device memory, so a captured frame
+// follows camera changes.
+void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles,
+                      int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
+                      int32_t* alive_idx, Counters* ctr);
 // scan_tmp holds kMaxScanBlocks words.  Launches 5 kernels.
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
                     int nwarps, int nblocks, uint32_t* scan_tmp);
@@ -265,9 +281,13 @@ void launchShade(cudaStream_t s, const ShadeArgs& a, int nblocks);
 void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
                    uint64_t n_host, uint32_t* list, uint32_t* count, int32_t* index_of,
                    uint32_t* block_tmp, int nblocks);
-void launchRetireImpl(cudaStream_t s, float4* image, int64_t npix, int spp, const int32_t* pixid,
-                      const int32_t* alive_idx, const ShadowBuf sh, const uint8_t* flag, int slots,
-                      double scale, int nblocks);
+// Adds the unoccluded shadow rays of every pixel of a wave (npix pixels over
+// ntiles tiles) to the frame image, samples of a pixel in order.
+void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
+                      const ViewDev* views, const int32_t* pixid, const int32_t* alive_idx,
+                      const ShadowBuf sh, const uint8_t* flag, int slots, int nblocks);
+// Uploads the constant tables of the shader (once per device).
+void initShadeTables();
 void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int list_size,
                   long long* scores, int32_t* order);
 // Out of core: entries of each listed domain that are still live.  A radiance

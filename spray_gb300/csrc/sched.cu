@@ -31,20 +31,26 @@ __device__ __forceinline__ uint32_t warpExclusiveScan(uint32_t v, uint32_t* tota
 // (src/ooc/ooc_tracer.inl:84-172) with Camera::generateRay
 // (src/render/camera.h:173-209): u = x / W, v = y / H, jitter drawn from a
 // sampler seeded with the tile-local sample id when pixel_samples > 1.
-__global__ void kGenPrimary(const CameraDev* __restrict__ camp, const TileDev* __restrict__ tiles, int ntiles,
-                            int64_t nsamples, int spp, int image_w, RayBuf rays,
-                            uint32_t* alive_list, uint32_t* alive_count, int32_t* alive_idx,
-                            Counters* ctr) {
+__global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __restrict__ tiles, int ntiles,
+                            int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
+                            int32_t* alive_idx, Counters* ctr) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const CameraDev cam = *camp;
   if (i == 0) {
     *alive_count = (uint32_t)nsamples;
     atomicAdd(&ctr->rays_primary, (unsigned long long)nsamples);
   }
   if (i >= nsamples) return;
-  int k = 0;
-  while (k + 1 < ntiles && tiles[k + 1].sample_base <= i) ++k;
-  const TileDev tl = tiles[k];
+  // last tile with sample_base <= i
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].sample_base <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  const TileDev tl = tiles[lo];
+  const ViewDev& vw = views[tl.view];
+  const CameraDev& cam = vw.cam;
+  const int spp = tl.spp;
   int32_t bufid = (int32_t)(i - tl.sample_base);
   int32_t lp = spp > 1 ? bufid / spp : bufid;
   int x = tl.x + lp % tl.w;
@@ -65,20 +71,21 @@ __global__ void kGenPrimary(const CameraDev* __restrict__ camp, const TileDev* _
   rays.org[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
   rays.dir[i] = make_float4(d.x, d.y, d.z, 0.f);
   rays.wgt[i] = make_float4(1.f, 1.f, 1.f, 0.f);
-  rays.pixid[i] = y * image_w + x;
+  rays.pixid[i] = y * vw.image_w + x;
   rays.samid[i] = bufid;
+  rays.view[i] = (uint16_t)tl.view;
   alive_list[i] = (uint32_t)i;
   alive_idx[i] = (int32_t)i;
 }
 
-void launchGenPrimary(cudaStream_t s, const CameraDev* cam, const TileDev* tiles, int ntiles,
-                      int64_t nsamples, int spp, int image_w, RayBuf rays, uint32_t* alive_list,
-                      uint32_t* alive_count, int32_t* alive_idx, Counters* ctr) {
+void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles, int64_t nsamples,
+                      RayBuf rays, uint32_t* alive_list, uint32_t* alive_count, int32_t* alive_idx,
+                      Counters* ctr) {
   int threads = 256;
   int64_t blocks = (nsamples + threads - 1) / threads;
   if (blocks < 1) blocks = 1;
-  kGenPrimary<<<(unsigned)blocks, threads, 0, s>>>(cam, tiles, ntiles, nsamples, spp, image_w, rays,
-                                                   alive_list, alive_count, alive_idx, ctr);
+  kGenPrimary<<<(unsigned)blocks, threads, 0, s>>>(views, tiles, ntiles, nsamples, rays, alive_list, alive_count,
+                                                   alive_idx, ctr);
 }
 
 // ---------------------------------------------------------------- schedule

@@ -96,13 +96,17 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
     const bool delta = dom.bsdf != 0;
     const int pixid = a.rays.pixid[sample];
     const int samid = a.rays.samid[sample];
+    const ViewDev& vw = a.views[a.rays.view[sample]];
+    const int ao_mode = vw.ao_mode, ao_samples = vw.ao_samples, bounces = vw.bounces;
+    const int rr_depth = vw.rr_depth, ao_light_shadow = vw.ao_light_shadow;
+    const float ao_max_distance = vw.ao_max_distance;
     const int next_depth = a.depth + 1;
     a.sh.hitpos[i] = make_float4(pos.x, pos.y, pos.z, __int_as_float(d));
     int slot = 0;
-    if (a.ao_mode) {
-      const float ao_weight = 1.0f / (float)a.ao_samples;
-      const float tmax = a.ao_max_distance > 0.0f ? a.ao_max_distance : __int_as_float(0x7f800000);
-      for (int l = 0; l < a.ao_samples; ++l, ++slot) {
+    if (ao_mode) {
+      const float ao_weight = 1.0f / (float)ao_samples;
+      const float tmax = ao_max_distance > 0.0f ? ao_max_distance : __int_as_float(0x7f800000);
+      for (int l = 0; l < ao_samples; ++l, ++slot) {
         bool valid = false;
         V3 wi = v3(0, 0, 0), Lr = v3(0, 0, 0);
         if (!delta) {
@@ -117,7 +121,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
         writeShadow(a, sbase + slot, wi, Lr, tmax, valid);
         nshadow += valid;
       }
-      if (a.ao_light_shadow) {
+      if (ao_light_shadow) {
         bool valid = false;
         V3 wi = v3(0, 0, 0), Lr = v3(0, 0, 0);
         if (a.num_lights > 0) {
@@ -139,7 +143,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
         const int type = (int)L[0];
         const V3 radiance = v3(L[4], L[5], L[6]);
         if (type == 1) {  // hemisphere "diffuse" light (light.h:67-89)
-          for (int s = 0; s < a.ao_samples; ++s, ++slot) {
+          for (int s = 0; s < ao_samples; ++s, ++slot) {
             float u1 = rngNext(st), u2 = rngNext(st);
             V3 wi;
             float pdf;
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
             if (pdf > 0.0f) {
               float costheta = clamp_ref(dot(nff, wi), 0.0f, 1.0f);
               Lr = (Lin * blinnPhong(costheta, surf, ks, a.shininess, radiance, wi, nff, wo)) *
-                   (1.0f / (pdf * (float)a.ao_samples));
+                   (1.0f / (pdf * (float)ao_samples));
               valid = hasPositive(Lr);
             }
             writeShadow(a, sbase + slot, wi, Lr, __int_as_float(0x7f800000), valid);
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
           const V3 nq = cross(e1, e2);
           const float area = sqrtf(dot(nq, nq));
           const V3 nqn = normalize(nq);
-          for (int s = 0; s < a.ao_samples; ++s, ++slot) {
+          for (int s = 0; s < ao_samples; ++s, ++slot) {
             float u1 = rngNext(st), u2 = rngNext(st);
             V3 q = (p0 + e1 * u1) + e2 * u2;
             V3 dv = q - pos;
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
               float pdf = dist2 / (area * cos_l);
               float costheta = clamp_ref(dot(nff, wi), 0.0f, 1.0f);
               Lr = (Lin * blinnPhong(costheta, surf, ks, a.shininess, radiance, wi, nff, wo)) *
-                   (1.0f / (pdf * (float)a.ao_samples));
+                   (1.0f / (pdf * (float)ao_samples));
               valid = hasPositive(Lr);
             }
             writeShadow(a, sbase + slot, wi, Lr, dist, valid);
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
 
     // bounce ray (genR2); the speculation-history wrap of the reference
     // (pending queue at SPRAY_HISTORY_SIZE) does not change the depth count
-    if (next_depth < a.bounces) {
+    if (next_depth < bounces) {
       wo = normalize(wo);
       bool emit = false;
       V3 wi = v3(0, 0, 0), Lr = v3(0, 0, 0);
@@ -259,7 +263,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
         Lr = (((Lin * surf) * kOneOverPi) * costheta) / pdf;
         emit = hasPositive(Lr);
       }
-      if (emit && a.rr_depth > 0 && next_depth >= a.rr_depth) {
+      if (emit && rr_depth > 0 && next_depth >= rr_depth) {
         // Russian roulette (extension): survive with q = min(1, max(Lr)),
         // drawn from its own stream so the reference streams stay untouched
         float q = fmin_ref(1.0f, fmax_ref(Lr.x, fmax_ref(Lr.y, Lr.z)));
@@ -287,27 +291,41 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
   }
 }
 
+void initShadeTables() {
+  float lut[256];
+  for (int i = 0; i < 256; ++i) lut[i] = (float)(i * kOneOver255);
+  cudaMemcpyToSymbol(c_unpack, lut, sizeof(lut));
+}
+
 void launchShade(cudaStream_t s, const ShadeArgs& a, int nblocks) {
-  static bool lut_ready = false;
-  if (!lut_ready) {
-    float lut[256];
-    for (int i = 0; i < 256; ++i) lut[i] = (float)(i * kOneOver255);
-    cudaMemcpyToSymbol(c_unpack, lut, sizeof(lut));
-    lut_ready = true;
-  }
   kShade<<<nblocks, 256, 0, s>>>(a);
 }
 
 // Per pixel of the wave: samples in order, slots in order, each unoccluded
 // shadow ray adds w * (1 / spp) with the double-precision scale of
 // HdrImage::add (src/display/image.h:99-109).
-__global__ void kRetire(float4* image, int64_t npix, int spp, const int32_t* __restrict__ pixid,
+// Per pixel of the wave: its tile (binary search on pix_base), its samples
+// (tile-local pixel lp holds samples lp * spp .. lp * spp + spp - 1), its view's
+// image slot and scale; samples and slots in order, the sum in double.
+__global__ void kRetire(float4* image, const TileDev* __restrict__ tiles, int ntiles, int64_t npix,
+                        const ViewDev* __restrict__ views, const int32_t* __restrict__ pixid,
                         const int32_t* __restrict__ alive_idx, ShadowBuf sh,
-                        const uint8_t* __restrict__ flag, int S, double scale) {
+                        const uint8_t* __restrict__ flag, int S) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
        p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t s0 = p * spp;
-    float4 acc = image[pixid[s0]];
+    int lo = 0, hi = ntiles - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tiles[mid].pix_base <= p) lo = mid;
+      else hi = mid - 1;
+    }
+    const TileDev tl = tiles[lo];
+    const ViewDev& vw = views[tl.view];
+    const int spp = tl.spp;
+    const double scale = vw.scale;
+    const int64_t s0 = tl.sample_base + (p - tl.pix_base) * spp;
+    float4* px = image + vw.pixel_base + pixid[s0];
+    float4 acc = *px;
     bool touched = false;
     for (int s = 0; s < spp; ++s) {
       int32_t ai = alive_idx[s0 + s];
@@ -322,14 +340,14 @@ __global__ void kRetire(float4* image, int64_t npix, int spp, const int32_t* __r
         touched = true;
       }
     }
-    if (touched) image[pixid[s0]] = acc;
+    if (touched) *px = acc;
   }
 }
 
-void launchRetireImpl(cudaStream_t s, float4* image, int64_t npix, int spp, const int32_t* pixid,
-                      const int32_t* alive_idx, const ShadowBuf sh, const uint8_t* flag, int slots,
-                      double scale, int nblocks) {
-  kRetire<<<nblocks, 256, 0, s>>>(image, npix, spp, pixid, alive_idx, sh, flag, slots, scale);
+void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
+                      const ViewDev* views, const int32_t* pixid, const int32_t* alive_idx, const ShadowBuf sh,
+                      const uint8_t* flag, int slots, int nblocks) {
+  kRetire<<<nblocks, 256, 0, s>>>(image, tiles, ntiles, npix, views, pixid, alive_idx, sh, flag, slots);
 }
 
 }  // namespace spray

@@ -333,7 +333,7 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   CK(cudaEventCreate(&ev_start));
   CK(cudaEventCreate(&ev_stop));
   devAlloc(&d_ctr, 1);
-  devAlloc(&d_cam, 1);
+  initShadeTables();
 }
 
 Tracer::~Tracer() {
@@ -342,7 +342,7 @@ Tracer::~Tracer() {
   freeBuffers();
   dropGraph();
   devFree(d_ctr);
-  devFree(d_cam);
+  devFree(d_views);
   for (auto& e : ev_pool) cudaEventDestroy(e);
   if (ev_start) cudaEventDestroy(ev_start);
   if (ev_stop) cudaEventDestroy(ev_stop);
@@ -391,6 +391,8 @@ void Tracer::freeBuffers() {
   }
   devFree(d_pixid);
   devFree(d_samid);
+  devFree(d_view);
+  devFree(d_views);
   devFree(d_alive_list);
   devFree(d_alive_idx);
   devFree(d_alive_count);
@@ -434,11 +436,26 @@ void Tracer::freeBuffers() {
   cap_samples = 0;
 }
 
-int Tracer::slots() const {
-  if (cfg.ao_mode) return cfg.ao_samples + (cfg.ao_light_shadow ? 1 : 0);
+int Tracer::slotsFor(int ao_mode, int ao_samples, int ao_light_shadow) const {
+  if (ao_mode) return ao_samples + (ao_light_shadow ? 1 : 0);
   int s = 0;
-  for (const auto& l : lights) s += (l.type == 0) ? 1 : cfg.ao_samples;
+  for (const auto& l : lights) s += (l.type == 0) ? 1 : ao_samples;
   return s;
+}
+
+// Shadow slots per alive ray: the most any view of the frame needs.
+int Tracer::slots() const {
+  if (fviews.empty()) return slotsFor(cfg.ao_mode, cfg.ao_samples, cfg.ao_light_shadow);
+  int s = 0;
+  for (const FrameView& v : fviews) s = std::max(s, slotsFor(v.ao_mode, v.ao_samples, v.ao_light_shadow));
+  return s;
+}
+
+int Tracer::maxBounces() const {
+  if (fviews.empty()) return cfg.bounces;
+  int b = 0;
+  for (const FrameView& v : fviews) b = std::max(b, v.bounces);
+  return b;
 }
 
 void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_light* ls, int nl) {
@@ -798,8 +815,14 @@ void Tracer::setCamera(const float p[3], const float l[3], const float up[3], fl
 }
 
 void Tracer::planWaves() {
-  tiles = makeTiles(cfg.image_w, cfg.image_h, cfg.pixel_samples, cfg.num_ranks, cfg.rank,
-                    cfg.max_samples_per_rank);
+  // every view's blocking tiles, views in order (ImageScheduleTileList::init per view)
+  tiles.clear();
+  for (size_t v = 0; v < fviews.size(); ++v) {
+    std::vector<HostTile> t = makeTiles(fviews[v].w, fviews[v].h, fviews[v].spp, cfg.num_ranks, cfg.rank,
+                                        cfg.max_samples_per_rank);
+    for (HostTile& h : t) h.view = (int)v;
+    tiles.insert(tiles.end(), t.begin(), t.end());
+  }
   const int S = std::max(slots(), 1);
   int64_t cap = cfg.wave_samples > 0 ? cfg.wave_samples : (int64_t)64 << 20;
   cap = std::min<int64_t>(cap, ((int64_t)1 << kRayIdBits) / S - 1);
@@ -810,25 +833,70 @@ void Tracer::planWaves() {
     w.first_tile = (int)k;
     w.num_tiles = 0;
     w.samples = 0;
+    w.pixels = 0;
     while (k < tiles.size()) {
-      int64_t ts = (int64_t)tiles[k].w * tiles[k].h * cfg.pixel_samples;
+      const int64_t tp = (int64_t)tiles[k].w * tiles[k].h;
+      const int64_t ts = tp * fviews[tiles[k].view].spp;
       if (w.num_tiles > 0 && w.samples + ts > cap) break;
       if (ts >= ((int64_t)1 << kRayIdBits) / S)
         throw std::invalid_argument("a blocking tile holds more rays than one wavefront can address");
       w.samples += ts;
+      w.pixels += tp;
       ++w.num_tiles;
       ++k;
     }
     waves.push_back(w);
   }
   wave_tiles.assign(tiles.size(), TileDev{});
+  uint64_t sig = 1469598103934665603ull;
+  auto mix = [&](uint64_t x) { sig = (sig ^ x) * 1099511628211ull; };
   for (const Wave& w : waves) {
-    int64_t base = 0;
-    for (int k = 0; k < w.num_tiles; ++k) {
-      const HostTile& t = tiles[w.first_tile + k];
-      wave_tiles[w.first_tile + k] = TileDev{t.x, t.y, t.w, t.h, base};
-      base += (int64_t)t.w * t.h * cfg.pixel_samples;
+    int64_t base = 0, pbase = 0;
+    for (int q = 0; q < w.num_tiles; ++q) {
+      const HostTile& t = tiles[w.first_tile + q];
+      const int spp = fviews[t.view].spp;
+      TileDev& td = wave_tiles[w.first_tile + q];
+      td = TileDev{};
+      td.x = t.x;
+      td.y = t.y;
+      td.w = t.w;
+      td.h = t.h;
+      td.sample_base = base;
+      td.pix_base = pbase;
+      td.view = t.view;
+      td.spp = spp;
+      base += (int64_t)t.w * t.h * spp;
+      pbase += (int64_t)t.w * t.h;
+      mix((uint64_t)t.x | ((uint64_t)t.y << 32));
+      mix((uint64_t)t.w | ((uint64_t)t.h << 32));
+      mix((uint64_t)t.view | ((uint64_t)spp << 32));
     }
+    mix((uint64_t)w.num_tiles);
+  }
+  // the view table: image slots back to back, shader settings
+  hviews.assign(fviews.size(), ViewDev{});
+  frame_pixels = 0;
+  for (size_t v = 0; v < fviews.size(); ++v) {
+    const FrameView& f = fviews[v];
+    ViewDev& d = hviews[v];
+    d.cam = f.cam;
+    d.image_w = f.w;
+    d.image_h = f.h;
+    d.spp = f.spp;
+    d.ao_mode = f.ao_mode;
+    d.ao_samples = f.ao_samples;
+    d.bounces = f.bounces;
+    d.rr_depth = f.rr_depth;
+    d.ao_light_shadow = f.ao_light_shadow;
+    d.ao_max_distance = f.ao_max_distance;
+    d.pixel_base = frame_pixels;
+    d.scale = 1.0 / (double)f.spp;
+    frame_pixels += (int64_t)f.w * f.h;
+    mix((uint64_t)f.ao_mode | ((uint64_t)f.bounces << 8) | ((uint64_t)f.ao_samples << 16));
+  }
+  if (sig != plan_sig) {
+    plan_sig = sig;
+    ++buf_gen;  // the captured frame no longer matches
   }
 }
 
@@ -843,7 +911,9 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   sched_chunks = 8 * sched_warps;
   if (chunkSize((uint64_t)1 << kRayIdBits, sched_chunks) >= 65536)
     throw std::runtime_error("too few scheduling chunks for 16-bit histogram counters");
-  if (nsamples <= cap_samples && cap_entries >= needed_entries) return;
+  if (nsamples <= cap_samples && cap_entries >= needed_entries && frame_pixels <= image_cap &&
+      (int64_t)tiles.size() <= tiles_cap && fviews.size() <= views_cap)
+    return;
   freeBuffers();
   ++buf_gen;
   int64_t N = std::max<int64_t>(nsamples, 1024);
@@ -857,9 +927,11 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   }
   devAlloc(&d_pixid, N);
   devAlloc(&d_samid, N);
+  devAlloc(&d_view, N);
   for (int k = 0; k < 2; ++k) {
     rays[k].pixid = d_pixid;
     rays[k].samid = d_samid;
+    rays[k].view = d_view;
   }
   devAlloc(&d_alive_list, N);
   devAlloc(&d_alive_idx, N);
@@ -902,10 +974,14 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_scan_tmp, kMaxScanBlocks);
   compact_blocks = num_sms * 4;
   devAlloc(&d_block_tmp, compact_blocks);
-  devAlloc(&d_image, (size_t)cfg.image_w * cfg.image_h);
+  devAlloc(&d_image, (size_t)std::max<int64_t>(frame_pixels, 1));
+  image_cap = frame_pixels;
+  devAlloc(&d_views, std::max<size_t>(fviews.size(), 1));
+  views_cap = fviews.size();
   devAlloc(&d_scores, D);
   devAlloc(&d_order, D);
   devAlloc(&d_tiles, tiles.size() + 1);
+  tiles_cap = (int64_t)tiles.size();
   cap_samples = N;
   cap_entries = E;
 }
@@ -924,12 +1000,12 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.ray_key = d_ray_key;
   a.dnodes = d_dnodes;
   a.dnode_count = dnode_count;
-  if (primary && use_bins) {
+  if (primary && use_bins && fviews.size() == 1) {
     a.bin_start = d_bin_start;
     a.bin_ids = d_bin_ids;
     a.bins_x = bins_x;
     a.bin_shift = kBinShift;
-    a.image_w = cfg.image_w;
+    a.image_w = fviews[0].w;
   }
   a.arena = d_arena;
   a.arena_top = d_arena_top;
@@ -1016,8 +1092,8 @@ cudaEvent_t Tracer::poolEvent() {
 // Generates the wave's primary rays (tiles and camera are already on the device).
 void Tracer::beginWave(const Wave& w) {
   cur = 0;
-  launchGenPrimary(stream, d_cam, d_tiles + w.first_tile, w.num_tiles, w.samples, cfg.pixel_samples,
-                   cfg.image_w, rays[0], d_alive_list, d_alive_count, d_alive_idx, d_ctr);
+  launchGenPrimary(stream, d_views, d_tiles + w.first_tile, w.num_tiles, w.samples, rays[0], d_alive_list,
+                   d_alive_count, d_alive_idx, d_ctr);
   launches += 1;
 }
 
@@ -1035,12 +1111,7 @@ ShadeArgs Tracer::shadeArgs(int b, int S) {
   sa.shadow_flag = d_shadow_flag;
   sa.slots = S;
   sa.depth = b;
-  sa.ao_mode = cfg.ao_mode;
-  sa.ao_samples = cfg.ao_samples;
-  sa.bounces = cfg.bounces;
-  sa.rr_depth = cfg.rr_depth;
-  sa.ao_light_shadow = cfg.ao_light_shadow;
-  sa.ao_max_distance = cfg.ao_max_distance;
+  sa.views = d_views;
   for (int c = 0; c < 3; ++c) sa.ks[c] = cfg.ks[c];
   sa.shininess = cfg.shininess;
   sa.lights = d_lights;
@@ -1051,14 +1122,14 @@ ShadeArgs Tracer::shadeArgs(int b, int S) {
 
 void Tracer::traceWave(const Wave& w, bool capture) {
   const int S = std::max(slots(), 1);
-  const int spp = cfg.pixel_samples;
+  const int nb_total = maxBounces();
   beginWave(w);
   // non-speculative (policy 4): one pass per list position, so radiance
   // queues are keyed by depth bucket out of core as well
   const bool nonspec = ooc && cfg.schedule_policy == 4;
   const int order_by_depth = (cfg.cull && (!ooc || nonspec)) ? 1 : 0;
   const int nblk = num_sms * 4;
-  for (int b = 0; b < cfg.bounces; ++b) {
+  for (int b = 0; b < nb_total; ++b) {
     if (capture) captureRays(b);
     // radiance rays -> per-domain queues
     if (b == 0 || capture || ooc) {
@@ -1140,12 +1211,11 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     if (capture) captureShadows(b, S);
     // retire
-    int64_t npix = w.samples / spp;
-    launchRetireImpl(stream, d_image, npix, spp, d_pixid, d_alive_idx, sh, d_shadow_flag, S,
-                     1.0 / (double)spp, nblk);
+    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, d_pixid,
+                     d_alive_idx, sh, d_shadow_flag, S, nblk);
     launches += 1;
     // next depth
-    if (b + 1 < cfg.bounces) {
+    if (b + 1 < nb_total) {
       launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count,
                     d_alive_idx, d_block_tmp, compact_blocks);
       launches += 3;
@@ -1414,7 +1484,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int 
 // changes, and hits fold through the order-independent packed atomicMin.
 void Tracer::traceWaveBatched(const Wave& w) {
   const int S = std::max(slots(), 1);
-  const int spp = cfg.pixel_samples;
+  const int nb_total = maxBounces();
   const int nblk = num_sms * 4;
   beginWave(w);
   // radiance queues keyed by depth bucket when culling, so each batch traces
@@ -1434,7 +1504,7 @@ void Tracer::traceWaveBatched(const Wave& w) {
   };
   scheduleRadiance(true);
   oocPass(true, false, S, rb);
-  for (int b = 0; b < cfg.bounces; ++b) {
+  for (int b = 0; b < nb_total; ++b) {
     TraceArgs ta = traceArgs(0, S);
     launchResolve(stream, ta, d_hit_ns, nblk);
     if (learned() && !proposal_trained) collectPairs();
@@ -1445,7 +1515,7 @@ void Tracer::traceWaveBatched(const Wave& w) {
     launches += 5;
     schedule(true, 0, d_shadow_count, d_shadow_list, S, false, true);
     const int32_t* retire_idx = d_alive_idx;
-    const bool more = b + 1 < cfg.bounces;
+    const bool more = b + 1 < nb_total;
     if (more) {
       std::swap(d_alive_idx, d_alive_idx_prev);
       launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count,
@@ -1455,8 +1525,8 @@ void Tracer::traceWaveBatched(const Wave& w) {
       scheduleRadiance(false);
     }
     oocPass(more, true, S, rb);
-    launchRetireImpl(stream, d_image, w.samples / spp, spp, d_pixid, retire_idx, sh, d_shadow_flag, S,
-                     1.0 / (double)spp, nblk);
+    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, d_pixid,
+                     retire_idx, sh, d_shadow_flag, S, nblk);
     launches += 1;
   }
 }
@@ -1635,7 +1705,7 @@ void Tracer::captureFrame() {
   capturing = true;
   try {
     CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
-    CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
+    CK(cudaMemsetAsync(d_image, 0, (size_t)frame_pixels * sizeof(float4), stream));
     for (const Wave& w : waves) traceWave(w, false);
   } catch (...) {
     capturing = false;
@@ -1662,7 +1732,8 @@ void Tracer::captureFrame() {
 // pass the exact slab test of a box whose projection contains its pixel, so
 // the per-bin lists are supersets of what the full test would find.
 void Tracer::buildScreenBins() {
-  const int W = cfg.image_w, H = cfg.image_h;
+  const int W = fviews[0].w, H = fviews[0].h;
+  const CameraDev& cam = fviews[0].cam;
   bins_x = (W + kBinSize - 1) / kBinSize;
   bins_y = (H + kBinSize - 1) / kBinSize;
   const int nb = bins_x * bins_y;
@@ -1747,9 +1818,56 @@ void Tracer::buildScreenBins() {
   h2d_bytes += start.size() * 4 + ids.size() * 2;
 }
 
+// One frame of the configured view (Tracer::trace, ooc_tracer.inl:184-234).
 void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
   if (!has_scene) throw StateError("trace before set_scene");
   if (!has_camera) throw StateError("trace before set_camera");
+  FrameView v;
+  v.cam = cam;
+  v.w = cfg.image_w;
+  v.h = cfg.image_h;
+  v.spp = cfg.pixel_samples;
+  v.ao_mode = cfg.ao_mode;
+  v.ao_samples = cfg.ao_samples;
+  v.bounces = cfg.bounces;
+  v.rr_depth = cfg.rr_depth;
+  v.ao_light_shadow = cfg.ao_light_shadow;
+  v.ao_max_distance = cfg.ao_max_distance;
+  fviews.assign(1, v);
+  traceFrame(out, out_is_device, st);
+}
+
+// Several views in one frame: their tiles share the wavefronts, so every
+// stage runs once per depth for all of them (multi-view batch).
+void Tracer::traceViews(const spray_gpu_view* views, int n, float* out, bool out_is_device, spray_gpu_stats* st) {
+  if (!has_scene) throw StateError("trace before set_scene");
+  if (n <= 0 || n > 65535) throw std::invalid_argument("num_views must be in [1, 65535]");
+  std::vector<FrameView> fv(n);
+  for (int k = 0; k < n; ++k) {
+    const spray_gpu_view& s = views[k];
+    if (s.image_w <= 0 || s.image_h <= 0 || s.pixel_samples <= 0 || s.bounces <= 0 || s.ao_samples <= 0)
+      throw std::invalid_argument("view " + std::to_string(k) + ": sizes, samples and bounces must be positive");
+    if (!s.ao_mode && lights.empty())
+      throw std::invalid_argument("view " + std::to_string(k) + ": path tracing needs at least one light");
+    FrameView& v = fv[k];
+    v.cam = makeCamera(s.position, s.lookat, s.up, s.vfov, s.image_w, s.image_h);
+    v.w = s.image_w;
+    v.h = s.image_h;
+    v.spp = s.pixel_samples;
+    v.ao_mode = s.ao_mode;
+    v.ao_samples = s.ao_samples;
+    v.bounces = s.bounces;
+    v.rr_depth = s.rr_depth;
+    v.ao_light_shadow = s.ao_light_shadow;
+    v.ao_max_distance = s.ao_max_distance;
+    if (slotsFor(v.ao_mode, v.ao_samples, v.ao_light_shadow) > kMaxSlots)
+      throw std::invalid_argument("view " + std::to_string(k) + ": too many shadow rays per hit (max 64)");
+  }
+  fviews.swap(fv);
+  traceFrame(out, out_is_device, st);
+}
+
+void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
   CK(cudaSetDevice(cfg.device));
   planWaves();
   int64_t maxw = 0;
@@ -1769,11 +1887,11 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
     dbg.clear();
     use_pred_order = false;
     CK(cudaEventRecord(ev_start, stream));
-    if (use_bins) buildScreenBins();
-    CK(cudaMemcpyAsync(d_cam, &cam, sizeof(CameraDev), cudaMemcpyHostToDevice, stream));
+    if (use_bins && fviews.size() == 1) buildScreenBins();
+    CK(cudaMemcpyAsync(d_views, hviews.data(), hviews.size() * sizeof(ViewDev), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_tiles, wave_tiles.data(), wave_tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice,
                        stream));
-    h2d_bytes += sizeof(CameraDev) + wave_tiles.size() * sizeof(TileDev);
+    h2d_bytes += hviews.size() * sizeof(ViewDev) + wave_tiles.size() * sizeof(TileDev);
     const bool graphed = cfg.graphs && !ooc && !cfg.debug_capture && !learned();
     if (graphed) {
       if (!graph_exec || graph_gen != buf_gen) captureFrame();
@@ -1784,7 +1902,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       occl_events = graph_occl;
     } else {
       CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
-      CK(cudaMemsetAsync(d_image, 0, (size_t)cfg.image_w * cfg.image_h * sizeof(float4), stream));
+      CK(cudaMemsetAsync(d_image, 0, (size_t)frame_pixels * sizeof(float4), stream));
       for (size_t k = 0; k < waves.size(); ++k) {
         const bool capture = cfg.debug_capture && k == 0;
         if (ooc && (cfg.schedule_policy == 2 || cfg.schedule_policy == 3) && !capture)
@@ -1812,7 +1930,7 @@ void Tracer::trace(float* out, bool out_is_device, spray_gpu_stats* st) {
       pairs_filled = (int64_t)filled;
       if (++frames_collected >= cfg.learn_frames || filled >= pairs_cap) trainProposal();
     }
-    size_t img_bytes = (size_t)cfg.image_w * cfg.image_h * sizeof(float4);
+    size_t img_bytes = (size_t)frame_pixels * sizeof(float4);
     if (out) {
       if (out_is_device) {
         CK(cudaMemcpyAsync(out, d_image, img_bytes, cudaMemcpyDeviceToDevice, stream));
@@ -2149,6 +2267,24 @@ int spray_gpu_trace_device(spray_gpu_tracer* t, float* rgba_dev, spray_gpu_stats
   if (!t) return fail(SPRAY_GPU_EINVAL, "null tracer");
   API_GUARD({
     t->impl->trace(rgba_dev, true, stats);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_trace_views(spray_gpu_tracer* t, const spray_gpu_view* views, int32_t num_views, float* images,
+                          spray_gpu_stats* stats) {
+  if (!t || !views) return fail(SPRAY_GPU_EINVAL, "null argument");
+  API_GUARD({
+    t->impl->traceViews(views, num_views, images, false, stats);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_trace_views_device(spray_gpu_tracer* t, const spray_gpu_view* views, int32_t num_views,
+                                 float* images, spray_gpu_stats* stats) {
+  if (!t || !views) return fail(SPRAY_GPU_EINVAL, "null argument");
+  API_GUARD({
+    t->impl->traceViews(views, num_views, images, true, stats);
     return SPRAY_GPU_OK;
   })
 }

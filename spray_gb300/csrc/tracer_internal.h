@@ -30,12 +30,22 @@ int fail(int code, const std::string& msg);
 
 struct HostTile {
   int x, y, w, h;
+  int view = 0;
 };
 
 struct Wave {
   int first_tile;
   int num_tiles;
   int64_t samples;
+  int64_t pixels;
+};
+
+// One view of a frame (multi-view batches trace several in the same wavefronts).
+struct FrameView {
+  CameraDev cam;
+  int w, h, spp;
+  int ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow;
+  float ao_max_distance;
 };
 
 // A domain prepared for the device: BVH, leaf-ordered triangles and the
@@ -87,11 +97,16 @@ class Tracer {
   void setScenePrepared(const std::string& dir, int nd, const spray_gpu_light* ls, int nl);
   void setCamera(const float p[3], const float l[3], const float up[3], float vfov);
   void trace(float* out, bool out_is_device, spray_gpu_stats* st);
+  // several views in one frame: images back to back in `out`, view order
+  void traceViews(const spray_gpu_view* views, int n, float* out, bool out_is_device, spray_gpu_stats* st);
   int64_t debugCount(int what, int bounce) const;
   const std::vector<char>* debugData(int what, int bounce) const;
 
  private:
   int slots() const;
+  int slotsFor(int ao_mode, int ao_samples, int ao_light_shadow) const;
+  int maxBounces() const;
+  void traceFrame(float* out, bool out_is_device, spray_gpu_stats* st);
   void planWaves();
   void ensureBuffers(int64_t nsamples);
   void freeScene();
@@ -158,7 +173,12 @@ class Tracer {
   float* d_normals = nullptr;
   float* d_lights = nullptr;
   CameraDev cam{};
-  CameraDev* d_cam = nullptr;
+  std::vector<FrameView> fviews;     // the views of the frame being traced
+  std::vector<ViewDev> hviews;
+  ViewDev* d_views = nullptr;
+  size_t views_cap = 0;
+  int64_t frame_pixels = 0, image_cap = 0, tiles_cap = 0;
+  uint64_t plan_sig = 0;             // layout of the planned waves (a change recaptures the graph)
   std::vector<TileDev> wave_tiles;   // every wave's tiles, sample bases relative to the wave
   // in-core frame captured as a CUDA graph; recaptured when buffers change
   cudaGraphExec_t graph_exec = nullptr;
@@ -204,6 +224,7 @@ class Tracer {
   RayBuf rays[2] = {};
   int32_t* d_pixid = nullptr;
   int32_t* d_samid = nullptr;
+  uint16_t* d_view = nullptr;
   uint32_t* d_alive_list = nullptr;
   int32_t* d_alive_idx = nullptr;
   uint32_t* d_alive_count = nullptr;

@@ -493,3 +493,40 @@ def test_non_speculative_order_visits_least(lib_built, scene64):
     (i0, s0), (i4, s4) = out[0], out[4]
     assert np.array_equal(bits(i0), bits(i4))
     assert s4["visits_radiance"] <= s0["visits_radiance"]
+
+
+def _mixed_views(scene):
+    """An uneven batch: different sizes, spp, AO or path tracing, bounces."""
+    specs = [dict(image_w=64, image_h=48, pixel_samples=1, ao_mode=1, ao_samples=4, bounces=1),
+             dict(image_w=96, image_h=64, pixel_samples=4, ao_mode=0, ao_samples=2, bounces=3),
+             dict(image_w=40, image_h=40, pixel_samples=2, ao_mode=0, ao_samples=1, bounces=4, rr_depth=2),
+             dict(image_w=128, image_h=32, pixel_samples=1, ao_mode=1, ao_samples=2, bounces=2,
+                  ao_light_shadow=1)]
+    views = []
+    for k, sp in enumerate(specs):
+        pos, look, up = scenes.orbit_camera(scene, frame=k)
+        views.append(dict(sp, position=pos, lookat=look, up=up, vfov=60.0))
+    return views
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(cache_size=16, schedule_policy=2),
+                                dict(wave_samples=3000, graphs=1)])
+def test_multi_view_batch_matches_single_views(lib_built, kw):
+    """Views of one multi-view frame equal single-view renders of each, bit for bit."""
+    scene = scenes.wavelet_grid(4, 32, colors="albedo", light="point")
+    views = _mixed_views(scene)
+    base = small_config()
+    t = sg.Tracer(base, **kw)
+    t.set_scene(scene)
+    for rep in range(2):  # the second frame replays whatever was captured
+        imgs, st = t.trace_views(views)
+        total_primary = 0
+        for v, img in zip(views, imgs):
+            cfg = dict(base, **{k: v[k] for k in v if k not in ("position", "lookat", "up", "vfov")}, fov=60.0)
+            r = sg.Tracer(cfg, **kw)
+            r.set_scene(scene)
+            r.set_camera(v["position"], v["lookat"], v["up"], 60.0)
+            want, sr = r.trace()
+            assert np.array_equal(bits(img), bits(want)), (rep, v["image_w"])
+            total_primary += sr["rays_primary"]
+        assert st["rays_primary"] == total_primary
