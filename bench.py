@@ -58,6 +58,10 @@ def workload(name: str, scene=None):
 
 def describe(name: str, spec: dict, cfg: dict) -> str:
     g = spec["grid"]
+    if name == "c5":
+        return (f"c5: {g}x{g}x{g} wavelet domains ({spec['samples']}^3 isosurfaces), {spec['views']} views "
+                "of mixed size (256..2048 squared), spp (1, 4, 16) and shader (AO / 4-bounce path tracing) "
+                "in one frame")
     mode = "AO" if cfg.get("ao_mode") else "path tracing"
     return (f"{name}: {g}x{g}x{g} wavelet domains ({spec['samples']}^3 isosurfaces), {mode}, "
             f"{cfg['image_w']}x{cfg['image_h']}, {cfg['pixel_samples']} spp, {cfg['bounces']} bounces")
@@ -172,7 +176,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
     ap.add_argument("--cpu-scale", type=int, default=2, help="CPU baseline frame downscale per axis")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
@@ -251,13 +255,26 @@ def main():
     # weak scaling: each rank renders its own seeded view of the scene
     tracer.set_camera(*scenes.orbit_camera(scene, frame=rank))
     W, H = cfg["image_w"], cfg["image_h"]
-    img_dev = torch.empty(H * W * 4, dtype=torch.float32, device="cuda")
+    views = None
+    if args.config == "c5":
+        # the uneven multi-view batch: every view of the batch traced in one frame
+        views = scenes.c5_views(scene, spec["views"], spec["view_seed"] + rank)
+        if args.scale > 1:
+            for v in views:
+                v["image_w"] = max(8, v["image_w"] // args.scale)
+                v["image_h"] = max(8, v["image_h"] // args.scale)
+        npix = sum(v["image_w"] * v["image_h"] for v in views)
+    else:
+        npix = W * H
+    img_dev = torch.empty(npix * 4, dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MiB > 129 MB L2
 
     def frame_device():
         if not args.no_flush:
             flush.fill_(1)
             torch.cuda.synchronize()
+        if views is not None:
+            return tracer.trace_views_device(views, img_dev.data_ptr())
         return tracer.trace_device(img_dev.data_ptr())
 
     warm = [frame_device() for _ in range(args.warmup)]
@@ -284,8 +301,8 @@ def main():
     value = rays_all / (t_max * 1e-3) / 1e6
 
     # end to end through the C ABI: image to pinned host memory every frame
-    host = torch.empty(H * W * 4, dtype=torch.float32, pin_memory=True)
-    host_np = host.numpy().reshape(H, W, 4)
+    host = torch.empty(npix * 4, dtype=torch.float32, pin_memory=True)
+    host_np = host.numpy().reshape(npix, 1, 4) if views is not None else host.numpy().reshape(H, W, 4)
     e2e_rays, e2e_s, h2d, d2h = 0, 0.0, 0, 0
     barrier()
     for _ in range(args.steps):
@@ -293,7 +310,10 @@ def main():
             flush.fill_(1)
             torch.cuda.synchronize()
         t0 = time.perf_counter()
-        _, st = tracer.trace(host_np)
+        if views is not None:
+            _, st = tracer.trace_views(views)
+        else:
+            _, st = tracer.trace(host_np)
         e2e_s += time.perf_counter() - t0
         e2e_rays += st["rays_primary"] + st["rays_shadow"] + st["rays_bounce"]
         h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
@@ -354,7 +374,12 @@ def main():
     }
     if learn is not None:
         out["learn"] = learn
-    if rank == 0 and not args.no_cpu_baseline:
+    if views is not None:
+        out["config"]["views"] = {"count": len(views), "pixels": npix,
+                                  "samples": sum(v["image_w"] * v["image_h"] * v["pixel_samples"] for v in views),
+                                  "ao_views": sum(1 for v in views if v["ao_mode"]),
+                                  "sizes": sorted({v["image_w"] for v in views})}
+    if rank == 0 and not args.no_cpu_baseline and views is None:
         threads = os.cpu_count() or 1
         r, dt, c, _ = cpu_speculative(args.config, spec, cfg, threads, args.cpu_scale)
         out["cpu_baseline"] = {

@@ -321,14 +321,8 @@ class Tracer:
         _check(lib().spray_gpu_trace(self._h, out.ctypes.data_as(C.c_void_p), C.byref(st)))
         return out, st.asdict()
 
-    def trace_views(self, views: list[dict]) -> tuple[list[np.ndarray], dict]:
-        """Several views in one frame (multi-view batch).  Each view is a dict with
-        position, lookat, up, vfov and any of image_w, image_h, pixel_samples,
-        ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow, ao_max_distance
-        (defaults: this tracer's configuration).  Returns one (H, W, 4) image per
-        view and the frame's stats."""
+    def _view_array(self, views: list[dict]):
         arr = (ViewC * len(views))()
-        shapes = []
         for i, v in enumerate(views):
             c = arr[i]
             c.position = (C.c_float * 3)(*[float(x) for x in v["position"]])
@@ -339,7 +333,23 @@ class Tracer:
                       "ao_light_shadow"):
                 setattr(c, k, int(v.get(k, self.config[k])))
             c.ao_max_distance = float(v.get("ao_max_distance", self.config["ao_max_distance"]))
-            shapes.append((c.image_h, c.image_w))
+        return arr
+
+    def trace_views_device(self, views: list[dict], dev_ptr: int) -> dict:
+        """trace_views into device memory at dev_ptr (the views' images back to back)."""
+        st = StatsC()
+        _check(lib().spray_gpu_trace_views_device(self._h, self._view_array(views), len(views),
+                                                  C.c_void_p(dev_ptr), C.byref(st)))
+        return st.asdict()
+
+    def trace_views(self, views: list[dict]) -> tuple[list[np.ndarray], dict]:
+        """Several views in one frame (multi-view batch).  Each view is a dict with
+        position, lookat, up, vfov and any of image_w, image_h, pixel_samples,
+        ao_mode, ao_samples, bounces, rr_depth, ao_light_shadow, ao_max_distance
+        (defaults: this tracer's configuration).  Returns one (H, W, 4) image per
+        view and the frame's stats."""
+        arr = self._view_array(views)
+        shapes = [(arr[q].image_h, arr[q].image_w) for q in range(len(views))]
         out = np.empty(sum(h * w for h, w in shapes) * 4, np.float32)
         st = StatsC()
         _check(lib().spray_gpu_trace_views(self._h, arr, len(views), out.ctypes.data_as(C.c_void_p), C.byref(st)))

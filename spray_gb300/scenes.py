@@ -48,6 +48,14 @@ CONFIGS = {
                cfg=dict(image_w=2048, image_h=2048, ao_mode=0, ao_samples=1, pixel_samples=8,
                         bounces=4, fov=60.0, list_size=22, cache_size=256),
                ext=dict()),
+    # uneven multi-view batch over the C2 scene: 24 seeded views, resolutions
+    # from {256, 512, 1024, 2048}^2, spp from {1, 4, 16}, half AO-only (8 rays,
+    # max distance 5% of the diagonal, one light ray), half path tracing with
+    # 4 bounces and Russian roulette after bounce 3 (views: c5_views)
+    "c5": dict(grid=4, samples=64, colors="albedo", light="quad", phase_seed=None,
+               cfg=dict(image_w=256, image_h=256, ao_mode=0, ao_samples=1, pixel_samples=1,
+                        bounces=4, fov=60.0),
+               ext=dict(), views=24, view_seed=5),
 }
 
 GREY = 200
@@ -220,3 +228,22 @@ def benchmark_scene(name: str) -> tuple[Path, dict]:
     path = write_wavelet_grid(d, spec["grid"], spec["samples"], spec["colors"], spec["light"],
                               spec["phase_seed"])
     return path, spec
+
+
+def c5_views(scene, n: int = 24, seed: int = 5) -> list[dict]:
+    """The uneven multi-view batch: seeded orbit cameras, sizes, spp and shaders."""
+    rng = np.random.default_rng(seed)
+    diag = scene_diagonal(scene)
+    views = []
+    for k in range(n):
+        pos, look, up = orbit_camera(scene, frame=k)
+        res = int(rng.choice([256, 512, 1024, 2048]))
+        spp = int(rng.choice([1, 4, 16]))
+        v = dict(position=pos, lookat=look, up=up, vfov=60.0, image_w=res, image_h=res, pixel_samples=spp)
+        if k % 2 == 0:
+            v.update(ao_mode=1, ao_samples=8, bounces=1, ao_light_shadow=1, ao_max_distance=0.05 * diag,
+                     rr_depth=0)
+        else:
+            v.update(ao_mode=0, ao_samples=1, bounces=4, rr_depth=3, ao_light_shadow=0, ao_max_distance=0.0)
+        views.append(v)
+    return views
