@@ -46,14 +46,7 @@ NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
 
 def workload(name: str, scene=None):
     from spray_gb300 import scenes
-    spec = scenes.CONFIGS[name]
-    cfg = dict(spec["cfg"])
-    ext = dict(spec["ext"])
-    frac = ext.pop("ao_max_distance_frac", None)
-    if frac is not None and scene is not None:
-        cfg["ao_max_distance"] = frac * scenes.scene_diagonal(scene)
-    cfg.update({k: v for k, v in ext.items() if k != "cache_bytes"})
-    return spec, cfg
+    return scenes.workload_config(name, scene)
 
 
 def describe(name: str, spec: dict, cfg: dict) -> str:
@@ -182,13 +175,15 @@ def main():
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--policy", default="plain", choices=list(POLICIES),
                     help="out-of-core domain order (plain: the reference's DomainStats order)")
-    ap.add_argument("--ooc-batch", type=int, default=0, help="domains per batch under --policy batched")
-    ap.add_argument("--ooc-inplace", type=int, default=16384,
+    ap.add_argument("--ooc-batch", type=int, default=None, help="domains per batch under --policy batched")
+    ap.add_argument("--ooc-inplace", type=int, default=None,
                     help="trace a non-resident domain in place from host memory when a batch holds at "
                          "most this many of its live entries (batched and learned policies)")
     ap.add_argument("--graphs", type=int, default=1, choices=[0, 1],
                     help="1: replay the in-core frame as a captured CUDA graph; 0: direct launches "
                          "(kernel profilers)")
+    ap.add_argument("--tuned", type=int, default=1, choices=[0, 1],
+                    help="apply the committed autotuner result for the workload (spray_gb300/tuned)")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide the image size (profiling captures on a small frame only)")
     args = ap.parse_args()
@@ -244,10 +239,19 @@ def main():
     if args.scale > 1:
         cfg["image_w"] = max(8, cfg["image_w"] // args.scale)
         cfg["image_h"] = max(8, cfg["image_h"] // args.scale)
+    tuned = None
+    if args.tuned:
+        from spray_gb300 import autotune
+        t = autotune.load(args.config)
+        if t:
+            tuned = dict(t["params"])
+            cfg.update(tuned)
     cfg["graphs"] = args.graphs
     cfg["schedule_policy"] = POLICIES[args.policy][0]
-    cfg["ooc_batch"] = args.ooc_batch
-    cfg["ooc_inplace"] = args.ooc_inplace
+    if args.ooc_batch is not None:
+        cfg["ooc_batch"] = args.ooc_batch
+    if args.ooc_inplace is not None:
+        cfg["ooc_inplace"] = args.ooc_inplace
     if args.policy == "learned":
         cfg["learn_frames"] = 1  # collect during the first warm-up frame, train after it
     tracer = sg.Tracer(cfg, device=local)
@@ -352,7 +356,8 @@ def main():
                    "domains": len(scene.domains), "triangles": s0["scene_triangles"],
                    "image": [W, H], "spp": cfg["pixel_samples"], "bounces": cfg["bounces"],
                    "l2": "256 MiB buffer written before every timed frame; ray state > L2",
-                   "parallelism": f"replicas x{world} (one view per GPU)"},
+                   "parallelism": f"replicas x{world} (one view per GPU)",
+                   "tuned": tuned},
         "rays_per_frame": {"primary": s0["rays_primary"], "shadow": s0["rays_shadow"],
                            "bounce": s0["rays_bounce"]},
         "mrays_per_s_by_class": {k: s0[f"rays_{k}"] / (s0["frame_ms"] * 1e-3) / 1e6

@@ -102,6 +102,10 @@ typedef struct spray_gpu_config {
                                    has at most this many live entries in a batch is traced in place
                                    from pinned host memory (read over the host link) instead of
                                    being copied into the cache; 0 = always copy (16384) */
+  /* ---- launch shapes (spray_gb300/autotune.py searches them) ---- */
+  int32_t trace_blocks_per_sm;  /* CTAs of 256 threads per SM in a traversal launch; 0 = 4 */
+  int32_t sched_chunks_per_warp;/* ray chunks (each with a histogram column) per scheduling warp;
+                                   0 = 8 */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as

@@ -323,6 +323,10 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
         "learn_frames >= 1");
   if (cfg.ooc_batch < 0) throw std::invalid_argument("ooc_batch must be >= 0");
   if (cfg.ooc_inplace < 0) throw std::invalid_argument("ooc_inplace must be >= 0");
+  if (cfg.trace_blocks_per_sm < 0 || cfg.trace_blocks_per_sm > 32)
+    throw std::invalid_argument("trace_blocks_per_sm must be in [0, 32]");
+  if (cfg.sched_chunks_per_warp < 0 || cfg.sched_chunks_per_warp > 64)
+    throw std::invalid_argument("sched_chunks_per_warp must be in [0, 64]");
   int ndev = 0;
   CK(cudaGetDeviceCount(&ndev));
   if (cfg.device < 0 || cfg.device >= ndev) throw CudaError("no CUDA device " + std::to_string(cfg.device));
@@ -450,6 +454,9 @@ int Tracer::slots() const {
   for (const FrameView& v : fviews) s = std::max(s, slotsFor(v.ao_mode, v.ao_samples, v.ao_light_shadow));
   return s;
 }
+
+// CTAs of a traversal launch: a multiple of the SM count (persistent warps pull work).
+int Tracer::traceBlocks() const { return num_sms * (cfg.trace_blocks_per_sm > 0 ? cfg.trace_blocks_per_sm : 4); }
 
 int Tracer::maxBounces() const {
   if (fviews.empty()) return cfg.bounces;
@@ -777,8 +784,8 @@ void Tracer::traceOutOfCore(bool shadow, const std::vector<int>& order, int S) {
     ta.nseg = nseg;
     cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
     CK(cudaEventRecord(e0, stream));
-    if (shadow) launchTraceOccluded(stream, ta, num_sms * 4);
-    else launchTraceClosest(stream, ta, num_sms * 4);
+    if (shadow) launchTraceOccluded(stream, ta, traceBlocks());
+    else launchTraceClosest(stream, ta, traceBlocks());
     CK(cudaEventRecord(e1, stream));
     (shadow ? occl_events : trace_events).push_back({e0, e1});
     launches += 1;
@@ -908,7 +915,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   sched_warps = sched_blocks * (kSchedThreads / 32);
   // eight ray chunks per scheduling warp, so that uneven rays balance out;
   // a chunk's per-key counts must fit 16 bits
-  sched_chunks = 8 * sched_warps;
+  sched_chunks = (cfg.sched_chunks_per_warp > 0 ? cfg.sched_chunks_per_warp : 8) * sched_warps;
   if (chunkSize((uint64_t)1 << kRayIdBits, sched_chunks) >= 65536)
     throw std::runtime_error("too few scheduling chunks for 16-bit histogram counters");
   if (nsamples <= cap_samples && cap_entries >= needed_entries && frame_pixels <= image_cap &&
@@ -1173,7 +1180,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
         ta.work = d_work + k;
         cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
         record(t0);
-        launchTraceClosest(stream, ta, num_sms * 4);
+        launchTraceClosest(stream, ta, traceBlocks());
         record(t1);
         trace_events.push_back({t0, t1});
       }
@@ -1204,7 +1211,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       TraceArgs to = traceArgs(0, S);
       cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
       record(o0);
-      launchTraceOccluded(stream, to, num_sms * 4);
+      launchTraceOccluded(stream, to, traceBlocks());
       record(o1);
       occl_events.push_back({o0, o1});
       launches += 1;
@@ -1455,8 +1462,8 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int 
       ta.nseg = nseg[q];
       cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
       CK(cudaEventRecord(e0, stream));
-      if (shadow) launchTraceOccluded(stream, ta, num_sms * 4);
-      else launchTraceClosest(stream, ta, num_sms * 4);
+      if (shadow) launchTraceOccluded(stream, ta, traceBlocks());
+      else launchTraceClosest(stream, ta, traceBlocks());
       CK(cudaEventRecord(e1, stream));
       (shadow ? occl_events : trace_events).push_back({e0, e1});
       launches += 1;

@@ -106,6 +106,7 @@ class Tracer {
   int slots() const;
   int slotsFor(int ao_mode, int ao_samples, int ao_light_shadow) const;
   int maxBounces() const;
+  int traceBlocks() const;
   void traceFrame(float* out, bool out_is_device, spray_gpu_stats* st);
   void planWaves();
   void ensureBuffers(int64_t nsamples);

@@ -247,3 +247,16 @@ def c5_views(scene, n: int = 24, seed: int = 5) -> list[dict]:
             v.update(ao_mode=0, ao_samples=1, bounces=4, rr_depth=3, ao_light_shadow=0, ao_max_distance=0.0)
         views.append(v)
     return views
+
+
+def workload_config(name: str, scene=None) -> tuple[dict, dict]:
+    """(spec, tracer configuration) of a benchmark workload; the AO range is a
+    fraction of the scene diagonal, so it needs the scene."""
+    spec = CONFIGS[name]
+    cfg = dict(spec["cfg"])
+    ext = dict(spec["ext"])
+    frac = ext.pop("ao_max_distance_frac", None)
+    if frac is not None and scene is not None:
+        cfg["ao_max_distance"] = frac * scene_diagonal(scene)
+    cfg.update({k: v for k, v in ext.items() if k != "cache_bytes"})
+    return spec, cfg
