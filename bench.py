@@ -67,7 +67,7 @@ def clock_sampler(out: Path):
     try:
         f = open(out, "w")
         return subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                 "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL), f
+                                 "-lms", "100"], stdout=f, stderr=subprocess.DEVNULL), f
     except Exception:
         return None, None
 
@@ -166,7 +166,7 @@ def run_reference(args, spec, cfg, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
