@@ -106,6 +106,9 @@ typedef struct spray_gpu_config {
   int32_t trace_blocks_per_sm;  /* CTAs of 256 threads per SM in a traversal launch; 0 = 4 */
   int32_t sched_chunks_per_warp;/* ray chunks (each with a histogram column) per scheduling warp;
                                    0 = 8 */
+  int32_t bucket_launches;      /* in core with culling: closest-hit launches per depth, 1 = one
+                                   launch over the depth buckets in order (fastest), 4 = one per
+                                   bucket (visit counts repeat exactly); 0 = 1 (0) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as

@@ -323,6 +323,8 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
         "learn_frames >= 1");
   if (cfg.ooc_batch < 0) throw std::invalid_argument("ooc_batch must be >= 0");
   if (cfg.ooc_inplace < 0) throw std::invalid_argument("ooc_inplace must be >= 0");
+  if (cfg.bucket_launches != 0 && cfg.bucket_launches != 1 && cfg.bucket_launches != kDepthBuckets)
+    throw std::invalid_argument("bucket_launches must be 0, 1 or 4");
   if (cfg.trace_blocks_per_sm < 0 || cfg.trace_blocks_per_sm > 32)
     throw std::invalid_argument("trace_blocks_per_sm must be in [0, 32]");
   if (cfg.sched_chunks_per_warp < 0 || cfg.sched_chunks_per_warp > 64)
@@ -1174,9 +1176,13 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       }
     } else {
       CK(cudaMemsetAsync(d_work, 0, 4 * kDepthBuckets, stream));
-      const int nb = order_by_depth ? kDepthBuckets : 1;
+      // entries are sorted bucket-major, so one launch that walks them in order
+      // still traces nearer list positions first; a launch per bucket makes
+      // every nearer hit visible to the culling test, so visit counts repeat
+      // exactly from frame to frame (the image is the same either way)
+      const int nb = (order_by_depth && cfg.bucket_launches == kDepthBuckets) ? kDepthBuckets : 1;
       for (int k = 0; k < nb; ++k) {
-        ta.bucket = order_by_depth ? k : -1;
+        ta.bucket = nb == kDepthBuckets ? k : -1;
         ta.work = d_work + k;
         cudaEvent_t t0 = poolEvent(), t1 = poolEvent();
         record(t0);

@@ -63,7 +63,8 @@ def test_invalid_config_rejected(lib_built):
 @pytest.mark.parametrize("kw", [dict(schedule_policy=5), dict(schedule_policy=-1), dict(ooc_batch=-1),
                                 dict(schedule_policy=3, learn_batch=0), dict(schedule_policy=3, learn_lr=0.0),
                                 dict(schedule_policy=3, learn_frames=0), dict(ooc_inplace=-1),
-                                dict(trace_blocks_per_sm=33), dict(sched_chunks_per_warp=-1)])
+                                dict(trace_blocks_per_sm=33), dict(sched_chunks_per_warp=-1),
+                                dict(bucket_launches=2)])
 def test_out_of_core_options_validated(lib_built, kw):
     """Options are checked before any device is touched."""
     import spray_gb300 as sg

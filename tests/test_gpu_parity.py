@@ -215,26 +215,35 @@ def test_waves_and_culling_do_not_change_the_image(lib_built, oracle_mod, scene6
                        max_samples_per_rank=2048)
     cam = scenes.orbit_camera(scene64)
     imgs = []
-    for kw in (dict(cull=1), dict(cull=0), dict(cull=1, wave_samples=3000), dict(cull=0, wave_samples=2048)):
+    for kw in (dict(cull=1, bucket_launches=4), dict(cull=0), dict(cull=1, wave_samples=3000, bucket_launches=4),
+               dict(cull=0, wave_samples=2048), dict(cull=1)):
         t = sg.Tracer(cfg, **kw)
         t.set_scene(scene64)
         t.set_camera(*cam)
         img, st = t.trace()
         imgs.append(img)
-        if kw["cull"]:
-            assert st["visits_culled"] > 0
+        if kw.get("bucket_launches") == 4:
+            assert st["visits_culled"] > 0  # one launch per bucket: nearer hits always seen
     for im in imgs[1:]:
         assert np.array_equal(bits(im), bits(imgs[0]))
 
 
-def test_deterministic_frames(lib_built, scene64):
-    t = sg.Tracer(small_config(image_w=64, image_h=64, ao_mode=0, pixel_samples=2, bounces=2))
+@pytest.mark.parametrize("launches", [1, 4])
+def test_deterministic_frames(lib_built, scene64, launches):
+    """Images and ray counts repeat exactly; with one launch per depth bucket the
+    visit counts do too."""
+    t = sg.Tracer(small_config(image_w=64, image_h=64, ao_mode=0, pixel_samples=2, bounces=2),
+                  bucket_launches=launches)
     t.set_scene(scene64)
     t.set_camera(*scenes.orbit_camera(scene64))
     a, sa = t.trace()
     b, sb = t.trace()
     assert np.array_equal(bits(a), bits(b))
-    for k in ("rays_primary", "rays_shadow", "rays_bounce", "visits_radiance", "visits_shadow"):
+    keys = ["rays_primary", "rays_shadow", "rays_bounce", "visits_shadow"]
+    if launches == 4:
+        keys.append("visits_radiance")
+        assert sa["trace_launches"] == 4 * 2
+    for k in keys:
         assert sa[k] == sb[k]
 
 
@@ -317,7 +326,7 @@ def test_out_of_core_cache_gives_the_in_core_image(lib_built, scene64, kw):
     """Streaming domains through a small LRU cache changes loads, never the image."""
     cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3)
     cam = scenes.orbit_camera(scene64)
-    ref = sg.Tracer(cfg)
+    ref = sg.Tracer(cfg, bucket_launches=4)
     ref.set_scene(scene64)
     ref.set_camera(*cam)
     want, st0 = ref.trace()
@@ -439,7 +448,8 @@ def test_trained_proposal_gains_over_untrained(lib_built):
 def test_graph_replay_follows_camera_and_matches_direct_launches(lib_built, scene64):
     """The in-core frame captured as a CUDA graph renders what direct launches
     render, across camera moves and several wavefronts per frame."""
-    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3, wave_samples=5000)
+    cfg = small_config(image_w=96, image_h=64, ao_mode=0, pixel_samples=2, bounces=3, wave_samples=5000,
+                       bucket_launches=4)
     tg = sg.Tracer(cfg, graphs=1)
     td = sg.Tracer(cfg, graphs=0)
     for t in (tg, td):
