@@ -283,6 +283,11 @@ void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, u
                    uint32_t* block_tmp, int nblocks);
 // Adds the unoccluded shadow rays of every pixel of a wave (npix pixels over
 // ntiles tiles) to the frame image, samples of a pixel in order.
+// Stable compaction of a list: keeps src[i] (i < *n_dev) where flag[src[i]] is
+// set, in order, into list and count; index_of[src[i]] = new position or -1.
+// list must not alias src.
+void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,
+                       uint32_t* list, uint32_t* count, int32_t* index_of, uint32_t* block_tmp, int nblocks);
 void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
                       const ViewDev* views, const int32_t* pixid, const int32_t* alive_idx,
                       const ShadowBuf sh, const uint8_t* flag, int slots, int nblocks);

@@ -514,13 +514,14 @@ void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int D, int nwarps,
 
 // ---------------------------------------------------------------- compaction
 __global__ void kCompactCount(const uint8_t* __restrict__ flag, const uint32_t* n_dev,
-                              uint32_t n_mul, uint64_t n_host, uint32_t* block_tmp) {
+                              uint32_t n_mul, uint64_t n_host, uint32_t* block_tmp,
+                              const uint32_t* __restrict__ src) {
   __shared__ uint32_t ws[32];
   const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
   const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
   const uint64_t b0 = min(n, per * blockIdx.x), b1 = min(n, b0 + per);
   uint32_t c = 0;
-  for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) c += flag[i] != 0;
+  for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) c += flag[src ? src[i] : i] != 0;
   for (int o = 16; o; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
   __syncthreads();
@@ -557,7 +558,7 @@ __global__ void __launch_bounds__(1024) kCompactScan(uint32_t* block_tmp, int nb
 
 __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* n_dev,
                               uint32_t n_mul, uint64_t n_host, const uint32_t* block_tmp,
-                              uint32_t* list, int32_t* index_of) {
+                              uint32_t* list, int32_t* index_of, const uint32_t* __restrict__ src) {
   __shared__ uint32_t ws[33];
   const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
   const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
@@ -567,7 +568,8 @@ __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* 
   const uint32_t lt = laneMaskLt();
   for (uint64_t s = b0; s < b1; s += blockDim.x) {
     const uint64_t i = s + threadIdx.x;
-    const bool f = i < b1 && flag[i] != 0;
+    const uint32_t id = i < b1 ? (src ? src[i] : (uint32_t)i) : 0u;
+    const bool f = i < b1 && flag[id] != 0;
     const uint32_t bal = __ballot_sync(0xffffffffu, f);
     if (lane == 0) ws[w] = __popc(bal);
     __syncthreads();
@@ -584,10 +586,10 @@ __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* 
     if (i < b1) {
       if (f) {
         uint32_t p = base + ws[w] + __popc(bal & lt);
-        list[p] = (uint32_t)i;
-        if (index_of) index_of[i] = (int32_t)p;
+        list[p] = id;
+        if (index_of) index_of[id] = (int32_t)p;
       } else if (index_of) {
-        index_of[i] = -1;
+        index_of[id] = -1;
       }
     }
     base += ws[32];
@@ -598,9 +600,16 @@ __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* 
 void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
                    uint64_t n_host, uint32_t* list, uint32_t* count, int32_t* index_of,
                    uint32_t* block_tmp, int nblocks) {
-  kCompactCount<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp);
+  kCompactCount<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp, nullptr);
   kCompactScan<<<1, 1024, 0, s>>>(block_tmp, nblocks, count);
-  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp, list, index_of);
+  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp, list, index_of, nullptr);
+}
+
+void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,
+                       uint32_t* list, uint32_t* count, int32_t* index_of, uint32_t* block_tmp, int nblocks) {
+  kCompactCount<<<nblocks, 256, 0, s>>>(flag, n_dev, 1, 0, block_tmp, src);
+  kCompactScan<<<1, 1024, 0, s>>>(block_tmp, nblocks, count);
+  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, 1, 0, block_tmp, list, index_of, src);
 }
 
 // ---------------------------------------------------------------- scores

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t sample = a.list[i];
     const uint64_t key = a.ray_key[sample];
+    a.next_flag[sample] = 0;  // set below when a bounce ray is emitted
     const uint32_t sbase = (uint32_t)i * S;
     if (key == kNoHit) {
       for (int s = 0; s < S; ++s) a.shadow_flag[sbase + s] = 0;

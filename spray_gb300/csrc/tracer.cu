@@ -400,6 +400,8 @@ void Tracer::freeBuffers() {
   devFree(d_view);
   devFree(d_views);
   devFree(d_alive_list);
+  devFree(d_alive_list2);
+  devFree(d_alive_count2);
   devFree(d_alive_idx);
   devFree(d_alive_count);
   devFree(d_next_flag);
@@ -943,6 +945,8 @@ void Tracer::ensureBuffers(int64_t nsamples) {
     rays[k].view = d_view;
   }
   devAlloc(&d_alive_list, N);
+  devAlloc(&d_alive_list2, N);
+  devAlloc(&d_alive_count2, 1);
   devAlloc(&d_alive_idx, N);
   devAlloc(&d_alive_count, 1);
   devAlloc(&d_next_flag, N);
@@ -1197,8 +1201,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     if (learned() && !proposal_trained) collectPairs();
     if (capture) captureHits(b);
     // shade
-    CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
-    launchShade(stream, shadeArgs(b, S), nblk);
+    launchShade(stream, shadeArgs(b, S), nblk);  // writes the next-depth flag of every alive ray
     launches += 1;
     // shadow rays -> queues -> occlusion
     launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
@@ -1229,8 +1232,12 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     launches += 1;
     // next depth
     if (b + 1 < nb_total) {
-      launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count,
-                    d_alive_idx, d_block_tmp, compact_blocks);
+      // compact this depth's alive list (not every sample of the wave): samples
+      // that stop get index -1, the ones dead before keep theirs (-1)
+      launchCompactList(stream, d_alive_list, d_alive_count, d_next_flag, d_alive_list2, d_alive_count2,
+                        d_alive_idx, d_block_tmp, compact_blocks);
+      std::swap(d_alive_list, d_alive_list2);
+      std::swap(d_alive_count, d_alive_count2);
       launches += 3;
       cur ^= 1;
     }

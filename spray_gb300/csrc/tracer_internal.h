@@ -227,6 +227,8 @@ class Tracer {
   int32_t* d_samid = nullptr;
   uint16_t* d_view = nullptr;
   uint32_t* d_alive_list = nullptr;
+  uint32_t* d_alive_list2 = nullptr;   // in core: the next depth's alive list (ping-pong)
+  uint32_t* d_alive_count2 = nullptr;
   int32_t* d_alive_idx = nullptr;
   uint32_t* d_alive_count = nullptr;
   uint8_t* d_next_flag = nullptr;
