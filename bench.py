@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -289,8 +290,7 @@ def main():
                  "pairs": warm[-1]["learn_pairs"] if warm else 0,
                  "train_ms": w0["learn_ms"] if w0 else None, "loss": w0["learn_loss"] if w0 else None}
 
-    clk_path = ROOT / "gpurun_out" / f"clocks_rank{rank}.csv"
-    clk_path.parent.mkdir(exist_ok=True)
+    clk_path = Path(tempfile.gettempdir()) / f"spray_bench_clocks_rank{rank}_{os.getpid()}.csv"
     proc, fh = clock_sampler(clk_path)
     barrier()
     torch.cuda.synchronize()
