@@ -1,6 +1,7 @@
 """Oracle known-answer tests: RNG, sin/cos, slab test, triangle test, LRU
 cache, blocking tiles, and mode A (speculative loop) vs mode B (wavefront)."""
 import math
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -199,3 +200,27 @@ def test_ao_of_open_plane_is_vertex_color(oracle_mod):
     px = img[..., :3].astype(np.float64)
     assert np.all(px <= hi * (1 + 3e-6)) and np.all(px >= lo * (1 - 3e-6))
     assert np.mean(np.abs(px - hi) <= hi * 3e-6) > 0.8
+
+
+REF_RNG = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "libref_rng.so"
+
+
+@pytest.mark.skipif(not REF_RNG.exists(), reason="reference sampler not built (reference tree absent)")
+def test_rng_matches_the_reference_sampler():
+    """The oracle's sampler equals the reference's own RandomSampler
+    (deps/embree/random_sampler.h, built by oracle/build_ref.sh), bit for bit,
+    for the seed forms the tracer uses: tile-local sample ids (eye jitter),
+    pixel * (l + 1) (AO), sample * depth (bounces) and their wrap-arounds."""
+    import ctypes as C
+    from oracle import oracle as O
+    L = C.CDLL(str(REF_RNG))
+    L.ref_rng.argtypes = [C.c_int32, C.c_int32, C.c_void_p]
+    rng = np.random.default_rng(3)
+    seeds = [0, 1, -1, 2 ** 31 - 1, -(2 ** 31)] + list(rng.integers(-(2 ** 31), 2 ** 31, 200))
+    seeds += [p * (l + 1) for p in (0, 5, 1919, 2073599) for l in range(8)]
+    for seed in seeds:
+        seed = int(np.int32(np.int64(seed) & 0xFFFFFFFF if seed >= 0 else seed))
+        want = np.zeros(16, np.float32)
+        L.ref_rng(seed, 16, want.ctypes.data)
+        got = O.rng_floats(seed, 16)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), seed
