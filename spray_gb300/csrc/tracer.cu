@@ -373,6 +373,7 @@ void Tracer::freeScene() {
   devFree(d_bin_start);
   devFree(d_bin_ids);
   bin_start_cap = bin_ids_cap = 0;
+  bins_key.clear();  // new domain boxes
   devFree(d_domains);
   devFree(d_nodes);
   devFree(d_tris);
@@ -1754,6 +1755,14 @@ void Tracer::captureFrame() {
 void Tracer::buildScreenBins() {
   const int W = fviews[0].w, H = fviews[0].h;
   const CameraDev& cam = fviews[0].cam;
+  // the bins depend only on the camera, the image size and the domain boxes:
+  // unchanged since the last build, the device copy is still current
+  std::vector<unsigned char> key(sizeof(CameraDev) + 2 * sizeof(int));
+  std::memcpy(key.data(), &cam, sizeof(CameraDev));
+  std::memcpy(key.data() + sizeof(CameraDev), &W, sizeof(int));
+  std::memcpy(key.data() + sizeof(CameraDev) + sizeof(int), &H, sizeof(int));
+  if (key == bins_key && d_bin_start && d_bin_ids) return;
+  bins_key = key;
   bins_x = (W + kBinSize - 1) / kBinSize;
   bins_y = (H + kBinSize - 1) / kBinSize;
   const int nb = bins_x * bins_y;

@@ -206,6 +206,7 @@ class Tracer {
   static constexpr int kBinShift = 4;
   static constexpr int kBinSize = 1 << kBinShift;
   bool use_bins = true;
+  std::vector<unsigned char> bins_key;  // camera and image the current bins were built for
   int bins_x = 0, bins_y = 0;
   uint32_t* d_bin_start = nullptr;
   uint16_t* d_bin_ids = nullptr;
