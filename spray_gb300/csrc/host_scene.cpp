@@ -267,7 +267,7 @@ void readPly(const std::string& filename, Mesh* mesh) {
   int elem = -1;  // 0 vertex, 1 face
   int order[2] = {-1, -1};
   int nelem = 0;
-  int vtype = T_UNDEF, ctype = T_UNDEF, ltype = T_UNDEF, itype = T_UNDEF;
+  int vtype = T_UNDEF, ltype = T_UNDEF, itype = T_UNDEF;
   bool has_color = false;
   int ncolor = 0, npos = 0;
   bool end_header = false;
@@ -302,7 +302,6 @@ void readPly(const std::string& filename, Mesh* mesh) {
         } else if (name == "red" || name == "green" || name == "blue") {
           int t = plyType(dt);
           if (t != T_UCHAR) throw std::runtime_error(filename + ": colors must be uchar");
-          ctype = t;
           ++ncolor;
           has_color = true;
         } else {
