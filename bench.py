@@ -243,7 +243,7 @@ def main():
     tuned = None
     if args.tuned:
         from spray_gb300 import autotune
-        t = autotune.load(args.config)
+        t = autotune.load(args.config, POLICIES[args.policy][0])
         if t:
             tuned = dict(t["params"])
             cfg.update(tuned)

@@ -12,8 +12,9 @@ frames after `warmup`) and runs coordinate descent over
                          and the in-place tracing threshold
 
 starting from the library defaults.  The result goes to
-`spray_gb300/tuned/<workload>.json`, which bench.py applies; every trial is
-kept in the file.  Images do not depend on these settings.
+`spray_gb300/tuned/<workload>.json` (`<workload>_policy<p>.json` when tuned
+for a schedule policy other than the workload's), which bench.py applies;
+every trial is kept in the file.  Images do not depend on these settings.
 
     python -m spray_gb300.autotune --config c2
 """
@@ -37,13 +38,19 @@ OOC_SPACE = {
 }
 
 
-def load(name: str) -> dict | None:
-    """The committed tuning of a workload, or None."""
-    p = TUNED / f"{name}.json"
-    try:
-        return json.loads(p.read_text())
-    except Exception:
-        return None
+def _path(name: str, policy: int | None) -> Path:
+    return TUNED / (f"{name}.json" if policy is None else f"{name}_policy{policy}.json")
+
+
+def load(name: str, policy: int | None = None) -> dict | None:
+    """The committed tuning of a workload for a schedule policy (falling back
+    to the workload's own), or None."""
+    for p in ([_path(name, policy)] if policy is not None else []) + [_path(name, None)]:
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            continue
+    return None
 
 
 def _frame_ms(scene, cfg: dict, cam, frames: int, warmup: int) -> float:
@@ -102,7 +109,7 @@ def tune(name: str, frames: int = 3, warmup: int = 2, policy: int | None = None,
         pass
     if write:
         TUNED.mkdir(exist_ok=True)
-        (TUNED / f"{name}.json").write_text(json.dumps(out, indent=1) + "\n")
+        _path(name, policy).write_text(json.dumps(out, indent=1) + "\n")
     return out
 
 
