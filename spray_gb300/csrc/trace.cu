@@ -48,12 +48,12 @@ __device__ __forceinline__ TravRay makeTravRay(V3 org, V3 dir) {
 __device__ __forceinline__ int testChildren(const BvhNode4* __restrict__ nodes, int node,
                                             const TravRay& r, float tnear, float tfar,
                                             float tn[4]) {
+  // the node stores lo/hi per axis as float4 pairs; the ray's signs pick the
+  // near and far plane of each pair by address
   const float4* p = reinterpret_cast<const float4*>(nodes + node);
-  const float4 lox = __ldg(p + 0), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
-  const float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
-  const float4 nx = r.sx ? hix : lox, fx = r.sx ? lox : hix;
-  const float4 ny = r.sy ? hiy : loy, fy = r.sy ? loy : hiy;
-  const float4 nz = r.sz ? hiz : loz, fz = r.sz ? loz : hiz;
+  const float4 nx = __ldg(p + r.sx), fx = __ldg(p + (r.sx ^ 1));
+  const float4 ny = __ldg(p + 2 + r.sy), fy = __ldg(p + (3 - r.sy));
+  const float4 nz = __ldg(p + 4 + r.sz), fz = __ldg(p + (5 - r.sz));
   const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
   const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
   const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
@@ -129,14 +129,21 @@ __device__ __forceinline__ Walk startWalk(const SceneDev& sc, const DomainDev& d
 __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const TravRay& r,
                                 uint64_t& best_key, float& best_t, uint32_t& best_prim,
                                 float& best_u, float& best_v, Counters* ctr,
-                                unsigned long long& nnodes, unsigned long long& ntris) {
+                                uint32_t& nnodes, uint32_t& ntris) {
   const DomArrays g = domArrays(sc, dom);
   const BvhNode4* nodes = g.nodes;
   const float4* tris = g.tris;
   uint2 stack[kStack];
   int sp = 0;
   bool found = false;
-  int steps = 0;
+  // node and triangle counts of this walk (32 bits: a walk is bounded by
+  // kMaxSteps); the node count is also the step bound's counter
+  uint32_t steps = 0, tested = 0;
+  auto finish = [&]() {
+    nnodes += steps;
+    ntris += tested;
+    return found;
+  };
   auto pop = [&]() -> int {
     while (sp > 0) {
       const uint2 e = stack[--sp];
@@ -148,38 +155,55 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
   while (cur != kDone) {
     // inner nodes until the nearest pending entry is a leaf
     while (cur >= 0) {
-      if (++steps > kMaxSteps) {
+      if (++steps > (uint32_t)kMaxSteps) {
         raise(ctr, kErrTraversalBound);
-        return found;
+        return finish();
       }
       if ((unsigned)cur >= (unsigned)dom.num_nodes) {
         raise(ctr, kErrBadNode);
-        return found;
+        return finish();
       }
       float tn[4];
-      ++nnodes;
       const int mask = testChildren(nodes, cur, r, kRayEpsilon, best_t, tn);
       const int4 ch = loadChildren(nodes, cur);
-      int ord[4], no = 0;
+      // Children sorted near to far by a key of the entry t with its two low
+      // bits replaced by the slot: t >= tnear > 0, so the bits order like the
+      // value, and the key's t (rounded down by at most 3 ulp) stays a lower
+      // bound of the entry.  A five-comparator network keeps it in registers.
+      uint32_t k[4];
+#pragma unroll
       for (int c = 0; c < 4; ++c)
-        if ((mask & (1 << c)) && childAt(ch, c) != kEmptyChild) {
-          int j = no++;
-          while (j > 0 && tn[ord[j - 1]] > tn[c]) {
-            ord[j] = ord[j - 1];
-            --j;
+        k[c] = ((mask & (1 << c)) && childAt(ch, c) != kEmptyChild)
+                   ? (__float_as_uint(tn[c]) & ~3u) | (uint32_t)c
+                   : 0xffffffffu;
+      auto cswap = [](uint32_t& x, uint32_t& y) {
+        const uint32_t lo = min(x, y), hi = max(x, y);
+        x = lo;
+        y = hi;
+      };
+      cswap(k[0], k[1]);
+      cswap(k[2], k[3]);
+      cswap(k[0], k[2]);
+      cswap(k[1], k[3]);
+      cswap(k[1], k[2]);
+      // The nearest child continues the walk when it starts within the best
+      // hit; the others go on the stack far to near.  Every other child starts
+      // at least as far as the nearest, so when the nearest is beyond the best
+      // hit all of them are (pop would drop them) and the walk pops instead.
+      if (k[0] != 0xffffffffu && __uint_as_float(k[0] & ~3u) <= best_t) {
+#pragma unroll
+        for (int j = 3; j >= 1; --j) {
+          if (k[j] == 0xffffffffu) continue;
+          if (sp == kStack) {
+            raise(ctr, kErrTraversalBound);
+            return finish();
           }
-          ord[j] = c;
+          stack[sp++] = make_uint2((uint32_t)childAt(ch, (int)(k[j] & 3u)), k[j] & ~3u);
         }
-      // far to near, so the nearest child is on top
-      for (int k = no - 1; k >= 0; --k) {
-        if (sp == kStack) {
-          raise(ctr, kErrTraversalBound);
-          return found;
-        }
-        const int c = ord[k];
-        stack[sp++] = make_uint2((uint32_t)childAt(ch, c), __float_as_uint(tn[c]));
+        cur = childAt(ch, (int)(k[0] & 3u));
+      } else {
+        cur = pop();
       }
-      cur = pop();
     }
     if (cur == kDone) break;
     // leaf
@@ -187,9 +211,9 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
     const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
     if (first + cnt > (uint32_t)dom.num_tris) {
       raise(ctr, kErrBadNode);
-      return found;
+      return finish();
     }
-    ntris += cnt;
+    tested += cnt;
     for (uint32_t q = 0; q < cnt; ++q) {
       const float4* tp = tris + 3 * (size_t)(first + q);
       const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
@@ -210,7 +234,7 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
     }
     cur = pop();
   }
-  return found;
+  return finish();
 }
 
 // Any hit in (tnear, tfar), the same rounds.  Returns true when the walk has
@@ -233,17 +257,24 @@ __device__ __forceinline__ bool anyRound(Walk& w, int* stack, const TravRay& r, 
     ++nnodes;
     const int mask = testChildren(w.nodes, w.cur, r, kRayEpsilon, tfar, tn);
     const int4 ch = loadChildren(w.nodes, w.cur);
+    // the last child hit continues the walk; the earlier ones are pushed
+    // (the order a push of all of them and a pop would give)
+    int next = kDone;
+#pragma unroll
     for (int c = 0; c < 4; ++c) {
       if (!(mask & (1 << c))) continue;
       const int ref = childAt(ch, c);
       if (ref == kEmptyChild) continue;
-      if (w.sp == kStack) {
-        raise(ctr, kErrTraversalBound);
-        return true;
+      if (next != kDone) {
+        if (w.sp == kStack) {
+          raise(ctr, kErrTraversalBound);
+          return true;
+        }
+        stack[w.sp++] = next;
       }
-      stack[w.sp++] = ref;
+      next = ref;
     }
-    w.cur = w.sp > 0 ? stack[--w.sp] : kDone;
+    w.cur = next != kDone ? next : (w.sp > 0 ? stack[--w.sp] : kDone);
   }
   if (w.cur == kDone) return true;
   const uint32_t v = ~(uint32_t)w.cur;
@@ -326,7 +357,9 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
     E = a.bucket + 1 < kDepthBuckets ? skeys[(a.bucket + 1) * D] : skeys[a.nkeys];
   }
   const int lane = threadIdx.x & 31;
-  unsigned long long visits = 0, culled = 0, nnodes = 0, ntris = 0;
+  // per-thread counts in 32 bits (entries are 32-bit indices); node and
+  // triangle counts go to the global counters before they could wrap
+  uint32_t visits = 0, culled = 0, nnodes = 0, ntris = 0;
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = E0 + atomicAdd(a.work, 32u);
@@ -375,18 +408,24 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
     } else {
       a.rec_key[e] = kNoHit;
     }
+    if ((nnodes | ntris) & 0x80000000u) {
+      atomicAdd(&a.ctr->nodes_radiance, (unsigned long long)nnodes);
+      atomicAdd(&a.ctr->tris_radiance, (unsigned long long)ntris);
+      nnodes = ntris = 0;
+    }
   }
+  unsigned long long sv = visits, sc = culled, sn = nnodes, st = ntris;
   for (int o = 16; o; o >>= 1) {
-    visits += __shfl_down_sync(0xffffffffu, visits, o);
-    culled += __shfl_down_sync(0xffffffffu, culled, o);
-    nnodes += __shfl_down_sync(0xffffffffu, nnodes, o);
-    ntris += __shfl_down_sync(0xffffffffu, ntris, o);
+    sv += __shfl_down_sync(0xffffffffu, sv, o);
+    sc += __shfl_down_sync(0xffffffffu, sc, o);
+    sn += __shfl_down_sync(0xffffffffu, sn, o);
+    st += __shfl_down_sync(0xffffffffu, st, o);
   }
   if (lane == 0) {
-    if (visits) atomicAdd(&a.ctr->visits_radiance, visits);
-    if (culled) atomicAdd(&a.ctr->visits_culled, culled);
-    if (nnodes) atomicAdd(&a.ctr->nodes_radiance, nnodes);
-    if (ntris) atomicAdd(&a.ctr->tris_radiance, ntris);
+    if (sv) atomicAdd(&a.ctr->visits_radiance, sv);
+    if (sc) atomicAdd(&a.ctr->visits_culled, sc);
+    if (sn) atomicAdd(&a.ctr->nodes_radiance, sn);
+    if (st) atomicAdd(&a.ctr->tris_radiance, st);
   }
 }
 
