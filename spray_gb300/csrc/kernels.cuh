@@ -30,7 +30,6 @@ constexpr uint32_t kRayIdMask = (1u << kRayIdBits) - 1u;
 constexpr int kMaxSlots = 64;      // shadow rays per hit
 constexpr int kSchedThreads = 256;
 constexpr int kDepthBuckets = 4;   // key = min(depth, 3) * D + domain when ordering by depth
-constexpr int kMaxScanBlocks = 4096;  // blocks of the histogram scan
 constexpr int kDomainBvhMin = 16;     // domain counts from which the scheduler descends a hierarchy
 
 struct DomainDev {
@@ -183,7 +182,7 @@ struct SchedArgs {
   unsigned long long arena_cap;
   uint32_t* list_off;         // per scheduled ray
   uint32_t* list_cnt;
-  uint32_t* hist;             // [nkeys][nchunks]
+  uint32_t* hist;             // [nchunks][nkeys]
   int nchunks;                // ray chunks, each with its own histogram column
   long long* dstats;          // [D][list_size] ray counts per (domain, depth)
   int want_stats;             // fill dstats (out-of-core order, debug hooks)
@@ -203,6 +202,18 @@ struct SchedArgs {
 // most nchunks chunks (chunk c holds rays [c * size, (c + 1) * size)).
 __host__ __device__ __forceinline__ uint64_t chunkSize(uint64_t n, int nchunks) {
   return (((n + (uint64_t)nchunks - 1) / (uint64_t)nchunks) + 31u) & ~(uint64_t)31u;
+}
+
+// Chunks in use for n rays: about kChunkRays rays each, at least one per
+// scheduling warp and at most the nchunks rows the histogram holds, so that
+// the histogram (rows x keys) shrinks with the wave.  Read from the device's
+// ray count by every kernel of one schedule, so a captured frame adapts too.
+constexpr uint64_t kChunkRays = 1024;
+__host__ __device__ __forceinline__ int chunksFor(uint64_t n, int nchunks, int nwarps) {
+  uint64_t want = (n + kChunkRays - 1) / kChunkRays;
+  if (want < (uint64_t)nwarps) want = (uint64_t)nwarps;
+  if (want > (uint64_t)nchunks) want = (uint64_t)nchunks;
+  return want < 1 ? 1 : (int)want;
 }
 
 // Depth bucket of the entry at list position j (p = predicted position, 0xff none).
@@ -260,15 +271,19 @@ struct ShadeArgs {
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles,
                       int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
                       int32_t* alive_idx, Counters* ctr);
-// scan_tmp holds kMaxScanBlocks words.  Launches 5 kernels.
+// scan_tmp holds scan_words words, at least scanTmpWords(nkeys, nchunks) for
+// the fastest scan (fewer give a scan over fewer chunk groups).  Launches 5
+// kernels.
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
-                    int nwarps, int nblocks, uint32_t* scan_tmp);
+                    int nwarps, int nblocks, uint32_t* scan_tmp, size_t scan_words);
+// Workspace words of the histogram scan for nkeys keys and nchunks chunks.
+size_t scanTmpWords(int nkeys, int nchunks);
 // The two halves of launchSchedule: the per-ray domain lists (1 kernel), then
 // the partition into queues (histogram when deferred, scan, scatter: 4 or 5).
 void launchSchedLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int ndomains,
                       int nwarps, int nblocks);
 void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int ndomains, int nwarps,
-                          uint32_t* scan_tmp);
+                          uint32_t* scan_tmp, size_t scan_words);
 // Resident blocks per SM of the scheduling kernel for this shared-memory use.
 int schedBlocksPerSm(int D, int nkeys, int dnode_count);
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks);

@@ -44,6 +44,8 @@ constexpr int kStaticMaxDomains = 256;
 constexpr int kStaticMaxEntries = 1 << 20;
 constexpr int kStaticBlocks = 64;
 constexpr int kStaticWarps = kStaticBlocks * (kSchedThreads / 32);
+// histogram scan workspace: 64 chunk groups of every key, the key bases, a ticket
+constexpr int kStaticScanWords = 64 * kStaticMaxDomains + kStaticMaxDomains + 1;
 
 struct StaticScratch {
   DomainDev domains[kStaticMaxDomains];
@@ -54,7 +56,7 @@ struct StaticScratch {
   uint32_t list_cnt[kStaticMaxRays];
   uint32_t hist[kStaticMaxDomains * kStaticWarps];
   long long dstats[kStaticMaxDomains * kMaxList];
-  uint32_t scan_tmp[kMaxScanBlocks];
+  uint32_t scan_tmp[kStaticScanWords];
   unsigned long long arena_top;
   uint32_t count;
   uint32_t num_entries;
@@ -150,7 +152,7 @@ extern "C" int spray_gpu_schedule_static(const float* domain_bounds, int32_t num
   a.key_start = domain_start;
   a.num_entries = &s->num_entries;
   a.ctr = &s->ctr;
-  launchSchedule(st, a, s->domains, D, kStaticWarps, kStaticBlocks, s->scan_tmp);
+  launchSchedule(st, a, s->domains, D, kStaticWarps, kStaticBlocks, s->scan_tmp, kStaticScanWords);
   Counters ctr;
   uint32_t ne = 0;
   e = cudaMemcpyAsync(&ne, &s->num_entries, sizeof(ne), cudaMemcpyDeviceToHost, st);

@@ -2,6 +2,7 @@
 // queues), stable stream compaction and the domain scores.
 #include <algorithm>
 #include <cfloat>
+#include <stdexcept>
 
 #include "kernels.cuh"
 #include "spray_math.cuh"
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
   __syncthreads();
   const uint32_t n = *a.count;
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
-  const int nch = a.nchunks;
+  const int nch = chunksFor(n, a.nchunks, nwarps);
   const uint64_t csize = chunkSize(n, nch);
   // chunks round-robin over the warps; a chunk's counts fit 16 bits (csize < 2^16)
   for (int ch = gw; ch < nch; ch += nwarps) {
@@ -281,15 +282,21 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
   }
   __syncwarp();
   if (!a.defer_hist) {
-    for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nch + ch] = (h[k >> 1] >> ((k & 1) << 4)) & 0xffffu;
+    for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)ch * nkeys + k] = (h[k >> 1] >> ((k & 1) << 4)) & 0xffffu;
     __syncwarp();
   }
   }
 }
 
-// Pass 2: exclusive scan of the key-major histogram, three phases over many
-// blocks: per-block sums, a scan of the block sums, then per-block scans.
-constexpr int kScanThreads = 512;
+// Pass 2: exclusive scan of the histogram in key-major order (every chunk of
+// key 0, then every chunk of key 1, ...).  The table is stored chunk-major,
+// hist[chunk * nkeys + key], so that passes 1 and 3 move a chunk's counters as
+// one contiguous row.  The chunks are cut into G groups: (a) per group and key
+// the column sum; (b) per key the exclusive scan of its G group sums, and in
+// the block that finishes last the scan of the key totals; (c) per group and
+// key the running offsets, written back in place.  scan_tmp holds the group
+// sums [G][nkeys], the key bases [nkeys] and a ticket word.
+constexpr int kScanMaxGroups = 1024;
 
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* total) {
   __shared__ uint32_t ws[32];
@@ -312,58 +319,145 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* tot
   return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) kScanReduce(const uint32_t* __restrict__ in, uint64_t M,
-                                                            uint64_t chunk, uint32_t* partial) {
-  const uint64_t b0 = min(M, chunk * blockIdx.x), b1 = min(M, b0 + chunk);
+// (a) grid (groups, key tiles): one thread per (group, key)
+__global__ void kHistColumns(const uint32_t* __restrict__ hist, const uint32_t* count, int nchunks, int nwarps,
+                             int nkeys, uint32_t* __restrict__ colsum, uint32_t* ticket) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *ticket = 0u;
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= nkeys) return;
+  const int nch = chunksFor(*count, nchunks, nwarps);
+  const int per = (nch + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int c0 = min(nch, (int)blockIdx.x * per), c1 = min(nch, c0 + per);
   uint32_t s = 0;
-  for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += in[i];
-  uint32_t tot;
-  blockExclusiveScan(s, &tot);
-  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+#pragma unroll 8
+  for (int c = c0; c < c1; ++c) s += hist[(size_t)c * nkeys + k];
+  colsum[(size_t)blockIdx.x * nkeys + k] = s;
 }
 
-__global__ void __launch_bounds__(1024) kScanPartials(uint32_t* partial, int nb) {
+// (b) one block per 32 keys: lane = key, the 32 warps split the groups
+__global__ void __launch_bounds__(1024) kHistKeyScan(uint32_t* colsum, int G, int nkeys, uint32_t* keybase,
+                                                     uint32_t* ticket, uint32_t* key_start,
+                                                     uint32_t* num_entries, unsigned long long entry_cap,
+                                                     Counters* ctr) {
+  __shared__ uint32_t wsum[32][33];
+  __shared__ int is_last;
   __shared__ uint32_t carry;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  const int gper = (G + 31) / 32;
+  const int g0 = min(G, w * gper), g1 = min(G, g0 + gper);
+  uint32_t s = 0;
+  if (k < nkeys) {
+#pragma unroll 8
+    for (int g = g0; g < g1; ++g) s += colsum[(size_t)g * nkeys + k];
+  }
+  wsum[w][lane] = s;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t run = 0;
+    for (int j = 0; j < 32; ++j) {
+      const uint32_t v = wsum[j][lane];
+      wsum[j][lane] = run;
+      run += v;
+    }
+    if (k < nkeys) keybase[k] = run;  // the key's total until the last block scans them
+  }
+  __syncthreads();
+  if (k < nkeys) {
+    uint32_t run = wsum[w][lane];
+    int g = g0;
+    for (; g + 8 <= g1; g += 8) {
+      uint32_t v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = colsum[(size_t)(g + j) * nkeys + k];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        colsum[(size_t)(g + j) * nkeys + k] = run;
+        run += v[j];
+      }
+    }
+    for (; g < g1; ++g) {
+      const uint32_t v = colsum[(size_t)g * nkeys + k];
+      colsum[(size_t)g * nkeys + k] = run;
+      run += v;
+    }
+  }
+  // the last block to finish scans the key totals
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
-  for (int base = 0; base < nb; base += blockDim.x) {
-    int i = base + threadIdx.x;
-    uint32_t v = i < nb ? partial[i] : 0u, tot;
-    uint32_t e = blockExclusiveScan(v, &tot);
-    if (i < nb) partial[i] = carry + e;
+  for (int base = 0; base < nkeys; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const uint32_t v = i < nkeys ? __ldcg(keybase + i) : 0u;
+    uint32_t tot;
+    const uint32_t e = blockExclusiveScan(v, &tot);
+    if (i < nkeys) {
+      keybase[i] = carry + e;
+      key_start[i] = carry + e;
+    }
     __syncthreads();
     if (threadIdx.x == 0) carry += tot;
     __syncthreads();
   }
+  if (threadIdx.x == 0) {
+    uint32_t total = carry;
+    key_start[nkeys] = total;
+    if (total > entry_cap) {
+      atomicAdd(&ctr->entry_overflows, 1ull);
+      total = 0;
+    }
+    *num_entries = total;
+  }
 }
 
-__global__ void __launch_bounds__(kScanThreads) kScanApply(uint32_t* hist, uint64_t M, uint64_t chunk,
-                                                           const uint32_t* partial, int nb, int nwarps,
-                                                           int nkeys, uint32_t* key_start,
-                                                           uint32_t* num_entries,
-                                                           unsigned long long entry_cap, Counters* ctr) {
-  const uint64_t b0 = min(M, chunk * blockIdx.x), b1 = min(M, b0 + chunk);
-  uint32_t run = partial[blockIdx.x];
-  for (uint64_t base = b0; base < b1; base += blockDim.x) {
-    const uint64_t i = base + threadIdx.x;
-    const uint32_t v = i < b1 ? hist[i] : 0u;
-    uint32_t tot;
-    const uint32_t e = blockExclusiveScan(v, &tot);
-    if (i < b1) {
-      hist[i] = run + e;
-      if (i % nwarps == 0) key_start[i / nwarps] = run + e;
-      if (i == M - 1) {
-        uint32_t total = run + e + v;
-        key_start[nkeys] = total;
-        if (total > entry_cap) {
-          atomicAdd(&ctr->entry_overflows, 1ull);
-          total = 0;
-        }
-        *num_entries = total;
-      }
+// (c) grid (groups, key tiles): the running offsets of each chunk
+__global__ void kHistApply(uint32_t* __restrict__ hist, const uint32_t* count, int nchunks, int nwarps,
+                           int nkeys, const uint32_t* __restrict__ colsum,
+                           const uint32_t* __restrict__ keybase) {
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= nkeys) return;
+  const int nch = chunksFor(*count, nchunks, nwarps);
+  const int per = (nch + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int c0 = min(nch, (int)blockIdx.x * per), c1 = min(nch, c0 + per);
+  uint32_t run = keybase[k] + colsum[(size_t)blockIdx.x * nkeys + k];
+  // rows in batches of 8, every load issued before the batch's stores (the
+  // compiler cannot prove that a row's store and the next row's load differ)
+  int c = c0;
+  for (; c + 8 <= c1; c += 8) {
+    uint32_t v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = hist[(size_t)(c + j) * nkeys + k];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      hist[(size_t)(c + j) * nkeys + k] = run;
+      run += v[j];
     }
-    run += tot;
   }
+  for (; c < c1; ++c) {
+    const uint32_t v = hist[(size_t)c * nkeys + k];
+    hist[(size_t)c * nkeys + k] = run;
+    run += v;
+  }
+}
+
+// Groups of the scan for this table and workspace (0 when the workspace
+// cannot hold even one group).
+static int scanGroups(int nkeys, int nch, size_t scan_words) {
+  if (scan_words < (size_t)2 * nkeys + 1) return 0;
+  const size_t fit = (scan_words - nkeys - 1) / nkeys;
+  const int g = (int)std::min<size_t>(std::min<size_t>(fit, kScanMaxGroups), (size_t)std::max(nch, 1));
+  const int per = (std::max(nch, 1) + g - 1) / g;
+  return (std::max(nch, 1) + per - 1) / per;
+}
+
+size_t scanTmpWords(int nkeys, int nchunks) {
+  const size_t g = (size_t)std::min(std::max(nchunks, 1), kScanMaxGroups);
+  return g * nkeys + nkeys + 1;
 }
 
 // Pass 3: stable scatter.  Each warp re-reads its rays in order, flattens
@@ -382,7 +476,7 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
   if (gw >= nwarps) return;
   const uint32_t n = *a.count;
   if (*a.num_entries == 0) return;
-  const int nch = a.nchunks;
+  const int nch = chunksFor(n, a.nchunks, nwarps);
   const uint64_t csize = chunkSize(n, nch);
   const uint32_t lt = laneMaskLt();
   for (int ch = gw; ch < nch; ch += nwarps) {
@@ -390,7 +484,7 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
   const uint64_t r1 = min((uint64_t)n, r0 + csize);
   if (r0 >= r1) break;
   __syncwarp();
-  for (int k = lane; k < nkeys; k += 32) running[k] = a.hist[(size_t)k * nch + ch];
+  for (int k = lane; k < nkeys; k += 32) running[k] = a.hist[(size_t)ch * nkeys + k];
   __syncwarp();
   for (uint64_t base = r0; base < r1; base += 32) {
     const uint64_t i = base + lane;
@@ -440,7 +534,7 @@ __global__ void __launch_bounds__(128) kSchedHist(SchedArgs a, int D, int nkeys,
   const int gw = blockIdx.x * (blockDim.x >> 5) + wib;
   if (gw >= nwarps) return;
   const uint32_t n = *a.count;
-  const int nch = a.nchunks;
+  const int nch = chunksFor(n, a.nchunks, nwarps);
   const uint64_t csize = chunkSize(n, nch);
   for (int ch = gw; ch < nch; ch += nwarps) {
   for (int k = lane; k < nkeys; k += 32) h[k] = 0;
@@ -459,7 +553,7 @@ __global__ void __launch_bounds__(128) kSchedHist(SchedArgs a, int D, int nkeys,
     }
   }
   __syncwarp();
-  for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)k * nch + ch] = h[k];
+  for (int k = lane; k < nkeys; k += 32) a.hist[(size_t)ch * nkeys + k] = h[k];
   __syncwarp();
   }
 }
@@ -487,25 +581,31 @@ void launchSchedLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domai
 }
 
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
-                    int nblocks, uint32_t* scan_tmp) {
+                    int nblocks, uint32_t* scan_tmp, size_t scan_words) {
   launchSchedLists(s, a, domains, D, nwarps, nblocks);
-  launchSchedPartition(s, a, D, nwarps, scan_tmp);
+  launchSchedPartition(s, a, D, nwarps, scan_tmp, scan_words);
 }
 
-void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int D, int nwarps, uint32_t* scan_tmp) {
+void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int D, int nwarps, uint32_t* scan_tmp,
+                          size_t scan_words) {
   const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
   if (a.defer_hist) {
     const size_t smemh = (size_t)4 * nkeys * 4;
     cudaFuncSetAttribute(kSchedHist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemh);
     kSchedHist<<<(nwarps + 3) / 4, 128, smemh, s>>>(a, D, nkeys, nwarps);
   }
-  const uint64_t M = (uint64_t)nkeys * a.nchunks;
-  const int nb = (int)std::min<uint64_t>(kMaxScanBlocks, (M + 2047) / 2048);
-  const uint64_t chunk = (M + nb - 1) / nb;
-  kScanReduce<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp);
-  kScanPartials<<<1, 1024, 0, s>>>(scan_tmp, nb);
-  kScanApply<<<nb, kScanThreads, 0, s>>>(a.hist, M, chunk, scan_tmp, nb, a.nchunks, nkeys, a.key_start,
-                                          a.num_entries, a.entry_cap, a.ctr);
+  const int nch = a.nchunks;
+  const int G = scanGroups(nkeys, nch, scan_words);
+  if (G < 1) throw std::runtime_error("histogram scan workspace too small");
+  uint32_t* colsum = scan_tmp;
+  uint32_t* keybase = scan_tmp + (size_t)G * nkeys;
+  uint32_t* ticket = keybase + nkeys;
+  const int bt = std::min(256, (nkeys + 31) / 32 * 32);
+  const dim3 grid(G, (nkeys + bt - 1) / bt);
+  kHistColumns<<<grid, bt, 0, s>>>(a.hist, a.count, nch, nwarps, nkeys, colsum, ticket);
+  kHistKeyScan<<<(nkeys + 31) / 32, 1024, 0, s>>>(colsum, G, nkeys, keybase, ticket, a.key_start,
+                                                   a.num_entries, a.entry_cap, a.ctr);
+  kHistApply<<<grid, bt, 0, s>>>(a.hist, a.count, nch, nwarps, nkeys, colsum, keybase);
   const int wpb = 4;
   size_t smem3 = (size_t)wpb * nkeys * 4 + (size_t)wpb * 32 * kMaxEmit * 3 * 4;
   cudaFuncSetAttribute(kSchedScatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);

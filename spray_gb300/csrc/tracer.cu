@@ -918,7 +918,8 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   // one resident wave: each warp owns a contiguous chunk of rays
   sched_blocks = num_sms * schedBlocksPerSm(D, kDepthBuckets * D, dnode_count);
   sched_warps = sched_blocks * (kSchedThreads / 32);
-  // eight ray chunks per scheduling warp, so that uneven rays balance out;
+  // up to eight ray chunks per scheduling warp, so that uneven rays balance
+  // out (a wave uses about one chunk per 1024 rays of these, see chunksFor);
   // a chunk's per-key counts must fit 16 bits
   sched_chunks = (cfg.sched_chunks_per_warp > 0 ? cfg.sched_chunks_per_warp : 8) * sched_warps;
   if (chunkSize((uint64_t)1 << kRayIdBits, sched_chunks) >= 65536)
@@ -985,7 +986,8 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_rec_key, E);
   devAlloc(&d_rec_attr, E);
   devAlloc(&d_work, kDepthBuckets);
-  devAlloc(&d_scan_tmp, kMaxScanBlocks);
+  scan_words = scanTmpWords(nkeys, sched_chunks);
+  devAlloc(&d_scan_tmp, scan_words);
   compact_blocks = num_sms * 4;
   devAlloc(&d_block_tmp, compact_blocks);
   devAlloc(&d_image, (size_t)std::max<int64_t>(frame_pixels, 1));
@@ -1045,10 +1047,10 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
     src.list = list;
     mlp::launchPredictArena(stream, proposalNet(), src, d_pred, num_sms * 4);
     a.pred = d_pred;
-    launchSchedPartition(stream, a, D, sched_warps, d_scan_tmp);
+    launchSchedPartition(stream, a, D, sched_warps, d_scan_tmp, scan_words);
     launches += 7;
   } else {
-    launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp);
+    launchSchedule(stream, a, d_domains, D, sched_warps, sched_blocks, d_scan_tmp, scan_words);
     launches += 5;
   }
 }
