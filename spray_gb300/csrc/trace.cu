@@ -42,14 +42,72 @@ __device__ __forceinline__ TravRay makeTravRay(V3 org, V3 dir) {
   return r;
 }
 
+// Two fp32 values in one 64-bit register for Blackwell's packed arithmetic
+// (sub.rn.f32x2, mul.rn.f32x2): each half is rounded exactly like the scalar
+// instruction, so the box test below gives the same bits as scalar code.
+__device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 f2unpack(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+// (a - b) * c per half
+__device__ __forceinline__ float2 f2subMul(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long d, e;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(e) : "l"(d), "l"(c));
+  return f2unpack(e);
+}
+
 // Intersects the four children of a node; returns a mask of hit children and
 // their entry distances.  Near and far planes are picked by the direction's
-// sign, so an empty slot (lo = +inf, hi = -inf) can never be entered.
+// sign, so an empty slot (lo = +inf, hi = -inf) can never be entered.  Per
+// child: t0 = max(max(tx0, ty0), max(tz0, tnear)), t1 = min(min(tx1, ty1),
+// min(tz1, tfar)) * kBoxSlack with tx = (plane - org.x) * inv.x; children
+// (0, 1) and (2, 3) share the packed subtractions and products.
 __device__ __forceinline__ int testChildren(const BvhNode4* __restrict__ nodes, int node,
                                             const TravRay& r, float tnear, float tfar,
                                             float tn[4]) {
   // the node stores lo/hi per axis as float4 pairs; the ray's signs pick the
   // near and far plane of each pair by address
+  const float4* p = reinterpret_cast<const float4*>(nodes + node);
+  const float4 nx = __ldg(p + r.sx), fx = __ldg(p + (r.sx ^ 1));
+  const float4 ny = __ldg(p + 2 + r.sy), fy = __ldg(p + (3 - r.sy));
+  const float4 nz = __ldg(p + 4 + r.sz), fz = __ldg(p + (5 - r.sz));
+  const unsigned long long ox = f2pack(r.org.x, r.org.x), oy = f2pack(r.org.y, r.org.y),
+                           oz = f2pack(r.org.z, r.org.z);
+  const unsigned long long ix = f2pack(r.inv.x, r.inv.x), iy = f2pack(r.inv.y, r.inv.y),
+                           iz = f2pack(r.inv.z, r.inv.z);
+  int mask = 0;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float2 ax = f2subMul(h ? f2pack(nx.z, nx.w) : f2pack(nx.x, nx.y), ox, ix);
+    const float2 ay = f2subMul(h ? f2pack(ny.z, ny.w) : f2pack(ny.x, ny.y), oy, iy);
+    const float2 az = f2subMul(h ? f2pack(nz.z, nz.w) : f2pack(nz.x, nz.y), oz, iz);
+    const float2 bx = f2subMul(h ? f2pack(fx.z, fx.w) : f2pack(fx.x, fx.y), ox, ix);
+    const float2 by = f2subMul(h ? f2pack(fy.z, fy.w) : f2pack(fy.x, fy.y), oy, iy);
+    const float2 bz = f2subMul(h ? f2pack(fz.z, fz.w) : f2pack(fz.x, fz.y), oz, iz);
+    const float t00 = fmaxf(fmaxf(ax.x, ay.x), fmaxf(az.x, tnear));
+    const float t01 = fmaxf(fmaxf(ax.y, ay.y), fmaxf(az.y, tnear));
+    const float t10 = fminf(fminf(bx.x, by.x), fminf(bz.x, tfar)) * kBoxSlack;
+    const float t11 = fminf(fminf(bx.y, by.y), fminf(bz.y, tfar)) * kBoxSlack;
+    tn[2 * h] = t00;
+    tn[2 * h + 1] = t01;
+    if (t00 <= t10) mask |= 1 << (2 * h);
+    if (t01 <= t11) mask |= 1 << (2 * h + 1);
+  }
+  return mask;
+}
+
+// The same test in scalar arithmetic (fewer live registers), for the
+// occlusion walk.
+__device__ __forceinline__ int testChildrenScalar(const BvhNode4* __restrict__ nodes, int node,
+                                                  const TravRay& r, float tnear, float tfar,
+                                                  float tn[4]) {
   const float4* p = reinterpret_cast<const float4*>(nodes + node);
   const float4 nx = __ldg(p + r.sx), fx = __ldg(p + (r.sx ^ 1));
   const float4 ny = __ldg(p + 2 + r.sy), fy = __ldg(p + (3 - r.sy));
@@ -151,6 +209,35 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
     }
     return kDone;
   };
+  // triangles of one leaf; false on a corrupt leaf reference
+  auto testLeaf = [&](int lf) -> bool {
+    const uint32_t v = ~(uint32_t)lf;
+    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+    if (first + cnt > (uint32_t)dom.num_tris) {
+      raise(ctr, kErrBadNode);
+      return false;
+    }
+    tested += cnt;
+    for (uint32_t q = 0; q < cnt; ++q) {
+      const float4* tp = tris + 3 * (size_t)(first + q);
+      const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+      float t, u, vv;
+      if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
+                            kRayEpsilon, __int_as_float(0x7f800000), &t, &u, &vv)) {
+        const uint32_t prim = __float_as_uint(a.w);
+        const uint64_t key = packHitKey(t, dom.gprim_base + prim);
+        if (key < best_key) {
+          best_key = key;
+          best_t = t;
+          best_prim = prim;
+          best_u = u;
+          best_v = vv;
+          found = true;
+        }
+      }
+    }
+    return true;
+  };
   int cur = 0;
   while (cur != kDone) {
     // inner nodes until the nearest pending entry is a leaf
@@ -206,32 +293,7 @@ __device__ bool traverseClosest(const SceneDev& sc, const DomainDev& dom, const 
       }
     }
     if (cur == kDone) break;
-    // leaf
-    const uint32_t v = ~(uint32_t)cur;
-    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
-    if (first + cnt > (uint32_t)dom.num_tris) {
-      raise(ctr, kErrBadNode);
-      return finish();
-    }
-    tested += cnt;
-    for (uint32_t q = 0; q < cnt; ++q) {
-      const float4* tp = tris + 3 * (size_t)(first + q);
-      const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
-      float t, u, vv;
-      if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
-                            kRayEpsilon, __int_as_float(0x7f800000), &t, &u, &vv)) {
-        const uint32_t prim = __float_as_uint(a.w);
-        const uint64_t key = packHitKey(t, dom.gprim_base + prim);
-        if (key < best_key) {
-          best_key = key;
-          best_t = t;
-          best_prim = prim;
-          best_u = u;
-          best_v = vv;
-          found = true;
-        }
-      }
-    }
+    if (!testLeaf(cur)) return finish();
     cur = pop();
   }
   return finish();
@@ -255,7 +317,8 @@ __device__ __forceinline__ bool anyRound(Walk& w, int* stack, const TravRay& r, 
     }
     float tn[4];
     ++nnodes;
-    const int mask = testChildren(w.nodes, w.cur, r, kRayEpsilon, tfar, tn);
+    // scalar: the packed test's registers make the refilling walk spill
+    const int mask = testChildrenScalar(w.nodes, w.cur, r, kRayEpsilon, tfar, tn);
     const int4 ch = loadChildren(w.nodes, w.cur);
     // the last child hit continues the walk; the earlier ones are pushed
     // (the order a push of all of them and a pop would give)
