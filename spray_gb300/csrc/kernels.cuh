@@ -198,6 +198,27 @@ struct SchedArgs {
   int defer_hist;             // kSchedLists leaves the histogram to the partition step
 };
 
+// Two fp32 values in one 64-bit register for Blackwell's packed arithmetic
+// (sub.rn.f32x2, mul.rn.f32x2): each half is rounded exactly like the scalar
+// instruction, so the box test below gives the same bits as scalar code.
+__device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 f2unpack(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+// (a - b) * c per half
+__device__ __forceinline__ float2 f2subMul(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long d, e;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(e) : "l"(d), "l"(c));
+  return f2unpack(e);
+}
+
 // Rays per chunk of the scheduler: a multiple of 32 covering n rays in at
 // most nchunks chunks (chunk c holds rays [c * size, (c + 1) * size)).
 __host__ __device__ __forceinline__ uint64_t chunkSize(uint64_t n, int nchunks) {
@@ -304,8 +325,8 @@ void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, u
 void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,
                        uint32_t* list, uint32_t* count, int32_t* index_of, uint32_t* block_tmp, int nblocks);
 void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
-                      const ViewDev* views, const int32_t* pixid, const int32_t* alive_idx,
-                      const ShadowBuf sh, const uint8_t* flag, int slots, int nblocks);
+                      const ViewDev* views, const int32_t* alive_idx, const ShadowBuf sh,
+                      const uint8_t* flag, int slots, int nblocks);
 // Uploads the constant tables of the shader (once per device).
 void initShadeTables();
 void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int list_size,

@@ -8,6 +8,8 @@
 // (src/ooc/ooc_vbuf.cc:41-52, ooc_tcontext.inl:123-135), which are exactly
 // the rays spawned here.  Shadow ray `slot` of alive ray a lives at
 // a * slots + slot.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "spray_math.cuh"
 
@@ -308,47 +310,94 @@ void launchShade(cudaStream_t s, const ShadeArgs& a, int nblocks) {
 // Per pixel of the wave: its tile (binary search on pix_base), its samples
 // (tile-local pixel lp holds samples lp * spp .. lp * spp + spp - 1), its view's
 // image slot and scale; samples and slots in order, the sum in double.
-__global__ void kRetire(float4* image, const TileDev* __restrict__ tiles, int ntiles, int64_t npix,
-                        const ViewDev* __restrict__ views, const int32_t* __restrict__ pixid,
-                        const int32_t* __restrict__ alive_idx, ShadowBuf sh,
-                        const uint8_t* __restrict__ flag, int S) {
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = ntiles - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (tiles[mid].pix_base <= p) lo = mid;
-      else hi = mid - 1;
-    }
-    const TileDev tl = tiles[lo];
-    const ViewDev& vw = views[tl.view];
-    const int spp = tl.spp;
-    const double scale = vw.scale;
-    const int64_t s0 = tl.sample_base + (p - tl.pix_base) * spp;
-    float4* px = image + vw.pixel_base + pixid[s0];
-    float4 acc = *px;
-    bool touched = false;
-    for (int s = 0; s < spp; ++s) {
-      int32_t ai = alive_idx[s0 + s];
-      if (ai < 0) continue;
-      for (int k = 0; k < S; ++k) {
-        uint32_t sid = (uint32_t)ai * S + k;
-        if (!flag[sid] || sh.occluded[sid]) continue;
-        float4 w = sh.wgt[sid];
-        acc.x = (float)((double)acc.x + scale * (double)w.x);
-        acc.y = (float)((double)acc.y + scale * (double)w.y);
-        acc.z = (float)((double)acc.z + scale * (double)w.z);
-        touched = true;
+//
+// A block takes 256 consecutive pixels, whose samples are one contiguous
+// range: their alive indices are staged in shared memory with coalesced loads
+// (one pad word per 32, so that each thread's run of spp indices is read
+// without bank conflicts) when the range fits kRetireStage, else read directly.
+constexpr int kRetireStage = 4096;
+
+__global__ void __launch_bounds__(256) kRetire(float4* image, const TileDev* __restrict__ tiles, int ntiles,
+                                               int64_t npix, const ViewDev* __restrict__ views,
+                                               const int32_t* __restrict__ alive_idx, ShadowBuf sh,
+                                               const uint8_t* __restrict__ flag, int S) {
+  __shared__ int32_t sidx[kRetireStage + kRetireStage / 32];
+  __shared__ int64_t range[2];
+  for (int64_t p0 = (int64_t)blockIdx.x * blockDim.x; p0 < npix; p0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = p0 + threadIdx.x;
+    const bool valid = p < npix;
+    int lo = 0;
+    if (valid) {
+      int hi = ntiles - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tiles[mid].pix_base <= p) lo = mid;
+        else hi = mid - 1;
       }
     }
-    if (touched) *px = acc;
+    const TileDev tl = tiles[lo];
+    const int spp = tl.spp;
+    const int64_t lp = p - tl.pix_base;
+    const int64_t s0 = tl.sample_base + lp * spp;
+    if (threadIdx.x == 0) range[0] = s0;
+    if (p == min(npix, p0 + (int64_t)blockDim.x) - 1) range[1] = s0 + spp;
+    __syncthreads();
+    const int64_t sbeg = range[0], nstage = range[1] - range[0];
+    const bool staged = nstage <= kRetireStage;
+    if (staged) {
+      // 8 loads in flight per thread before their shared-memory stores
+      for (int j0 = threadIdx.x; j0 < (int)nstage; j0 += 8 * blockDim.x) {
+        int32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int j = j0 + u * (int)blockDim.x;
+          v[u] = j < (int)nstage ? alive_idx[sbeg + j] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int j = j0 + u * (int)blockDim.x;
+          if (j < (int)nstage) sidx[j + (j >> 5)] = v[u];
+        }
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      const ViewDev& vw = views[tl.view];
+      const double scale = vw.scale;
+      const int lpi = (int)lp;  // tile-local pixel (32-bit division)
+      const int x = tl.x + lpi % tl.w, y = tl.y + lpi / tl.w;
+      float4* px = image + vw.pixel_base + (int64_t)y * vw.image_w + x;
+      float4 acc = *px;
+      bool touched = false;
+      const int f0 = (int)(s0 - sbeg);
+      for (int s = 0; s < spp; ++s) {
+        const int f = f0 + s;
+        const int32_t ai = staged ? sidx[f + (f >> 5)] : alive_idx[s0 + s];
+        if (ai < 0) continue;
+        for (int k = 0; k < S; ++k) {
+          uint32_t sid = (uint32_t)ai * S + k;
+          if (!flag[sid] || sh.occluded[sid]) continue;
+          float4 w = sh.wgt[sid];
+          acc.x = (float)((double)acc.x + scale * (double)w.x);
+          acc.y = (float)((double)acc.y + scale * (double)w.y);
+          acc.z = (float)((double)acc.z + scale * (double)w.z);
+          touched = true;
+        }
+      }
+      if (touched) *px = acc;
+    }
+    __syncthreads();  // the next group restages sidx and range
   }
 }
 
 void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
-                      const ViewDev* views, const int32_t* pixid, const int32_t* alive_idx, const ShadowBuf sh,
+                      const ViewDev* views, const int32_t* alive_idx, const ShadowBuf sh,
                       const uint8_t* flag, int slots, int nblocks) {
-  kRetire<<<nblocks, 256, 0, s>>>(image, tiles, ntiles, npix, views, pixid, alive_idx, sh, flag, slots);
+  // one 256-pixel group per block where the grid allows (the staged loads of
+  // many blocks overlap), at least nblocks
+  const int64_t groups = (npix + 255) / 256;
+  const int64_t blocks = std::max<int64_t>(nblocks, std::min<int64_t>(groups, 1 << 24));
+  kRetire<<<(unsigned)blocks, 256, 0, s>>>(image, tiles, ntiles, npix, views, alive_idx, sh, flag, slots);
 }
 
 }  // namespace spray

@@ -42,27 +42,6 @@ __device__ __forceinline__ TravRay makeTravRay(V3 org, V3 dir) {
   return r;
 }
 
-// Two fp32 values in one 64-bit register for Blackwell's packed arithmetic
-// (sub.rn.f32x2, mul.rn.f32x2): each half is rounded exactly like the scalar
-// instruction, so the box test below gives the same bits as scalar code.
-__device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ float2 f2unpack(unsigned long long v) {
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-// (a - b) * c per half
-__device__ __forceinline__ float2 f2subMul(unsigned long long a, unsigned long long b, unsigned long long c) {
-  unsigned long long d, e;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(e) : "l"(d), "l"(c));
-  return f2unpack(e);
-}
-
 // Intersects the four children of a node; returns a mask of hit children and
 // their entry distances.  Near and far planes are picked by the direction's
 // sign, so an empty slot (lo = +inf, hi = -inf) can never be entered.  Per

@@ -1230,8 +1230,8 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     if (capture) captureShadows(b, S);
     // retire
-    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, d_pixid,
-                     d_alive_idx, sh, d_shadow_flag, S, nblk);
+    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, d_alive_idx, sh,
+                     d_shadow_flag, S, nblk);
     launches += 1;
     // next depth
     if (b + 1 < nb_total) {
@@ -1548,8 +1548,8 @@ void Tracer::traceWaveBatched(const Wave& w) {
       scheduleRadiance(false);
     }
     oocPass(more, true, S, rb);
-    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, d_pixid,
-                     retire_idx, sh, d_shadow_flag, S, nblk);
+    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, retire_idx, sh,
+                     d_shadow_flag, S, nblk);
     launches += 1;
   }
 }
