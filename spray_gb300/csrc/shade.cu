@@ -68,7 +68,19 @@ __device__ float frDielectric(float cosThetaI, float etaI, float etaT, V3 wo, V3
 
 }  // namespace
 
-__global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
+// Domains whose first global face number the shader keeps in shared memory
+// for the hit's domain search (more domains search the device table).
+constexpr int kShadeSmemDomains = 4096;
+
+// Four resident blocks per SM (64 registers): the shader is latency-bound,
+// and occupancy pays more than the few spills (measured against 94 registers).
+__global__ void __launch_bounds__(256, 4) kShade(ShadeArgs a) {
+  __shared__ uint32_t sprim[kShadeSmemDomains];
+  const int D = a.scene.num_domains;
+  const bool stab = D <= kShadeSmemDomains;
+  if (stab)
+    for (int k = threadIdx.x; k < D; k += blockDim.x) sprim[k] = a.scene.domains[k].gprim_base;
+  __syncthreads();
   const uint32_t n = *a.count;
   const int S = a.slots;
   unsigned long long nshadow = 0, nbounce = 0;
@@ -83,13 +95,27 @@ __global__ void __launch_bounds__(256) kShade(ShadeArgs a) {
       continue;
     }
     const float t = hitKeyT(key);
-    const int d = domainOfPrim(a.scene.domains, a.scene.num_domains, (uint32_t)key);
-    const DomainDev dom = a.scene.domains[d];
+    // the sample's loads first: they do not depend on the domain search
     const float4 o4 = a.rays.org[sample], d4 = a.rays.dir[sample], w4 = a.rays.wgt[sample];
+    const float4 hn = a.hit_ns[sample];
+    int d;
+    if (stab) {
+      // last domain whose first global face is <= the hit's
+      const uint32_t gprim = (uint32_t)key;
+      int lo = 0, hi = D - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sprim[mid] <= gprim) lo = mid;
+        else hi = mid - 1;
+      }
+      d = lo;
+    } else {
+      d = domainOfPrim(a.scene.domains, D, (uint32_t)key);
+    }
+    const DomainDev dom = a.scene.domains[d];
     const V3 org = v3(o4.x, o4.y, o4.z), dir = v3(d4.x, d4.y, d4.z);
     const V3 Lin = v3(w4.x, w4.y, w4.z);
     const V3 pos = v3(dir.x * t + org.x, dir.y * t + org.y, dir.z * t + org.z);
-    const float4 hn = a.hit_ns[sample];
     const V3 normal = v3(hn.x, hn.y, hn.z);
     const V3 surf = unpackColor(__float_as_uint(hn.w));
     V3 wo = -dir;

@@ -19,6 +19,12 @@
 
 namespace spray {
 
+// Blocks per SM of the compaction passes and of the grid-stride streaming
+// kernels (resolve, shade, retire); 8 measured best against 4, 6, 12, 16, 24
+// on a GB300 (C2 frame 13.18 -> 12.69 ms).
+constexpr int kCompactBlocksPerSm = 8;
+constexpr int kStreamBlocksPerSm = 8;
+
 thread_local std::string g_last_error;
 
 int fail(int code, const std::string& msg) {
@@ -988,7 +994,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_work, kDepthBuckets);
   scan_words = scanTmpWords(nkeys, sched_chunks);
   devAlloc(&d_scan_tmp, scan_words);
-  compact_blocks = num_sms * 4;
+  compact_blocks = num_sms * kCompactBlocksPerSm;
   devAlloc(&d_block_tmp, compact_blocks);
   devAlloc(&d_image, (size_t)std::max<int64_t>(frame_pixels, 1));
   image_cap = frame_pixels;
@@ -1144,7 +1150,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
   // queues are keyed by depth bucket out of core as well
   const bool nonspec = ooc && cfg.schedule_policy == 4;
   const int order_by_depth = (cfg.cull && (!ooc || nonspec)) ? 1 : 0;
-  const int nblk = num_sms * 4;
+  const int nblk = num_sms * kStreamBlocksPerSm;
   for (int b = 0; b < nb_total; ++b) {
     if (capture) captureRays(b);
     // radiance rays -> per-domain queues
@@ -1508,7 +1514,7 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int 
 void Tracer::traceWaveBatched(const Wave& w) {
   const int S = std::max(slots(), 1);
   const int nb_total = maxBounces();
-  const int nblk = num_sms * 4;
+  const int nblk = num_sms * kStreamBlocksPerSm;
   beginWave(w);
   // radiance queues keyed by depth bucket when culling, so each batch traces
   // its entries front to back (learned: predicted domain and those in front
