@@ -463,15 +463,19 @@ size_t scanTmpWords(int nkeys, int nchunks) {
 // Pass 3: stable scatter.  Each warp re-reads its rays in order, flattens
 // their entries into shared memory and ranks them per key with match_any, so
 // every domain's queue keeps ray order (the order a single-threaded
-// Isector::isectAll pushes them, ooc_isector.h:133-144).
+// Isector::isectAll pushes them, ooc_isector.h:133-144).  The flattened entries
+// of 32 rays pass through a window of kScatterWindow entries per warp, in
+// order, so that the staging buffer stays small and many warps fit per SM.
+constexpr int kScatterWindow = 128;
+
 __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nkeys, int nwarps) {
   extern __shared__ uint32_t smem[];
   const int wpb = blockDim.x >> 5;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t* running = smem + (size_t)wib * nkeys;
-  uint32_t* fkey = smem + (size_t)wpb * nkeys + (size_t)wib * (32 * kMaxEmit) * 3;
-  uint32_t* fw0 = fkey + 32 * kMaxEmit;
-  uint32_t* fw1 = fw0 + 32 * kMaxEmit;
+  uint32_t* fkey = smem + (size_t)wpb * nkeys + (size_t)wib * kScatterWindow * 3;
+  uint32_t* fw0 = fkey + kScatterWindow;
+  uint32_t* fw1 = fw0 + kScatterWindow;
   const int gw = blockIdx.x * wpb + wib;
   if (gw >= nwarps) return;
   const uint32_t n = *a.count;
@@ -488,38 +492,44 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
   __syncwarp();
   for (uint64_t base = r0; base < r1; base += 32) {
     const uint64_t i = base + lane;
-    uint32_t cnt = 0, off = 0, rid = 0;
+    uint32_t cnt = 0, off = 0, rid = 0, p = 0xffu;
     if (i < r1) {
       cnt = a.list_cnt[i];
       off = a.list_off[i];
       rid = a.list[i];
+      if (a.pred) p = a.pred[i];
     }
     uint32_t total;
-    uint32_t pos = warpExclusiveScan(cnt, &total);
-    for (uint32_t j = 0; j < cnt; ++j) {
-      uint2 e = a.arena[off + j];
-      uint32_t d = e.x & 0xffffu;
-      uint32_t depth = (e.x >> 16) & 0x7fffu;
-      uint32_t origin = e.x >> 31;
-      uint32_t key = a.order_by_depth ? bucketOf(depth, a.pred ? a.pred[i] : 0xffu) * D + d : d;
-      fkey[pos + j] = key;
-      fw0[pos + j] = (rid & kRayIdMask) | (min(depth, 31u) << kRayIdBits) | (origin << 31);
-      fw1[pos + j] = e.y;
-    }
-    __syncwarp();
-    for (uint32_t s = 0; s < total; s += 32) {
-      const uint32_t e = s + lane;
-      const bool valid = e < total;
-      const uint32_t key = valid ? fkey[e] : 0xffffffffu;
-      const uint32_t m = __match_any_sync(0xffffffffu, key);
-      uint32_t rank = 0;
-      if (valid) rank = running[key] + __popc(m & lt);
+    const uint32_t pos = warpExclusiveScan(cnt, &total);
+    for (uint32_t w0 = 0; w0 < total; w0 += kScatterWindow) {
+      const uint32_t w1 = min(total, w0 + (uint32_t)kScatterWindow);
+      // this lane's entries that fall in [w0, w1)
+      const uint32_t lo = max(pos, w0), hi = min(pos + cnt, w1);
+      for (uint32_t f = lo; f < hi; ++f) {
+        const uint2 e = a.arena[off + (f - pos)];
+        const uint32_t d = e.x & 0xffffu;
+        const uint32_t depth = (e.x >> 16) & 0x7fffu;
+        const uint32_t origin = e.x >> 31;
+        const uint32_t key = a.order_by_depth ? bucketOf(depth, p) * D + d : d;
+        fkey[f - w0] = key;
+        fw0[f - w0] = (rid & kRayIdMask) | (min(depth, 31u) << kRayIdBits) | (origin << 31);
+        fw1[f - w0] = e.y;
+      }
       __syncwarp();
-      if (valid && (__ffs(m) - 1) == lane) running[key] += __popc(m);
+      for (uint32_t s = w0; s < w1; s += 32) {
+        const uint32_t e = s + lane;
+        const bool valid = e < w1;
+        const uint32_t key = valid ? fkey[e - w0] : 0xffffffffu;
+        const uint32_t m = __match_any_sync(0xffffffffu, key);
+        uint32_t rank = 0;
+        if (valid) rank = running[key] + __popc(m & lt);
+        __syncwarp();
+        if (valid && (__ffs(m) - 1) == lane) running[key] += __popc(m);
+        __syncwarp();
+        if (valid && rank < a.entry_cap) a.entries[rank] = make_uint2(fw0[e - w0], fw1[e - w0]);
+      }
       __syncwarp();
-      if (valid && rank < a.entry_cap) a.entries[rank] = make_uint2(fw0[e], fw1[e]);
     }
-    __syncwarp();
   }
   }
 }
@@ -607,7 +617,7 @@ void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int D, int nwarps,
                                                    a.num_entries, a.entry_cap, a.ctr);
   kHistApply<<<grid, bt, 0, s>>>(a.hist, a.count, nch, nwarps, nkeys, colsum, keybase);
   const int wpb = 4;
-  size_t smem3 = (size_t)wpb * nkeys * 4 + (size_t)wpb * 32 * kMaxEmit * 3 * 4;
+  size_t smem3 = (size_t)wpb * nkeys * 4 + (size_t)wpb * kScatterWindow * 3 * 4;
   cudaFuncSetAttribute(kSchedScatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
   kSchedScatter<<<(nwarps + wpb - 1) / wpb, wpb * 32, smem3, s>>>(a, D, nkeys, nwarps);
 }

@@ -1216,8 +1216,12 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
                   nullptr, d_block_tmp, compact_blocks);
     launches += 3;
-    schedule(true, 0, d_shadow_count, d_shadow_list, S, false, nonspec);
-    if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, 0);
+    // In core the shadow entries are sorted by list position (the ray's own
+    // domain first): the occlusion walk takes them in that order, so an
+    // occluder found near the ray culls its entries in farther domains.
+    const int sorder = (!ooc && !nonspec) ? 1 : 0;
+    schedule(true, sorder, d_shadow_count, d_shadow_list, S, false, nonspec);
+    if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, sorder);
     if (nonspec) {
       oocPass(false, true, S, 1, 0, 0, true);
     } else if (ooc && cfg.schedule_policy == 0) {
@@ -1226,7 +1230,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       traceOutOfCore(true, residentFirst(order), S);
     } else {
       CK(cudaMemsetAsync(d_work, 0, 4, stream));
-      TraceArgs to = traceArgs(0, S);
+      TraceArgs to = traceArgs(sorder, S);
       cudaEvent_t o0 = poolEvent(), o1 = poolEvent();
       record(o0);
       launchTraceOccluded(stream, to, traceBlocks());
