@@ -385,6 +385,11 @@ __device__ __forceinline__ uint32_t lanesBelow() {
 
 // Closest hits: warps take 32 consecutive entries at a time, so the lanes of a
 // warp walk coherent rays (consecutive samples of the same domain queue).
+// kPack: culled entries are dropped before the warp's lanes are assigned
+// (in core); out of core the per-batch launches keep the 32 consecutive
+// entries a warp takes (packing across culled entries measured slower there:
+// the batches are small and the packed rays less coherent).
+template <bool kPack>
 __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
@@ -402,14 +407,56 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
   // per-thread counts in 32 bits (entries are 32-bit indices); node and
   // triangle counts go to the global counters before they could wrap
   uint32_t visits = 0, culled = 0, nnodes = 0, ntris = 0;
+  // Live entries waiting for a lane, in queue order: a warp takes 32 entries
+  // at a time, drops the ones the culling test rejects (kPack) and traces 32
+  // live ones together, so that culled entries leave no lane idle.
+  __shared__ uint32_t sbuf[8][64];
+  uint32_t* buf = sbuf[threadIdx.x >> 5];
+  const uint32_t below = lanesBelow();
+  int nbuf = 0;
+  bool exhausted = false;
   while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = E0 + atomicAdd(a.work, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= E) break;
-    const uint32_t w = base + lane;
-    if (w >= E) continue;
-    const uint32_t e = entryOf(a, sbeg, spre, w);
+    while (nbuf < 32 && !exhausted) {
+      uint32_t base = 0;
+      if (lane == 0) base = E0 + atomicAdd(a.work, 32u);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= E) {
+        exhausted = true;
+        break;
+      }
+      if (base + 32u >= E) exhausted = true;
+      const uint32_t w = base + lane;
+      bool live = false;
+      uint32_t ce = 0;
+      if (w < E) {
+        ce = entryOf(a, sbeg, spre, w);
+        live = true;
+        if (kPack && a.cull) {
+          const uint2 ent = a.entries[ce];
+          const uint64_t cur = *((volatile uint64_t*)&a.ray_key[ent.x & kRayIdMask]);
+          if (cur != kNoHit && __uint_as_float(ent.y) > hitKeyT(cur)) {
+            a.rec_key[ce] = kNoHit;
+            ++culled;
+            live = false;
+          }
+        }
+      }
+      const uint32_t lm = __ballot_sync(0xffffffffu, live);
+      if (live) buf[nbuf + __popc(lm & below)] = ce;
+      nbuf += __popc(lm);
+      __syncwarp();
+    }
+    if (nbuf == 0) break;
+    const int take = min(nbuf, 32), rest = nbuf - take;
+    const bool has = lane < take;
+    const uint32_t mine = has ? buf[lane] : 0u;
+    const uint32_t moved = lane < rest ? buf[take + lane] : 0u;
+    __syncwarp();
+    if (lane < rest) buf[lane] = moved;
+    __syncwarp();
+    nbuf = rest;
+    if (!has) continue;
+    const uint32_t e = mine;
     const uint2 ent = a.entries[e];
     const uint32_t ray = ent.x & kRayIdMask;
     const float tdom = __uint_as_float(ent.y);
@@ -473,7 +520,8 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
 
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks) {
   size_t smem = (size_t)(a.nkeys + 2 + 2 * a.nseg) * 4;
-  kTraceClosest<<<nblocks, 256, smem, s>>>(a);
+  if (a.nseg == 0) kTraceClosest<true><<<nblocks, 256, smem, s>>>(a);
+  else kTraceClosest<false><<<nblocks, 256, smem, s>>>(a);
 }
 
 // The entry that holds a ray's final key publishes its colour and normal.
