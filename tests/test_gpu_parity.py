@@ -91,6 +91,27 @@ def test_radiance_queues_bit_exact(lib_built, oracle_mod, scene64, cull):
     assert np.array_equal(np.argsort(sc["order"]), oorder)
 
 
+def test_many_domains_queues_and_image(lib_built, oracle_mod):
+    # 125 domains: 500 scheduler keys, so the histogram scan runs over several
+    # key tiles and key-scan blocks; radiance queues and the path-traced image
+    # (shadow queues sorted by list position, 500 keys too) stay bit-exact
+    sc = scenes.wavelet_grid(5, 16, colors="albedo", light="point+diffuse")
+    cfg = small_config(image_w=80, image_h=60, ao_mode=0, ao_samples=2, pixel_samples=2, bounces=3)
+    t, img, st, o = run(cfg, sc, 5, oracle_mod, cull=0)
+    rays = t.debug(sg.DBG_RAYS, 0)
+    q = t.debug(sg.DBG_RQUEUES, 0)
+    oq, _ = o.schedule(rays["org"], rays["dir"])
+    oq["ray"] = rays["sample"][oq["ray"]]
+    assert len(q) == len(oq) > 0
+    assert np.array_equal(q["domain"], oq["domain"]) and np.array_equal(q["ray"], oq["ray"])
+    assert np.array_equal(bits(q["tdom"]), bits(oq["tdom"]))
+    assert np.array_equal(q["depth"], oq["depth"])
+    wb, sb = o.render_wavefront()
+    assert np.array_equal(bits(img), bits(wb))
+    assert st["rays_shadow"] == sb["rays_shadow"] and st["rays_bounce"] == sb["rays_bounce"]
+    assert img[..., :3].max() > 0
+
+
 def _hits_match(h, oh):
     same = (h["hit"] == oh["hit"]) & (h["domain"] == oh["domain"]) & (h["prim"] == oh["prim"])
     return same
