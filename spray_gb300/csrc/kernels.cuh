@@ -262,6 +262,7 @@ struct TraceArgs {
   uint64_t* rec_key;          // per entry
   float4* rec_attr;           // per entry: Ns xyz, colour bits in w
   int cull;
+  int refill;                 // occlusion: refilling walk (AO rays) instead of batches
   Counters* ctr;
 };
 

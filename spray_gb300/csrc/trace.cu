@@ -542,9 +542,9 @@ void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nbloc
 
 // Occlusion with persistent, refilling warps: each round, the lanes whose
 // entry has ended take the next entries (one warp-aggregated atomic), then
-// every busy lane advances its walk by one while-while round.  Any-hit walks
-// end early and unevenly, so refilling keeps lanes busy; closest-hit walks do
-// better with the coherence of consecutive entries.
+// every busy lane advances its walk by one while-while round.  Used for AO
+// frames, whose short bounded rays end early and unevenly; path-traced frames
+// use kTraceOccludedBatch (measured faster there).
 __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
@@ -607,9 +607,148 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(Tr
   }
 }
 
+// Any hit in (tnear, tfar) in one domain, the whole walk at once: the last
+// hit child continues, the others are pushed.  Returns true on a hit.
+__device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const TravRay& r, float tfar,
+                            Counters* ctr, uint32_t& nnodes, uint32_t& ntris) {
+  const DomArrays g = domArrays(sc, dom);
+  int stack[kStack];
+  int sp = 0, cur = 0;
+  uint32_t steps = 0;
+  while (cur != kDone) {
+    while (cur >= 0) {
+      if (++steps > (uint32_t)kMaxSteps || (unsigned)cur >= (unsigned)dom.num_nodes) {
+        raise(ctr, steps > (uint32_t)kMaxSteps ? kErrTraversalBound : kErrBadNode);
+        nnodes += steps;
+        return false;
+      }
+      float tn[4];
+      const int mask = testChildren(g.nodes, cur, r, kRayEpsilon, tfar, tn);
+      const int4 ch = loadChildren(g.nodes, cur);
+      int next = kDone;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (!(mask & (1 << c))) continue;
+        const int ref = childAt(ch, c);
+        if (ref == kEmptyChild) continue;
+        if (next != kDone) {
+          if (sp == kStack) {
+            raise(ctr, kErrTraversalBound);
+            nnodes += steps;
+            return false;
+          }
+          stack[sp++] = next;
+        }
+        next = ref;
+      }
+      cur = next != kDone ? next : (sp > 0 ? stack[--sp] : kDone);
+    }
+    if (cur == kDone) break;
+    const uint32_t v = ~(uint32_t)cur;
+    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+    if (first + cnt > (uint32_t)dom.num_tris) {
+      raise(ctr, kErrBadNode);
+      nnodes += steps;
+      return false;
+    }
+    ntris += cnt;
+    for (uint32_t q = 0; q < cnt; ++q) {
+      const float4* tp = g.tris + 3 * (size_t)(first + q);
+      const float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+      float t, u, vv;
+      if (intersectTriangle(r.sh, r.org, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(cc.x, cc.y, cc.z),
+                            kRayEpsilon, tfar, &t, &u, &vv)) {
+        nnodes += steps;
+        return true;
+      }
+    }
+    cur = sp > 0 ? stack[--sp] : kDone;
+  }
+  nnodes += steps;
+  return false;
+}
+
+// Occlusion in batches: a warp takes 32 entries at a time, drops those whose
+// shadow ray is already occluded, queues the rest in a per-warp FIFO (queue
+// order kept) and walks 32 of them together, each lane to the end of its walk.
+__global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccludedBatch(TraceArgs a) {
+  extern __shared__ uint32_t skeys[];
+  const int D = a.scene.num_domains;
+  uint32_t* sbeg = skeys + a.nkeys + 1;
+  uint32_t* spre = sbeg + a.nseg;
+  loadTables(a, skeys, sbeg, spre);
+  const uint32_t E = a.nseg > 0 ? spre[a.nseg] : *a.num_entries;
+  const int lane = threadIdx.x & 31;
+  const uint32_t below = lanesBelow();
+  __shared__ uint32_t sbuf[8][64];
+  uint32_t* buf = sbuf[threadIdx.x >> 5];
+  uint32_t visits = 0, nnodes = 0, ntris = 0;
+  int nbuf = 0;
+  bool exhausted = false;
+  while (true) {
+    while (nbuf < 32 && !exhausted) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(a.work, 32u);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= E) {
+        exhausted = true;
+        break;
+      }
+      if (base + 32u >= E) exhausted = true;
+      const uint32_t wi = base + lane;
+      bool live = false;
+      uint32_t ce = 0;
+      if (wi < E) {
+        ce = entryOf(a, sbeg, spre, wi);
+        live = !*((volatile uint8_t*)&a.sh.occluded[a.entries[ce].x & kRayIdMask]);
+      }
+      const uint32_t lm = __ballot_sync(0xffffffffu, live);
+      if (live) buf[nbuf + __popc(lm & below)] = ce;
+      nbuf += __popc(lm);
+      __syncwarp();
+    }
+    if (nbuf == 0) break;
+    const int take = min(nbuf, 32), rest = nbuf - take;
+    const bool has = lane < take;
+    const uint32_t mine = has ? buf[lane] : 0u;
+    const uint32_t moved = lane < rest ? buf[take + lane] : 0u;
+    __syncwarp();
+    if (lane < rest) buf[lane] = moved;
+    __syncwarp();
+    nbuf = rest;
+    if (!has) continue;
+    const uint32_t e = mine;
+    const uint32_t ray = a.entries[e].x & kRayIdMask;
+    if (*((volatile uint8_t*)&a.sh.occluded[ray])) continue;
+    const int d = findKey(skeys, a.nkeys, e) % D;
+    ++visits;
+    const float4 hp = a.sh.hitpos[ray / a.slots];
+    const float4 dd = a.sh.dir[ray];
+    const TravRay r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
+    if (traverseAny(a.scene, a.scene.domains[d], r, dd.w, a.ctr, nnodes, ntris)) a.sh.occluded[ray] = 1;
+    if ((nnodes | ntris) & 0x80000000u) {
+      atomicAdd(&a.ctr->nodes_shadow, (unsigned long long)nnodes);
+      atomicAdd(&a.ctr->tris_shadow, (unsigned long long)ntris);
+      nnodes = ntris = 0;
+    }
+  }
+  unsigned long long sv = visits, sn = nnodes, st = ntris;
+  for (int o = 16; o; o >>= 1) {
+    sv += __shfl_down_sync(0xffffffffu, sv, o);
+    sn += __shfl_down_sync(0xffffffffu, sn, o);
+    st += __shfl_down_sync(0xffffffffu, st, o);
+  }
+  if (lane == 0) {
+    if (sv) atomicAdd(&a.ctr->visits_shadow, sv);
+    if (sn) atomicAdd(&a.ctr->nodes_shadow, sn);
+    if (st) atomicAdd(&a.ctr->tris_shadow, st);
+  }
+}
+
 void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {
   size_t smem = (size_t)(a.nkeys + 2 + 2 * a.nseg) * 4;
-  kTraceOccluded<<<nblocks, 256, smem, s>>>(a);
+  if (a.refill) kTraceOccluded<<<nblocks, 256, smem, s>>>(a);
+  else kTraceOccludedBatch<<<nblocks, 256, smem, s>>>(a);
 }
 
 // One block per listed domain; the same cull test as kTraceClosest.

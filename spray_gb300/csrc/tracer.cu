@@ -1080,6 +1080,11 @@ TraceArgs Tracer::traceArgs(int order_by_depth, int S) {
   t.rec_key = d_rec_key;
   t.rec_attr = d_rec_attr;
   t.cull = cfg.cull;
+  // AO frames: short, bounded shadow rays whose walks end unevenly suit the
+  // refilling occlusion walk; path-traced frames the batched one (measured)
+  bool ao = fviews.empty() ? cfg.ao_mode != 0 : true;
+  for (const FrameView& v : fviews) ao = ao && v.ao_mode != 0;
+  t.refill = ao ? 1 : 0;
   t.ctr = d_ctr;
   return t;
 }
