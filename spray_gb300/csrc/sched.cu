@@ -71,7 +71,6 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
   V3 d = normalize(((ll + u * wv) + v * hv) - pos);
   rays.org[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
   rays.dir[i] = make_float4(d.x, d.y, d.z, 0.f);
-  rays.wgt[i] = make_float4(1.f, 1.f, 1.f, 0.f);
   rays.pixid[i] = y * vw.image_w + x;
   rays.samid[i] = bufid;
   rays.view[i] = (uint16_t)tl.view;

@@ -96,7 +96,9 @@ __global__ void __launch_bounds__(256, 4) kShade(ShadeArgs a) {
     }
     const float t = hitKeyT(key);
     // the sample's loads first: they do not depend on the domain search
-    const float4 o4 = a.rays.org[sample], d4 = a.rays.dir[sample], w4 = a.rays.wgt[sample];
+    // primary rays (depth 0) carry weight 1, which kGenPrimary does not store
+    const float4 o4 = a.rays.org[sample], d4 = a.rays.dir[sample];
+    const float4 w4 = a.depth == 0 ? make_float4(1.f, 1.f, 1.f, 0.f) : a.rays.wgt[sample];
     const float4 hn = a.hit_ns[sample];
     int d;
     if (stab) {

@@ -2061,7 +2061,8 @@ void Tracer::captureRays(int b) {
     r[i].sample = s;
     r[i].pixid = pix[s];
     r[i].samid = sam[s];
-    float4 o = org[s], d = dir[s], w = wgt[s];
+    // primary rays carry weight 1 (not stored: the shader knows depth 0)
+    float4 o = org[s], d = dir[s], w = b == 0 ? make_float4(1.f, 1.f, 1.f, 0.f) : wgt[s];
     float ov[3] = {o.x, o.y, o.z}, dv[3] = {d.x, d.y, d.z}, wv[3] = {w.x, w.y, w.z};
     std::memcpy(r[i].org, ov, 12);
     std::memcpy(r[i].dir, dv, 12);
