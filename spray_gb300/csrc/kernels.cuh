@@ -25,8 +25,13 @@ namespace spray {
 
 constexpr int kMaxList = 32;       // longest per-ray domain list handled
 constexpr int kMaxEmit = kMaxList + 1;  // entries per ray: list plus a shadow ray's own domain
-constexpr int kRayIdBits = 26;     // entry word 0: ray id | depth << 26 | origin << 31
+constexpr int kRayIdBits = 31;     // entry word 0: ray id | origin << 31
 constexpr uint32_t kRayIdMask = (1u << kRayIdBits) - 1u;
+// The allocation-free scheduler's entries keep the list position in bits
+// 26..30 (ray id | position << 26 | origin << 31, ray ids below 2^26).
+constexpr int kPackedIdBits = 26;
+// Shadow rays one wavefront may hold (alive samples x slots).
+constexpr int64_t kMaxWaveShadowRays = (int64_t)1 << 28;
 constexpr int kMaxSlots = 64;      // shadow rays per hit
 constexpr int kSchedThreads = 256;
 constexpr int kDepthBuckets = 4;   // key = min(depth, 3) * D + domain when ordering by depth
@@ -196,6 +201,8 @@ struct SchedArgs {
   // later ones buckets 1, 2, 3+ (null: bucket = list position, capped at 3)
   const uint8_t* pred;
   int defer_hist;             // kSchedLists leaves the histogram to the partition step
+  int pack_depth;             // entries in the packed format (kPackedIdBits)
+  uint8_t* dbg_depth;         // debug capture: list position of every entry (or null)
 };
 
 // Two fp32 values in one 64-bit register for Blackwell's packed arithmetic

@@ -146,6 +146,7 @@ extern "C" int spray_gpu_schedule_static(const float* domain_bounds, int32_t num
   a.list_cnt = s->list_cnt;
   a.hist = s->hist;
   a.nchunks = kStaticWarps;  // one chunk per warp: at most 512 rays, 16-bit counts
+  a.pack_depth = 1;  // ray | position << 26 | origin << 31, as the header documents
   a.dstats = s->dstats;
   a.entries = reinterpret_cast<uint2*>(entries);
   a.entry_cap = (unsigned long long)entry_capacity;

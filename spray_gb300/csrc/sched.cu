@@ -510,22 +510,30 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
         const uint32_t depth = (e.x >> 16) & 0x7fffu;
         const uint32_t origin = e.x >> 31;
         const uint32_t key = a.order_by_depth ? bucketOf(depth, p) * D + d : d;
-        fkey[f - w0] = key;
-        fw0[f - w0] = (rid & kRayIdMask) | (min(depth, 31u) << kRayIdBits) | (origin << 31);
+        const uint32_t pos = min(depth, 31u);
+        // the key (< 2^18) with the list position in the top byte
+        fkey[f - w0] = key | (pos << 24);
+        fw0[f - w0] = (a.pack_depth ? (rid & ((1u << kPackedIdBits) - 1u)) | (pos << kPackedIdBits)
+                                    : (rid & kRayIdMask)) |
+                      (origin << 31);
         fw1[f - w0] = e.y;
       }
       __syncwarp();
       for (uint32_t s = w0; s < w1; s += 32) {
         const uint32_t e = s + lane;
         const bool valid = e < w1;
-        const uint32_t key = valid ? fkey[e - w0] : 0xffffffffu;
+        const uint32_t kp = valid ? fkey[e - w0] : 0xffffffffu;
+        const uint32_t key = valid ? (kp & 0xffffffu) : 0xffffffffu;
         const uint32_t m = __match_any_sync(0xffffffffu, key);
         uint32_t rank = 0;
         if (valid) rank = running[key] + __popc(m & lt);
         __syncwarp();
         if (valid && (__ffs(m) - 1) == lane) running[key] += __popc(m);
         __syncwarp();
-        if (valid && rank < a.entry_cap) a.entries[rank] = make_uint2(fw0[e - w0], fw1[e - w0]);
+        if (valid && rank < a.entry_cap) {
+          a.entries[rank] = make_uint2(fw0[e - w0], fw1[e - w0]);
+          if (a.dbg_depth) a.dbg_depth[rank] = (uint8_t)(kp >> 24);
+        }
       }
       __syncwarp();
     }

@@ -428,6 +428,7 @@ void Tracer::freeBuffers() {
   devFree(d_hist);
   devFree(d_dstats);
   devFree(d_entries);
+  devFree(d_dbg_depth);
   devFree(d_key_start);
   devFree(d_num_entries);
   devFree(d_pred);
@@ -843,7 +844,10 @@ void Tracer::planWaves() {
   }
   const int S = std::max(slots(), 1);
   int64_t cap = cfg.wave_samples > 0 ? cfg.wave_samples : (int64_t)64 << 20;
-  cap = std::min<int64_t>(cap, ((int64_t)1 << kRayIdBits) / S - 1);
+  // shadow ray ids (alive index x slots + slot) stay below the entry's id
+  // field and the wavefront's shadow buffers below kMaxWaveShadowRays
+  const int64_t lim = std::min<int64_t>((int64_t)kRayIdMask, kMaxWaveShadowRays) / S;
+  cap = std::min<int64_t>(cap, lim - 1);
   waves.clear();
   size_t k = 0;
   while (k < tiles.size()) {
@@ -856,7 +860,7 @@ void Tracer::planWaves() {
       const int64_t tp = (int64_t)tiles[k].w * tiles[k].h;
       const int64_t ts = tp * fviews[tiles[k].view].spp;
       if (w.num_tiles > 0 && w.samples + ts > cap) break;
-      if (ts >= ((int64_t)1 << kRayIdBits) / S)
+      if (ts >= lim)
         throw std::invalid_argument("a blocking tile holds more rays than one wavefront can address");
       w.samples += ts;
       w.pixels += tp;
@@ -928,7 +932,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   // out (a wave uses about one chunk per 1024 rays of these, see chunksFor);
   // a chunk's per-key counts must fit 16 bits
   sched_chunks = (cfg.sched_chunks_per_warp > 0 ? cfg.sched_chunks_per_warp : 8) * sched_warps;
-  if (chunkSize((uint64_t)1 << kRayIdBits, sched_chunks) >= 65536)
+  if (chunkSize((uint64_t)std::max<int64_t>(nsamples, 1024) * S, sched_chunks) >= 65536)
     throw std::runtime_error("too few scheduling chunks for 16-bit histogram counters");
   if (nsamples <= cap_samples && cap_entries >= needed_entries && frame_pixels <= image_cap &&
       (int64_t)tiles.size() <= tiles_cap && fviews.size() <= views_cap)
@@ -974,6 +978,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_hist, (size_t)nkeys * sched_chunks);
   devAlloc(&d_dstats, (size_t)D * cfg.list_size);
   devAlloc(&d_entries, E);
+  if (cfg.debug_capture) devAlloc(&d_dbg_depth, E);  // list positions of the captured queues
   devAlloc(&d_key_start, nkeys + 1);
   devAlloc(&d_num_entries, 1);
   if (learned()) {
@@ -1041,6 +1046,7 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.entries = into_shadow_queues ? d_sentries : d_entries;
   a.entry_cap = cap_entries;
   a.key_start = into_shadow_queues ? d_skey_start : d_key_start;
+  a.dbg_depth = into_shadow_queues ? nullptr : d_dbg_depth;
   a.num_entries = into_shadow_queues ? d_snum_entries : d_num_entries;
   a.ctr = d_ctr;
   CK(cudaMemsetAsync(d_arena_top, 0, sizeof(unsigned long long), stream));
@@ -2075,6 +2081,7 @@ void Tracer::captureQueues(int what, int b, int order_by_depth) {
   const int nkeys = order_by_depth ? kDepthBuckets * D : D;
   auto ks = fetch(d_key_start, nkeys + 1, stream);
   auto ent = fetch(d_entries, E, stream);
+  std::vector<uint8_t> dep = d_dbg_depth ? fetch(d_dbg_depth, E, stream) : std::vector<uint8_t>(E, 0xff);
   std::vector<char>& out = dbg[{what, b}];
   out.resize(E * sizeof(spray_gpu_dbg_entry));
   auto* r = (spray_gpu_dbg_entry*)out.data();
@@ -2086,7 +2093,7 @@ void Tracer::captureQueues(int what, int b, int order_by_depth) {
     float t;
     std::memcpy(&t, &ent[e].y, 4);
     r[e].tdom = t;
-    r[e].depth = (int32_t)((ent[e].x >> kRayIdBits) & 31u);
+    r[e].depth = dep[e] == 0xff ? -1 : (int32_t)dep[e];
     r[e].origin = (int32_t)(ent[e].x >> 31);
   }
 }

@@ -282,6 +282,7 @@ class Tracer {
   float4* d_rec_attr = nullptr;
   unsigned int* d_work = nullptr;
   uint32_t* d_scan_tmp = nullptr;
+  uint8_t* d_dbg_depth = nullptr;  // debug capture only
   size_t scan_words = 0;
   uint32_t* d_block_tmp = nullptr;
   float4* d_image = nullptr;
