@@ -249,6 +249,29 @@ def test_waves_and_culling_do_not_change_the_image(lib_built, oracle_mod, scene6
         assert np.array_equal(bits(im), bits(imgs[0]))
 
 
+def test_large_wavefront_ray_ids(lib_built, scene64):
+    # 1024 x 1024 x 8 spp AO with 8 AO rays and the light ray: 9 shadow slots,
+    # so one wavefront numbers its shadow rays up to ~75 M (beyond 2^26); the
+    # image equals, bit for bit, the same frame cut into 1 M-sample wavefronts
+    diag = scenes.scene_diagonal(scene64)
+    cfg = small_config(image_w=1024, image_h=1024, ao_mode=1, ao_samples=8, pixel_samples=8,
+                       ao_max_distance=0.05 * diag, ao_light_shadow=1)
+    cam = scenes.orbit_camera(scene64)
+    imgs, stats = [], []
+    for kw in (dict(), dict(wave_samples=1 << 20)):
+        t = sg.Tracer(cfg, **kw)
+        t.set_scene(scene64)
+        t.set_camera(*cam)
+        img, st = t.trace()
+        imgs.append(img)
+        stats.append(st)
+        del t
+    assert stats[0]["rays_primary"] == 1024 * 1024 * 8  # one wavefront: ids up to 9 x 8.4 M
+    assert stats[0]["rays_shadow"] == stats[1]["rays_shadow"] > 0
+    assert np.array_equal(bits(imgs[0]), bits(imgs[1]))
+    assert imgs[0][..., :3].max() > 0
+
+
 @pytest.mark.parametrize("launches", [1, 4])
 def test_deterministic_frames(lib_built, scene64, launches):
     """Images and ray counts repeat exactly; with one launch per depth bucket the
