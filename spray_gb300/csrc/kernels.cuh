@@ -358,6 +358,11 @@ struct LiveArgs {
   int D;
   int cull;
   uint32_t* live;
+  // 0: exact counts.  Else a domain's counting may stop once its radiance
+  // count exceeds `cap` and, with shadows, once radiance + shadow exceed it and
+  // one live shadow entry was seen: the counts then read cap + 1 or more (the
+  // caller only compares them with cap and with 0).
+  uint32_t cap;
 };
 void launchCountLive(cudaStream_t s, const LiveArgs& a);
 

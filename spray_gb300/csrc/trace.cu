@@ -751,47 +751,63 @@ void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {
   else kTraceOccludedBatch<<<nblocks, 256, smem, s>>>(a);
 }
 
-// One block per listed domain; the same cull test as kTraceClosest.
+// One block per listed domain; the same cull test as kTraceClosest.  The
+// entries are taken in rounds of 8 per thread; with a cap, the block stops
+// after the round in which its counts settle the caller's questions (over the
+// cap; with shadows, also one live shadow entry).  Culled radiance entries of
+// the rounds counted get rec_key = kNoHit; a domain whose counting stopped
+// early has live entries and is traced, which writes every entry's record.
+__device__ __forceinline__ uint32_t blockSum(uint32_t v, uint32_t* ws) {
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) ws[warp] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+  return t;
+}
+
 __global__ void __launch_bounds__(256) kCountLive(LiveArgs a) {
-  __shared__ uint32_t wsum[2][8];
+  __shared__ uint32_t ws[8];
   const int d = a.domains[blockIdx.x];
-  uint32_t nr = 0, ns = 0;
-  for (int b = a.rbucket0; a.rentries && b < a.rbucket0 + a.rbuckets; ++b) {
+  const uint32_t round = 8 * blockDim.x;
+  uint32_t nr = 0, ns = 0;  // block totals of the rounds counted
+  bool stop = false;
+  for (int b = a.rbucket0; a.rentries && b < a.rbucket0 + a.rbuckets && !stop; ++b) {
     const uint32_t e0 = a.rkey_start[b * a.D + d], e1 = a.rkey_start[b * a.D + d + 1];
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const uint2 ent = a.rentries[e];
-      bool live = true;
-      if (a.cull) {
-        const uint64_t cur = a.ray_key[ent.x & kRayIdMask];
-        live = !(cur != kNoHit && __uint_as_float(ent.y) > hitKeyT(cur));
+    for (uint32_t r0 = e0; r0 < e1 && !stop; r0 += round) {
+      uint32_t c = 0;
+      const uint32_t r1 = min(e1, r0 + round);
+      for (uint32_t e = r0 + threadIdx.x; e < r1; e += blockDim.x) {
+        const uint2 ent = a.rentries[e];
+        bool live = true;
+        if (a.cull) {
+          const uint64_t cur = a.ray_key[ent.x & kRayIdMask];
+          live = !(cur != kNoHit && __uint_as_float(ent.y) > hitKeyT(cur));
+        }
+        if (live) ++c;
+        else a.rec_key[e] = kNoHit;
       }
-      if (live) ++nr;
-      else a.rec_key[e] = kNoHit;
+      nr += blockSum(c, ws);
+      stop = a.cap && nr > a.cap;
     }
   }
   if (a.sentries) {
     const uint32_t e0 = a.skey_start[d], e1 = a.skey_start[d + 1];
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x)
-      if (!a.occluded[a.sentries[e].x & kRayIdMask]) ++ns;
-  }
-  for (int o = 16; o; o >>= 1) {
-    nr += __shfl_down_sync(0xffffffffu, nr, o);
-    ns += __shfl_down_sync(0xffffffffu, ns, o);
-  }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) {
-    wsum[0][warp] = nr;
-    wsum[1][warp] = ns;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t tr = 0, ts = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      tr += wsum[0][w];
-      ts += wsum[1][w];
+    stop = false;
+    for (uint32_t r0 = e0; r0 < e1 && !stop; r0 += round) {
+      uint32_t c = 0;
+      const uint32_t r1 = min(e1, r0 + round);
+      for (uint32_t e = r0 + threadIdx.x; e < r1; e += blockDim.x)
+        if (!a.occluded[a.sentries[e].x & kRayIdMask]) ++c;
+      ns += blockSum(c, ws);
+      stop = a.cap && ns > 0 && nr + ns > a.cap;
     }
-    a.live[d] = tr;
-    a.live[a.D + d] = ts;
+  }
+  if (threadIdx.x == 0) {
+    a.live[d] = nr;
+    a.live[a.D + d] = ns;
   }
 }
 

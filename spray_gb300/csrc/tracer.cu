@@ -1359,6 +1359,9 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int 
       la.D = D;
       la.cull = cfg.cull;
       la.live = d_live;
+      // the batched orders compare counts only with ooc_inplace and 0; the
+      // most-pending-first order of the non-speculative policy sorts by them
+      la.cap = by_live ? 0u : (uint32_t)std::max<int64_t>(cfg.ooc_inplace, 0);
       launchCountLive(stream, la);
       launches += 1;
       CK(cudaMemcpyAsync(hlive, d_live, 2 * (size_t)D * 4, cudaMemcpyDeviceToHost, stream));
