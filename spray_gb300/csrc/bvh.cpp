@@ -329,4 +329,67 @@ void buildDomainBvh(const float* boxes, int n, std::vector<DomNode>* out) {
   b.build(0, n);
 }
 
+namespace {
+
+struct DomCollapse {
+  const std::vector<DomNode>& bin;
+  std::vector<BvhNode4>* out;
+
+  static void setSlot(BvhNode4& nd, int k, const float lo[3], const float hi[3], int32_t child) {
+    nd.lox[k] = lo[0];
+    nd.loy[k] = lo[1];
+    nd.loz[k] = lo[2];
+    nd.hix[k] = hi[0];
+    nd.hiy[k] = hi[1];
+    nd.hiz[k] = hi[2];
+    nd.child[k] = child;
+  }
+
+  // 4-wide node for binary inner node b; returns its index.
+  int emit(int b) {
+    const int id = (int)out->size();
+    out->emplace_back();
+    BvhNode4 nd;
+    std::memset(&nd, 0, sizeof(nd));
+    for (int k = 0; k < 4; ++k) {
+      const float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      setSlot(nd, k, lo, hi, kEmptyChild);
+    }
+    int pending[4] = {-1, -1, -1, -1};  // binary inner node behind each slot
+    int k = 0;
+    for (int s = 0; s < 2; ++s) {
+      const DomNode& n = bin[b];
+      const int32_t c = s ? n.c1 : n.c0;
+      if (c < 0) {
+        setSlot(nd, k++, s ? n.lo1 : n.lo0, s ? n.hi1 : n.hi0, c);
+        continue;
+      }
+      const DomNode& m = bin[c];
+      for (int t = 0; t < 2; ++t) {
+        const int32_t g = t ? m.c1 : m.c0;
+        setSlot(nd, k, t ? m.lo1 : m.lo0, t ? m.hi1 : m.hi0, g);
+        if (g >= 0) pending[k] = g;
+        ++k;
+      }
+    }
+    (*out)[id] = nd;
+    for (int q = 0; q < 4; ++q)
+      if (pending[q] >= 0) {
+        const int child = emit(pending[q]);
+        (*out)[id].child[q] = child;
+      }
+    return id;
+  }
+};
+
+}  // namespace
+
+void buildDomainBvh4(const float* boxes, int n, std::vector<BvhNode4>* out) {
+  std::vector<DomNode> bin;
+  buildDomainBvh(boxes, n, &bin);
+  out->clear();
+  DomCollapse c{bin, out};
+  c.emit(0);
+}
+
 }  // namespace spray

@@ -42,6 +42,12 @@ static_assert(sizeof(DomNode) == 64, "domain node must be 64 bytes");
 // boxes: 6 floats per domain (min xyz, max xyz); n >= 2.
 void buildDomainBvh(const float* boxes, int n, std::vector<DomNode>* out);
 
+// The same hierarchy collapsed to 4-wide nodes in the BvhNode4 layout (root
+// at 0): each node holds the children of its binary node's children (a leaf
+// child keeps its own slot), boxes unchanged (enlarged outward), child < 0 a
+// leaf ~domain, unused slots empty (lo = +inf, hi = -inf, kEmptyChild).
+void buildDomainBvh4(const float* boxes, int n, std::vector<BvhNode4>* out);
+
 struct BvhBuildResult {
   std::vector<BvhNode4> nodes;     // nodes[0] is the root
   std::vector<uint32_t> tri_order;  // leaf order -> original face index

@@ -175,7 +175,7 @@ struct SchedArgs {
   int order_by_depth;         // key = min(depth,3)*D + domain, else domain
   int list_size;              // SPRAY_RAY_DOMAIN_LIST_SIZE, for the domain statistics
   uint64_t* ray_key;          // radiance: reset to kNoHit per scheduled ray
-  const DomNode* dnodes;      // hierarchy over the domain boxes (null: test every domain)
+  const BvhNode4* dnodes;     // 4-wide hierarchy over the domain boxes (null: test every domain)
   int dnode_count;
   // primary rays: candidate domains per screen bin (null: not primary rays)
   const uint32_t* bin_start;  // [bins_x * bins_y + 1]

@@ -97,14 +97,19 @@ void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles
 // per-(key, warp) histogram to global memory.
 __device__ __forceinline__ bool fitsList(int cnt, int j) { return j < cnt; }
 
-__global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
+// kMinBlocks 6 caps the kernel at 40 registers (a few spills) so that six
+// blocks fit an SM when shared memory allows; with larger domain tables
+// shared memory holds fewer blocks and the variant for five (48 registers,
+// no spills) runs instead.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kSchedThreads, kMinBlocks) kSchedLists(SchedArgs a,
                                                              const DomainDev* __restrict__ doms,
                                                              int D, int nkeys, int nwarps) {
   extern __shared__ uint32_t smem[];
   const int NN = a.dnode_count;
-  float4* snode = reinterpret_cast<float4*>(smem);  // 4 float4 per hierarchy node
-  float* sbox = reinterpret_cast<float*>(smem + 16 * NN);
-  uint32_t* hist = smem + 16 * NN + 6 * D;  // per warp: nkeys 16-bit counters, packed in pairs
+  float4* snode = reinterpret_cast<float4*>(smem);  // 8 float4 per hierarchy node (BvhNode4)
+  float* sbox = reinterpret_cast<float*>(smem + 32 * NN);
+  uint32_t* hist = smem + 32 * NN + 6 * D;  // per warp: nkeys 16-bit counters, packed in pairs
   const int hwords = (nkeys + 1) >> 1;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int d = threadIdx.x; d < D; d += blockDim.x) {
@@ -113,7 +118,7 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
       sbox[6 * d + 3 + c] = doms[d].bmax[c];
     }
   }
-  for (int k = threadIdx.x; k < 4 * NN; k += blockDim.x)
+  for (int k = threadIdx.x; k < 8 * NN; k += blockDim.x)
     snode[k] = reinterpret_cast<const float4*>(a.dnodes)[k];
   uint32_t* h = hist + (size_t)wib * hwords;
   __syncthreads();
@@ -186,46 +191,64 @@ __global__ void __launch_bounds__(kSchedThreads) kSchedLists(SchedArgs a,
       } else if (NN == 0) {
         for (int d = 0; d < D; ++d) consider(d);
       } else {
-        // conservative descent of the domain hierarchy, exact test at the leaves
+        // conservative descent of the 4-wide domain hierarchy (the node boxes
+        // are enlarged outward, the test widened by 2 ulp), exact slab test at
+        // the leaves; children near to far, so that domains arrive roughly in
+        // entry order and the sorted insertion above is mostly an append
         const int sx = inv.x < 0.0f, sy = inv.y < 0.0f, sz = inv.z < 0.0f;
         const float tfar = t1 * 1.0000004f;
-        int stack[40];
+        int stack[32];
         int sp = 0;
         int node = 0;
-        for (int steps = 0; steps < 4 * NN + 4; ++steps) {
-          const float4 l0 = snode[4 * node], h0 = snode[4 * node + 1];
-          const float4 l1 = snode[4 * node + 2], h1 = snode[4 * node + 3];
-          int next = -1;
-          float tn[2];
-          bool hit[2];
-          for (int c = 0; c < 2; ++c) {
-            const float4 lo = c ? l1 : l0, hi = c ? h1 : h0;
-            const float nx = sx ? hi.x : lo.x, fx = sx ? lo.x : hi.x;
-            const float ny = sy ? hi.y : lo.y, fy = sy ? lo.y : hi.y;
-            const float nz = sz ? hi.z : lo.z, fz = sz ? lo.z : hi.z;
-            const float t0 = fmaxf(fmaxf((nx - org.x) * inv.x, (ny - org.y) * inv.y),
-                                   fmaxf((nz - org.z) * inv.z, kRayEpsilon));
-            const float tt = fminf(fminf((fx - org.x) * inv.x, (fy - org.y) * inv.y),
-                                   fminf((fz - org.z) * inv.z, tfar)) * 1.0000004f;
-            hit[c] = t0 <= tt;
-            tn[c] = t0;
+        for (int steps = 0; steps < NN + 4; ++steps) {
+          const float4* nd = snode + 8 * node;
+          const float4 nx = nd[sx], fx = nd[sx ^ 1], ny = nd[2 + sy], fy = nd[3 - sy];
+          const float4 nz = nd[4 + sz], fz = nd[5 - sz];
+          const int4 ch = *reinterpret_cast<const int4*>(nd + 6);
+          const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
+          const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
+          const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
+          const int cha[4] = {ch.x, ch.y, ch.z, ch.w};
+          uint32_t k[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const float t0 = fmaxf(fmaxf((nxa[c] - org.x) * inv.x, (nya[c] - org.y) * inv.y),
+                                   fmaxf((nza[c] - org.z) * inv.z, kRayEpsilon));
+            const float tt = fminf(fminf((fxa[c] - org.x) * inv.x, (fya[c] - org.y) * inv.y),
+                                   fminf((fza[c] - org.z) * inv.z, tfar)) * 1.0000004f;
+            // (entry t with the slot in its two low bits: t > 0 orders like its bits)
+            k[c] = (t0 <= tt && cha[c] != kEmptyChild) ? ((__float_as_uint(t0) & ~3u) | (uint32_t)c)
+                                                        : 0xffffffffu;
           }
-          // nearer child first, so leaves arrive roughly in entry order and the
-          // sorted insertion above is mostly an append
-          const int first = (hit[1] && (!hit[0] || tn[1] < tn[0])) ? 1 : 0;
-          for (int k = 0; k < 2; ++k) {
-            const int c = k ^ first;
-            if (!hit[c]) continue;
-            const int ref = __float_as_int(c ? l1.w : l0.w);
+          auto cswap = [](uint32_t& x, uint32_t& y) {
+            const uint32_t lo = min(x, y), hi = max(x, y);
+            x = lo;
+            y = hi;
+          };
+          cswap(k[0], k[1]);
+          cswap(k[2], k[3]);
+          cswap(k[0], k[2]);
+          cswap(k[1], k[3]);
+          cswap(k[1], k[2]);
+          int inner[4], ni = 0;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (k[j] == 0xffffffffu) break;
+            const int ref = cha[k[j] & 3u];
             if (ref < 0) consider(~ref);
-            else if (next < 0) next = ref;
-            else if (sp < 40) stack[sp++] = ref;
+            else inner[ni++] = ref;
           }
-          if (next < 0) {
+          // the nearest inner child next, the others on the stack far to near
+          for (int j = ni - 1; j >= 1; --j) {
+            if (sp < 32) stack[sp++] = inner[j];
+            else atomicAdd(&a.ctr->list_overflows, 1ull);  // unreachable: depth <= 8, 3 per level
+          }
+          if (ni > 0) {
+            node = inner[0];
+          } else {
             if (sp == 0) break;
-            next = stack[--sp];
+            node = stack[--sp];
           }
-          node = next;
         }
       }
       if (a.shadow) {
@@ -576,25 +599,42 @@ __global__ void __launch_bounds__(128) kSchedHist(SchedArgs a, int D, int nkeys,
 }
 
 static size_t listsSmem(int D, int nkeys, int dnode_count) {
-  return (size_t)dnode_count * 64 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * ((nkeys + 1) / 2) * 4;
+  return (size_t)dnode_count * 128 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * ((nkeys + 1) / 2) * 4;
 }
 
-int schedBlocksPerSm(int D, int nkeys, int dnode_count) {
-  size_t smem = listsSmem(D, nkeys, dnode_count);
-  cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// Resident blocks per SM of a kSchedLists variant with this shared memory.
+template <int kMinBlocks>
+static int listsOccupancy(size_t smem) {
+  cudaFuncSetAttribute(kSchedLists<kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int bps = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kSchedLists, kSchedThreads, smem) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kSchedLists<kMinBlocks>, kSchedThreads, smem) !=
+          cudaSuccess ||
       bps < 1)
     bps = 1;
   return bps;
 }
 
+// The register-capped variant when shared memory lets six blocks share an SM.
+static bool listsCapped(size_t smem) { return listsOccupancy<6>(smem) >= 6; }
+
+int schedBlocksPerSm(int D, int nkeys, int dnode_count) {
+  const size_t smem = listsSmem(D, nkeys, dnode_count);
+  return listsCapped(smem) ? listsOccupancy<6>(smem) : listsOccupancy<5>(smem);
+}
+
 void launchSchedLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
                       int nblocks) {
   const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
-  size_t smem1 = listsSmem(D, nkeys, a.dnode_count);
-  cudaFuncSetAttribute(kSchedLists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-  kSchedLists<<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
+  // the variant is chosen for the allocation's key count (4 D), as in schedBlocksPerSm
+  const bool capped = listsCapped(listsSmem(D, kDepthBuckets * D, a.dnode_count));
+  const size_t smem1 = listsSmem(D, nkeys, a.dnode_count);
+  if (capped) {
+    cudaFuncSetAttribute(kSchedLists<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    kSchedLists<6><<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
+  } else {
+    cudaFuncSetAttribute(kSchedLists<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    kSchedLists<5><<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
+  }
 }
 
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,

@@ -608,11 +608,11 @@ void Tracer::installScene(std::vector<DomainPack>& packs, const spray_gpu_light*
         boxes[6 * d + c] = hdoms[d].bmin[c];
         boxes[6 * d + 3 + c] = hdoms[d].bmax[c];
       }
-    std::vector<DomNode> dn;
-    buildDomainBvh(boxes.data(), nd, &dn);
+    std::vector<BvhNode4> dn;
+    buildDomainBvh4(boxes.data(), nd, &dn);
     dnode_count = (int)dn.size();
     devAlloc(&d_dnodes, dn.size());
-    CK(cudaMemcpy(d_dnodes, dn.data(), dn.size() * sizeof(DomNode), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_dnodes, dn.data(), dn.size() * sizeof(BvhNode4), cudaMemcpyHostToDevice));
   }
   std::vector<float> lf(13 * std::max(nl, 1), 0.f);
   for (int l = 0; l < nl; ++l) {

@@ -200,7 +200,7 @@ class Tracer {
   std::vector<size_t> host_off;   // per domain offset into h_pinned
   char* h_stage = nullptr;        // pinned staging of the domain and segment tables
   uint32_t* d_segs = nullptr;
-  DomNode* d_dnodes = nullptr;   // hierarchy over the domain boxes
+  BvhNode4* d_dnodes = nullptr;  // 4-wide hierarchy over the domain boxes
   int dnode_count = 0;
   // screen bins of candidate domains for the primary rays
   static constexpr int kBinShift = 4;
