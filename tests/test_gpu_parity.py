@@ -205,6 +205,7 @@ def test_occlusion_and_shadow_queues(lib_built, oracle_mod, scene64):
 @pytest.mark.parametrize("mode,spp,bounces,light", [
     ("ao", 1, 1, "point"), ("ao", 2, 2, "point"), ("pt", 1, 1, "point"),
     ("pt", 2, 3, "point+diffuse"), ("pt", 4, 4, "point+diffuse"), ("pt", 2, 3, "quad"),
+    ("pt", 32, 2, "point"),  # 256 pixels x 32 spp: retire reads alive indices unstaged
 ])
 def test_image_matches_oracles(lib_built, oracle_mod, mode, spp, bounces, light):
     sc = scenes.wavelet_grid(2, 24, colors="albedo", light=light)
