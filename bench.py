@@ -73,6 +73,14 @@ def clock_sampler(out: Path):
         return None, None
 
 
+def smi_index(local: int) -> int:
+    """nvidia-smi index of this process's CUDA device (CUDA_VISIBLE_DEVICES may remap it)."""
+    vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    if local < len(vis) and vis[local].isdigit():
+        return int(vis[local])
+    return local
+
+
 def clock_summary(path: Path, device: int) -> dict | None:
     try:
         rows = [l.split(",") for l in path.read_text().splitlines() if l.strip()]
@@ -327,7 +335,7 @@ def main():
         proc.terminate()
         proc.wait()
         fh.close()
-    clocks = clock_summary(clk_path, local)
+    clocks = clock_summary(clk_path, smi_index(local))
 
     s0 = stats[-1]
     peak, peak_kind = hbm_peak()
