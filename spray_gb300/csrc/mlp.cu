@@ -242,11 +242,14 @@ struct ArenaRows {
 // Forward shared memory: W1 W2 W3 (8 KB each), W4 (2 KB), activations (16 KB),
 // biases, the mbarrier and the tensor-memory address.
 constexpr int kFwdW = 0, kFwdW4 = 3 * 8192, kFwdAct = kFwdW4 + 2048, kFwdBias = kFwdAct + 16384;
-// The request is padded to 50 KB so that at most four CTAs (4 x 128 tensor-
-// memory columns = all 512) are resident per SM and an allocation never waits.
-constexpr int kFwdBar = kFwdBias + (3 * kHid + kOutPad) * 4, kFwdSmem = 50 * 1024;
+// 44 KB: five CTAs share an SM (5 x 64 tensor-memory columns of the 512), so
+// a tensor-memory allocation never waits.
+constexpr int kFwdBar = kFwdBias + (3 * kHid + kOutPad) * 4, kFwdSmem = 44 * 1024;
 static_assert(kFwdBar + 16 <= kFwdSmem, "forward shared memory");
-constexpr uint32_t kFwdCols = 128;  // D0: columns 0..63, logits: 64..79
+// D0: columns 0..63; the logits reuse columns 0..15 once layer 3's output has
+// been read back (the tcgen05 fences around the barrier order the read before
+// the next MMA, as between the hidden layers)
+constexpr uint32_t kFwdCols = 64;
 
 template <class Rows>
 __global__ void __launch_bounds__(kTile) kForward(Net net, Rows rows) {
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(kTile) kForward(Net net, Rows rows) {
       if (t == 0) {
         fenceAfterSync();
         if (l < 3) gemm(tm, b_act, 8, b_w + 8192 * l, 8, kK, kHid, false);
-        else gemm(tm + 64, b_act, 8, b_w4, 8, kHid, kOutPad, false);
+        else gemm(tm, b_act, 8, b_w4, 8, kHid, kOutPad, false);
         commit(mbar);
       }
       ok = __syncthreads_and(mbarWait(mbar, phase));
@@ -308,7 +311,7 @@ __global__ void __launch_bounds__(kTile) kForward(Net net, Rows rows) {
         fenceProxyAsync();
       } else {
         float z[16];
-        tmemLd16(tm + lane_base + 64, z);
+        tmemLd16(tm + lane_base, z);
         float lg[kCand];
         int best = 0;
         for (int c = 0; c < kCand; ++c) {

@@ -1057,7 +1057,7 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
     mlp::ArenaSource src = arenaSource();
     src.count = count;
     src.list = list;
-    mlp::launchPredictArena(stream, proposalNet(), src, d_pred, num_sms * 4);
+    mlp::launchPredictArena(stream, proposalNet(), src, d_pred, num_sms * 5);  // 5 CTAs per SM
     a.pred = d_pred;
     launchSchedPartition(stream, a, D, sched_warps, d_scan_tmp, scan_words);
     launches += 7;
@@ -1690,7 +1690,7 @@ void Tracer::collectPairs() {
 void Tracer::predictDomainCounts(bool run_predict) {
   CK(cudaMemsetAsync(d_predcount, 0, (size_t)D * 4, stream));
   if (run_predict) {
-    mlp::launchPredictArena(stream, proposalNet(), arenaSource(), d_pred, num_sms * 4);
+    mlp::launchPredictArena(stream, proposalNet(), arenaSource(), d_pred, num_sms * 5);
     launches += 1;
   }
   mlp::launchPredCount(stream, arenaSource(), d_pred, d_predcount, num_sms * 4);
