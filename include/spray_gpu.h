@@ -68,7 +68,7 @@ typedef struct spray_gpu_config {
   int32_t rr_depth;             /* Russian roulette on bounce rays from this depth; 0 = off (0) */
   int32_t cull;                 /* skip (ray, domain) pairs entered beyond the closest hit found so far (1) */
   int64_t cache_bytes;          /* device domain-cache cap in bytes; 0 = use cache_size (0) */
-  int64_t wave_samples;         /* samples traced per wavefront; 0 = library default (0) */
+  int64_t wave_samples;         /* samples per wavefront; 0 = up to 64 M (always at most 2^28 / shadow slots) */
   int32_t debug_capture;        /* keep the first wavefront's stage buffers for the debug hooks (0) */
   int32_t device;               /* CUDA device ordinal (0) */
   int32_t schedule_policy;      /* out-of-core domain order: 0 DomainStats score order (the
@@ -292,7 +292,7 @@ typedef struct spray_gpu_dbg_ray {
  * src/ooc/ooc_tcontext.inl:73-91). */
 typedef struct spray_gpu_dbg_entry {
   int32_t domain;
-  uint32_t ray;      /* radiance: sample index; shadow: sample * slots + slot */
+  uint32_t ray;      /* radiance: sample index; shadow: alive index * slots + slot */
   float tdom;
   int32_t depth;
   int32_t origin;
