@@ -292,6 +292,12 @@ struct ShadeArgs {
   const float* lights;        // 13 floats per light: type, pos, radiance, e1, e2
   int num_lights;
   Counters* ctr;
+  // Optional (null: not written): per block, the shadow rays and the bounce
+  // rays it emitted.  Block b shades alive rays [b * per, (b + 1) * per) with
+  // per = ceil(alive / blocks), the ranges of the compaction passes launched
+  // with as many blocks, which then need no count pass.
+  uint32_t* blk_shadow;
+  uint32_t* blk_next;
 };
 
 // ---------------------------------------------------------------- launchers
@@ -332,6 +338,11 @@ void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, u
 // list must not alias src.
 void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,
                        uint32_t* list, uint32_t* count, int32_t* index_of, uint32_t* block_tmp, int nblocks);
+// The scan and write passes of launchCompact / launchCompactList when
+// block_tmp already holds each block's kept count (kShade's block counts).
+void launchCompactCounted(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
+                          uint32_t* list, uint32_t* count, int32_t* index_of, const uint32_t* src,
+                          uint32_t* block_tmp, int nblocks);
 void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
                       const ViewDev* views, const int32_t* alive_idx, const ShadowBuf sh,
                       const uint8_t* flag, int slots, int nblocks);

@@ -670,12 +670,19 @@ void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int D, int nwarps,
 }
 
 // ---------------------------------------------------------------- compaction
+// Elements per block of the compaction passes: whole groups of n_mul (the
+// shadow slots of one alive ray), so that a block's range is the range of
+// alive rays a shader block with the same grid covered (kShade's block counts).
+__host__ __device__ __forceinline__ uint64_t compactPer(uint64_t units, uint32_t n_mul, uint32_t blocks) {
+  return (units + blocks - 1) / blocks * n_mul;
+}
+
 __global__ void kCompactCount(const uint8_t* __restrict__ flag, const uint32_t* n_dev,
                               uint32_t n_mul, uint64_t n_host, uint32_t* block_tmp,
                               const uint32_t* __restrict__ src) {
   __shared__ uint32_t ws[32];
   const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
-  const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const uint64_t per = compactPer(n_dev ? *n_dev : n_host, n_dev ? n_mul : 1u, gridDim.x);
   const uint64_t b0 = min(n, per * blockIdx.x), b1 = min(n, b0 + per);
   uint32_t c = 0;
   for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) c += flag[src ? src[i] : i] != 0;
@@ -718,7 +725,7 @@ __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* 
                               uint32_t* list, int32_t* index_of, const uint32_t* __restrict__ src) {
   __shared__ uint32_t ws[33];
   const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
-  const uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const uint64_t per = compactPer(n_dev ? *n_dev : n_host, n_dev ? n_mul : 1u, gridDim.x);
   const uint64_t b0 = min(n, per * blockIdx.x), b1 = min(n, b0 + per);
   uint32_t base = block_tmp[blockIdx.x];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -760,6 +767,13 @@ void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, u
   kCompactCount<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp, nullptr);
   kCompactScan<<<1, 1024, 0, s>>>(block_tmp, nblocks, count);
   kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, n_host, block_tmp, list, index_of, nullptr);
+}
+
+void launchCompactCounted(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
+                          uint32_t* list, uint32_t* count, int32_t* index_of, const uint32_t* src,
+                          uint32_t* block_tmp, int nblocks) {
+  kCompactScan<<<1, 1024, 0, s>>>(block_tmp, nblocks, count);
+  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, 0, block_tmp, list, index_of, src);
 }
 
 void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,

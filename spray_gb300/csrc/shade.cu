@@ -84,8 +84,10 @@ __global__ void __launch_bounds__(256, 4) kShade(ShadeArgs a) {
   const uint32_t n = *a.count;
   const int S = a.slots;
   unsigned long long nshadow = 0, nbounce = 0;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  // a contiguous range of alive rays per block (the compaction's partition)
+  const uint64_t per = ((uint64_t)n + gridDim.x - 1) / gridDim.x;
+  const uint64_t i0 = min((uint64_t)n, per * blockIdx.x), i1 = min((uint64_t)n, i0 + per);
+  for (uint64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const uint32_t sample = a.list[i];
     const uint64_t key = a.ray_key[sample];
     a.next_flag[sample] = 0;  // set below when a bounce ray is emitted
@@ -319,6 +321,21 @@ __global__ void __launch_bounds__(256, 4) kShade(ShadeArgs a) {
   if ((threadIdx.x & 31) == 0) {
     if (nshadow) atomicAdd(&a.ctr->rays_shadow, nshadow);
     if (nbounce) atomicAdd(&a.ctr->rays_bounce, nbounce);
+  }
+  if (a.blk_shadow) {
+    // this block's kept counts for the two compactions that follow
+    __shared__ unsigned int bsum[2];
+    if (threadIdx.x == 0) bsum[0] = bsum[1] = 0u;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&bsum[0], (unsigned int)nshadow);
+      atomicAdd(&bsum[1], (unsigned int)nbounce);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      a.blk_shadow[blockIdx.x] = bsum[0];
+      a.blk_next[blockIdx.x] = bsum[1];
+    }
   }
 }
 

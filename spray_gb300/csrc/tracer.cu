@@ -445,6 +445,7 @@ void Tracer::freeBuffers() {
   devFree(d_work);
   devFree(d_scan_tmp);
   devFree(d_block_tmp);
+  devFree(d_block_tmp2);
   devFree(d_image);
   devFree(d_scores);
   devFree(d_order);
@@ -1001,6 +1002,7 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_scan_tmp, scan_words);
   compact_blocks = num_sms * kCompactBlocksPerSm;
   devAlloc(&d_block_tmp, compact_blocks);
+  devAlloc(&d_block_tmp2, compact_blocks);  // the shader's bounce counts per block
   devAlloc(&d_image, (size_t)std::max<int64_t>(frame_pixels, 1));
   image_cap = frame_pixels;
   devAlloc(&d_views, std::max<size_t>(fviews.size(), 1));
@@ -1221,12 +1223,17 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     if (learned() && !proposal_trained) collectPairs();
     if (capture) captureHits(b);
     // shade
-    launchShade(stream, shadeArgs(b, S), nblk);  // writes the next-depth flag of every alive ray
+    // the shader writes the next-depth flag of every alive ray and, per block,
+    // the kept counts of the two compactions below (same partition)
+    ShadeArgs sa = shadeArgs(b, S);
+    sa.blk_shadow = d_block_tmp;
+    sa.blk_next = d_block_tmp2;
+    launchShade(stream, sa, compact_blocks);
     launches += 1;
     // shadow rays -> queues -> occlusion
-    launchCompact(stream, d_shadow_flag, d_alive_count, (uint32_t)S, 0, d_shadow_list, d_shadow_count,
-                  nullptr, d_block_tmp, compact_blocks);
-    launches += 3;
+    launchCompactCounted(stream, d_shadow_flag, d_alive_count, (uint32_t)S, d_shadow_list, d_shadow_count,
+                         nullptr, nullptr, d_block_tmp, compact_blocks);
+    launches += 2;
     // In core the shadow entries are sorted by list position (the ray's own
     // domain first): the occlusion walk takes them in that order, so an
     // occluder found near the ray culls its entries in farther domains.
@@ -1258,11 +1265,11 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     if (b + 1 < nb_total) {
       // compact this depth's alive list (not every sample of the wave): samples
       // that stop get index -1, the ones dead before keep theirs (-1)
-      launchCompactList(stream, d_alive_list, d_alive_count, d_next_flag, d_alive_list2, d_alive_count2,
-                        d_alive_idx, d_block_tmp, compact_blocks);
+      launchCompactCounted(stream, d_next_flag, d_alive_count, 1, d_alive_list2, d_alive_count2, d_alive_idx,
+                           d_alive_list, d_block_tmp2, compact_blocks);
       std::swap(d_alive_list, d_alive_list2);
       std::swap(d_alive_count, d_alive_count2);
-      launches += 3;
+      launches += 2;
       cur ^= 1;
     }
   }

@@ -283,6 +283,7 @@ class Tracer {
   unsigned int* d_work = nullptr;
   uint32_t* d_scan_tmp = nullptr;
   uint8_t* d_dbg_depth = nullptr;  // debug capture only
+  uint32_t* d_block_tmp2 = nullptr;  // compaction counts from the shader
   size_t scan_words = 0;
   uint32_t* d_block_tmp = nullptr;
   float4* d_image = nullptr;
