@@ -338,8 +338,9 @@ void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, u
 // list must not alias src.
 void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,
                        uint32_t* list, uint32_t* count, int32_t* index_of, uint32_t* block_tmp, int nblocks);
-// The scan and write passes of launchCompact / launchCompactList when
-// block_tmp already holds each block's kept count (kShade's block counts).
+// The write pass of launchCompact / launchCompactList when block_tmp already
+// holds each block's kept count (kShade's block counts): each block adds the
+// counts before its own, the last writes *count.  One launch.
 void launchCompactCounted(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
                           uint32_t* list, uint32_t* count, int32_t* index_of, const uint32_t* src,
                           uint32_t* block_tmp, int nblocks);

@@ -720,14 +720,31 @@ __global__ void __launch_bounds__(1024) kCompactScan(uint32_t* block_tmp, int nb
   if (threadIdx.x == 1023) *count = part[1023];
 }
 
+// block_tmp holds each block's first output position, or with `count` set,
+// each block's kept count: the block then adds the counts before its own and
+// the last block writes the total to *count (no separate scan launch).
 __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* n_dev,
                               uint32_t n_mul, uint64_t n_host, const uint32_t* block_tmp,
-                              uint32_t* list, int32_t* index_of, const uint32_t* __restrict__ src) {
+                              uint32_t* list, int32_t* index_of, const uint32_t* __restrict__ src,
+                              uint32_t* count = nullptr) {
   __shared__ uint32_t ws[33];
   const uint64_t n = n_dev ? (uint64_t)(*n_dev) * n_mul : n_host;
   const uint64_t per = compactPer(n_dev ? *n_dev : n_host, n_dev ? n_mul : 1u, gridDim.x);
   const uint64_t b0 = min(n, per * blockIdx.x), b1 = min(n, b0 + per);
-  uint32_t base = block_tmp[blockIdx.x];
+  uint32_t base;
+  if (count) {
+    uint32_t sum = 0;
+    for (uint32_t k = threadIdx.x; k < blockIdx.x; k += blockDim.x) sum += block_tmp[k];
+    for (int o = 16; o; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    base = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) base += ws[k];
+    __syncthreads();
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *count = base + block_tmp[blockIdx.x];
+  } else {
+    base = block_tmp[blockIdx.x];
+  }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t lt = laneMaskLt();
   for (uint64_t s = b0; s < b1; s += blockDim.x) {
@@ -772,8 +789,7 @@ void launchCompact(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, u
 void launchCompactCounted(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
                           uint32_t* list, uint32_t* count, int32_t* index_of, const uint32_t* src,
                           uint32_t* block_tmp, int nblocks) {
-  kCompactScan<<<1, 1024, 0, s>>>(block_tmp, nblocks, count);
-  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, 0, block_tmp, list, index_of, src);
+  kCompactWrite<<<nblocks, 256, 0, s>>>(flag, n_dev, n_mul, 0, block_tmp, list, index_of, src, count);
 }
 
 void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_dev, const uint8_t* flag,

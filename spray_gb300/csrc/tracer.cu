@@ -1233,7 +1233,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     // shadow rays -> queues -> occlusion
     launchCompactCounted(stream, d_shadow_flag, d_alive_count, (uint32_t)S, d_shadow_list, d_shadow_count,
                          nullptr, nullptr, d_block_tmp, compact_blocks);
-    launches += 2;
+    launches += 1;
     // In core the shadow entries are sorted by list position (the ray's own
     // domain first): the occlusion walk takes them in that order, so an
     // occluder found near the ray culls its entries in farther domains.
@@ -1269,7 +1269,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
                            d_alive_list, d_block_tmp2, compact_blocks);
       std::swap(d_alive_list, d_alive_list2);
       std::swap(d_alive_count, d_alive_count2);
-      launches += 2;
+      launches += 1;
       cur ^= 1;
     }
   }
