@@ -512,14 +512,29 @@ __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nke
   __syncwarp();
   for (int k = lane; k < nkeys; k += 32) running[k] = a.hist[(size_t)ch * nkeys + k];
   __syncwarp();
+  // the next group's list sizes, offsets, ray ids and predictions load while
+  // this group is flattened and ranked
+  uint32_t ncnt = 0, noff = 0, nrid = 0, np = 0xffu;
+  if (r0 + lane < r1) {
+    ncnt = a.list_cnt[r0 + lane];
+    noff = a.list_off[r0 + lane];
+    nrid = a.list[r0 + lane];
+    if (a.pred) np = a.pred[r0 + lane];
+  }
   for (uint64_t base = r0; base < r1; base += 32) {
-    const uint64_t i = base + lane;
-    uint32_t cnt = 0, off = 0, rid = 0, p = 0xffu;
-    if (i < r1) {
-      cnt = a.list_cnt[i];
-      off = a.list_off[i];
-      rid = a.list[i];
-      if (a.pred) p = a.pred[i];
+    const uint32_t cnt = ncnt, off = noff, rid = nrid, p = np;
+    {
+      const uint64_t j = base + 32 + lane;
+      ncnt = 0;
+      noff = 0;
+      nrid = 0;
+      np = 0xffu;
+      if (j < r1) {
+        ncnt = a.list_cnt[j];
+        noff = a.list_off[j];
+        nrid = a.list[j];
+        if (a.pred) np = a.pred[j];
+      }
     }
     uint32_t total;
     const uint32_t pos = warpExclusiveScan(cnt, &total);
