@@ -134,9 +134,13 @@ __global__ void __launch_bounds__(kSchedThreads, kMinBlocks) kSchedLists(SchedAr
     for (int k = lane; k < hwords; k += 32) h[k] = 0;
     __syncwarp();
   }
+  // the next group's ray ids load while this group is scheduled
+  uint32_t nrid = r0 + lane < r1 ? a.list[r0 + lane] : 0u;
   for (uint64_t base = r0; base < r1; base += 32) {
     const uint64_t i = base + lane;
     const bool active = i < r1;
+    const uint32_t rid_cur = nrid;
+    nrid = base + 32 + lane < r1 ? a.list[base + 32 + lane] : 0u;
     float lt[kMaxList];
     uint32_t ld[kMaxList];
     int cnt = 0;
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(kSchedThreads, kMinBlocks) kSchedLists(SchedAr
     bool origin_in_list = false;
     float origin_t = 0.f;
     if (active) {
-      uint32_t rid = a.list[i];
+      const uint32_t rid = rid_cur;
       V3 org, dir;
       float t1 = INFINITY;
       if (!a.shadow) {
