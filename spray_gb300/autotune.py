@@ -65,8 +65,11 @@ def _frame_ms(scene, cfg: dict, cam, frames: int, warmup: int) -> float:
     return statistics.median(ms)
 
 
-def tune(name: str, frames: int = 3, warmup: int = 2, policy: int | None = None, rounds: int = 1,
-         write: bool = True) -> dict:
+def tune(name: str, frames: int | None = None, warmup: int | None = None, policy: int | None = None,
+         rounds: int = 1, write: bool = True) -> dict:
+    """frames / warmup default to 3 / 2 in core and 10 / 5 out of core, where the
+    domain cache settles over several frames (with fewer, the early frames'
+    loads mislead the comparison)."""
     import spray_gb300 as sg
     from spray_gb300 import scenes
     path, _ = scenes.benchmark_scene(name)
@@ -75,6 +78,10 @@ def tune(name: str, frames: int = 3, warmup: int = 2, policy: int | None = None,
     if policy is not None:
         cfg["schedule_policy"] = policy
     ooc = 0 < cfg.get("cache_size", -1) < len(scene.domains)
+    if frames is None:
+        frames = 10 if ooc else 3
+    if warmup is None:
+        warmup = 5 if ooc else 2
     space = dict(SPACE)
     if ooc:
         space.update(OOC_SPACE)
@@ -116,8 +123,8 @@ def tune(name: str, frames: int = 3, warmup: int = 2, policy: int | None = None,
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2")
-    ap.add_argument("--frames", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--frames", type=int, default=None, help="timed frames per trial (3; 10 out of core)")
+    ap.add_argument("--warmup", type=int, default=None, help="warm-up frames per trial (2; 5 out of core)")
     ap.add_argument("--policy", type=int, default=None)
     ap.add_argument("--rounds", type=int, default=1)
     args = ap.parse_args()
