@@ -53,14 +53,16 @@ def load(name: str, policy: int | None = None) -> dict | None:
     return None
 
 
-def _frame_ms(scene, cfg: dict, cam, frames: int, warmup: int) -> float:
+def _frame_ms(scene, cfg: dict, cam, frames: int, warmup: int, views: list | None = None) -> float:
+    """Median frame time; a multi-view workload traces its whole view batch."""
     import spray_gb300 as sg
     t = sg.Tracer(cfg)
     t.set_scene(scene)
     t.set_camera(*cam)
+    frame = (lambda: t.trace_views(views)) if views else t.trace
     for _ in range(warmup):
-        t.trace()
-    ms = [t.trace()[1]["frame_ms"] for _ in range(frames)]
+        frame()
+    ms = [frame()[1]["frame_ms"] for _ in range(frames)]
     t.close()
     return statistics.median(ms)
 
@@ -86,6 +88,7 @@ def tune(name: str, frames: int | None = None, warmup: int | None = None, policy
     if ooc:
         space.update(OOC_SPACE)
     cam = scenes.orbit_camera(scene)
+    views = scenes.c5_views(scene, spec["views"], spec["view_seed"]) if "views" in spec else None
     best = {k: 0 for k in space}
     best.update({"trace_blocks_per_sm": 4, "sched_chunks_per_warp": 8, "wave_samples": 0})
     if ooc:
@@ -93,7 +96,7 @@ def tune(name: str, frames: int | None = None, warmup: int | None = None, policy
     trials = []
 
     def run(params):
-        ms = _frame_ms(scene, dict(cfg, **params), cam, frames, warmup)
+        ms = _frame_ms(scene, dict(cfg, **params), cam, frames, warmup, views)
         trials.append({"params": dict(params), "frame_ms": ms})
         return ms
 
