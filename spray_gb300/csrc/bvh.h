@@ -23,8 +23,9 @@ static_assert(sizeof(BvhNode4) == 128, "node must be one 128-byte line");
 constexpr int kMaxLeafTris = 8;
 constexpr int32_t kEmptyChild = (int32_t)0x80000000;
 
-// Binary hierarchy over the domain boxes, used by the scheduler to find the
-// domains a ray may overlap before it runs SpRay's exact slab test on them.
+// Binary hierarchy over the domain boxes (median splits); the scheduler
+// descends its 4-wide collapse (buildDomainBvh4) to find the domains a ray may
+// overlap before it runs SpRay's exact slab test on them.
 // Node boxes are enlarged outward so a conservative node test never rejects a
 // domain the exact test accepts.  c0/c1 >= 0: inner node; < 0: leaf ~domain.
 struct alignas(16) DomNode {
