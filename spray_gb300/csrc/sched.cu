@@ -766,30 +766,46 @@ __global__ void kCompactWrite(const uint8_t* __restrict__ flag, const uint32_t* 
   }
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t lt = laneMaskLt();
-  for (uint64_t s = b0; s < b1; s += blockDim.x) {
-    const uint64_t i = s + threadIdx.x;
-    const uint32_t id = i < b1 ? (src ? src[i] : (uint32_t)i) : 0u;
-    const bool f = i < b1 && flag[id] != 0;
-    const uint32_t bal = __ballot_sync(0xffffffffu, f);
-    if (lane == 0) ws[w] = __popc(bal);
+  // four elements per thread per round (element s + k * blockDim + thread:
+  // order row k, warp, lane), so that a round's loads overlap and its two
+  // barriers cover 4 x blockDim elements
+  __shared__ uint32_t wk[4][8];
+  for (uint64_t s = b0; s < b1; s += 4 * (uint64_t)blockDim.x) {
+    uint32_t id[4], bal[4];
+    bool f[4], valid[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t i = s + (uint64_t)k * blockDim.x + threadIdx.x;
+      valid[k] = i < b1;
+      id[k] = valid[k] ? (src ? src[i] : (uint32_t)i) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      f[k] = valid[k] && flag[id[k]] != 0;
+      bal[k] = __ballot_sync(0xffffffffu, f[k]);
+      if (lane == 0) wk[k][w] = __popc(bal[k]);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       uint32_t run = 0;
-      for (int k = 0; k < nw; ++k) {
-        uint32_t v = ws[k];
-        ws[k] = run;
-        run += v;
-      }
+      for (int k = 0; k < 4; ++k)
+        for (int q = 0; q < nw; ++q) {
+          const uint32_t v = wk[k][q];
+          wk[k][q] = run;
+          run += v;
+        }
       ws[32] = run;
     }
     __syncthreads();
-    if (i < b1) {
-      if (f) {
-        uint32_t p = base + ws[w] + __popc(bal & lt);
-        list[p] = id;
-        if (index_of) index_of[id] = (int32_t)p;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (!valid[k]) continue;
+      if (f[k]) {
+        const uint32_t p = base + wk[k][w] + __popc(bal[k] & lt);
+        list[p] = id[k];
+        if (index_of) index_of[id[k]] = (int32_t)p;
       } else if (index_of) {
-        index_of[id] = -1;
+        index_of[id[k]] = -1;
       }
     }
     base += ws[32];

@@ -527,12 +527,21 @@ void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks) {
 // The entry that holds a ray's final key publishes its colour and normal.
 __global__ void kResolve(TraceArgs a, float4* hit_ns) {
   const uint32_t E = *a.num_entries;
-  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < E;
-       e += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t k = a.rec_key[e];
-    if (k == kNoHit) continue;
-    uint32_t ray = a.entries[e].x & kRayIdMask;
-    if (a.ray_key[ray] == k) hit_ns[ray] = a.rec_attr[e];
+  // four entries per thread per step, their loads in flight together
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t e0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e0 < E; e0 += 4 * stride) {
+    uint64_t k[4];
+    uint32_t ray[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint64_t e = e0 + q * stride;
+      k[q] = e < E ? a.rec_key[e] : kNoHit;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ray[q] = k[q] != kNoHit ? a.entries[e0 + q * stride].x & kRayIdMask : 0u;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (k[q] != kNoHit && a.ray_key[ray[q]] == k[q]) hit_ns[ray[q]] = a.rec_attr[e0 + q * stride];
   }
 }
 
