@@ -99,7 +99,7 @@ __device__ __forceinline__ bool fitsList(int cnt, int j) { return j < cnt; }
 
 // kMinBlocks 6 caps the kernel at 40 registers (a few spills) so that six
 // blocks fit an SM when shared memory allows; with larger domain tables
-// shared memory holds fewer blocks and the variant for five (48 registers,
+// shared memory holds fewer blocks and the variant for five (46 registers,
 // no spills) runs instead.
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kSchedThreads, kMinBlocks) kSchedLists(SchedArgs a,
