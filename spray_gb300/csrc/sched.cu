@@ -492,7 +492,7 @@ size_t scanTmpWords(int nkeys, int nchunks) {
 // Isector::isectAll pushes them, ooc_isector.h:133-144).  The flattened entries
 // of 32 rays pass through a window of kScatterWindow entries per warp, in
 // order, so that the staging buffer stays small and many warps fit per SM.
-constexpr int kScatterWindow = 128;
+constexpr int kScatterWindow = 256;
 
 __global__ void __launch_bounds__(128) kSchedScatter(SchedArgs a, int D, int nkeys, int nwarps) {
   extern __shared__ uint32_t smem[];
