@@ -492,6 +492,35 @@ F3 blinnPhong(float costheta, F3 kd, F3 ks, float shininess, F3 li, F3 wi, F3 n_
   return mul(li, add(cd, cs));
 }
 
+// Reflect (src/render/reflection.h:126-128)
+F3 reflect(F3 wo, F3 normal_ff) { return add(neg(wo), muls(normal_ff, 2.0f * dot(wo, normal_ff))); }
+
+// FrDielectric (src/render/reflection.h:134-158): reflectance, and the
+// transmitted direction unless the reflection is total (then 1, wt untouched)
+float frDielectric(float cosThetaI, float etaI, float etaT, F3 wo, F3 normal_ff, F3* wt) {
+  float sin2ThetaI = gmax(0.0f, 1.0f - (cosThetaI * cosThetaI));
+  float eta = etaI / etaT;
+  float sin2ThetaT = eta * eta * sin2ThetaI;
+  if (sin2ThetaT >= 1.0f) return 1.0f;
+  float cosThetaT = std::sqrt(1.0f - sin2ThetaT);
+  float Rparl = ((etaT * cosThetaI) - (etaI * cosThetaT)) / ((etaT * cosThetaI) + (etaI * cosThetaT));
+  float Rperp = ((etaI * cosThetaI) - (etaT * cosThetaT)) / ((etaI * cosThetaI) + (etaT * cosThetaT));
+  float fr = (Rparl * Rparl + Rperp * Rperp) / 2.0f;
+  *wt = add(smul(eta, neg(wo)), muls(normal_ff, eta * cosThetaI - cosThetaT));
+  return fr;
+}
+
+// Refract (src/render/reflection.h:160-174): false on total internal reflection
+bool refract(float cosThetaI, float etaI, float etaT, F3 wo, F3 normal_ff, F3* wt) {
+  float sin2ThetaI = gmax(0.0f, 1.0f - (cosThetaI * cosThetaI));
+  float eta = etaI / etaT;
+  float sin2ThetaT = eta * eta * sin2ThetaI;
+  if (sin2ThetaT >= 1.0f) return false;
+  float cosThetaT = std::sqrt(1.0f - sin2ThetaT);
+  *wt = add(smul(eta, neg(wo)), muls(normal_ff, eta * cosThetaI - cosThetaT));
+  return true;
+}
+
 struct Tile {
   int x, y, w, h;
 };
@@ -731,38 +760,22 @@ struct Oracle {
           } else {
             float etaI = entering ? D_.params[0] : D_.params[1];
             float etaT = entering ? D_.params[1] : D_.params[0];
-            float sin2ThetaI = gmax(0.0f, 1.0f - (cos_theta_i * cos_theta_i));
-            float eta = etaI / etaT;
-            float sin2ThetaT = eta * eta * sin2ThetaI;
             if (D_.bsdf == 2) {  // GlassBsdf + FrDielectric (reflection.h:134-158, 288-326)
-              if (sin2ThetaT >= 1.0f) {
-                fr = 1.0f;
-              } else {
-                float cosThetaT = std::sqrt(1.0f - sin2ThetaT);
-                float Rparl = ((etaT * cos_theta_i) - (etaI * cosThetaT)) /
-                              ((etaT * cos_theta_i) + (etaI * cosThetaT));
-                float Rperp = ((etaI * cos_theta_i) - (etaT * cosThetaT)) /
-                              ((etaI * cos_theta_i) + (etaT * cosThetaT));
-                fr = (Rparl * Rparl + Rperp * Rperp) / 2.0f;
-                wt = add(smul(eta, neg(wo)), muls(normal_ff, eta * cos_theta_i - cosThetaT));
-              }
+              fr = frDielectric(cos_theta_i, etaI, etaT, wo, normal_ff, &wt);
               if (fr == 1.0f) refl = true;
               else if (fr == 0.0f) trans = true;
               else refl = true;  // the reference aborts here (CHECK in the shader)
-            } else {  // TransmissionBsdf + Refract (reflection.h:160-174, 331-364)
-              if (sin2ThetaT >= 1.0f) {
-                fr = 1.0f;
-                refl = true;
-              } else {
-                float cosThetaT = std::sqrt(1.0f - sin2ThetaT);
-                wt = add(smul(eta, neg(wo)), muls(normal_ff, eta * cos_theta_i - cosThetaT));
-                fr = 0.0f;
-                trans = true;
-              }
+            } else if (refract(cos_theta_i, etaI, etaT, wo, normal_ff, &wt)) {
+              // TransmissionBsdf + Refract (reflection.h:160-174, 331-364)
+              fr = 0.0f;
+              trans = true;
+            } else {
+              fr = 1.0f;
+              refl = true;
             }
           }
           if (refl) {
-            F3 wr = add(neg(wo), muls(normal_ff, 2.0f * dot(wo, normal_ff)));
+            F3 wr = reflect(wo, normal_ff);
             bo->dir = normalize(wr);
             bo->w = muls(Lin, fr / abs_cos_theta_i);
             bo->valid = hasPositive(bo->w);
@@ -1768,6 +1781,100 @@ int orc_triangle(const float org[3], const float dir[3], const float v[9], float
                           f3(v[6], v[7], v[8]), tnear, tfar, t, u, vv)
              ? 1
              : 0;
+}
+
+int orc_camera_rays(const float pos[3], const float lookat[3], const float up[3], float vfov, int32_t w,
+                    int32_t h, int64_t n, const float* xy, float* dir) {
+  if (w <= 0 || h <= 0 || n < 0) return 1;
+  Oracle o;
+  o.cfg = orc_config{};
+  o.cfg.image_w = w;
+  o.cfg.image_h = h;
+  o.setCamera(pos, lookat, up, vfov);
+  for (int64_t i = 0; i < n; ++i) {
+    F3 d = o.generateRay(xy[2 * i], xy[2 * i + 1]);
+    for (int k = 0; k < 3; ++k) dir[3 * i + k] = d[k];
+  }
+  return 0;
+}
+
+int orc_disk(int64_t n, const float* u, float* d) {
+  for (int64_t i = 0; i < n; ++i) orc::concentricDisk(u[2 * i], u[2 * i + 1], &d[2 * i], &d[2 * i + 1]);
+  return 0;
+}
+
+int orc_local_to_world(int64_t n, const float* N, const float* v, float* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    F3 r = orc::localToWorld(f3(N[3 * i], N[3 * i + 1], N[3 * i + 2]), f3(v[3 * i], v[3 * i + 1], v[3 * i + 2]));
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = r[k];
+  }
+  return 0;
+}
+
+int orc_cosine_sample(int64_t n, const float* u, const float* N, float* wi, float* pdf) {
+  for (int64_t i = 0; i < n; ++i) {
+    F3 d;
+    orc::cosineSample(u[2 * i], u[2 * i + 1], f3(N[3 * i], N[3 * i + 1], N[3 * i + 2]), &d, &pdf[i]);
+    for (int k = 0; k < 3; ++k) wi[3 * i + k] = d[k];
+  }
+  return 0;
+}
+
+// the shaders' point-light shadow direction, normalize(light - p)
+// (PointLight::sample, src/render/light.h:47-52)
+int orc_point_light(int64_t n, const float* light, const float* p, float* wi) {
+  for (int64_t i = 0; i < n; ++i) {
+    F3 d = orc::normalize(orc::sub(f3(light[3 * i], light[3 * i + 1], light[3 * i + 2]),
+                                   f3(p[3 * i], p[3 * i + 1], p[3 * i + 2])));
+    for (int k = 0; k < 3; ++k) wi[3 * i + k] = d[k];
+  }
+  return 0;
+}
+
+int orc_blinn_phong(int64_t n, const float* a, float* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = a + 20 * i;
+    auto v = [&](int o) { return f3(p[o], p[o + 1], p[o + 2]); };
+    F3 r = orc::blinnPhong(p[0], v(1), v(4), p[7], v(8), v(11), v(14), v(17));
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = r[k];
+  }
+  return 0;
+}
+
+int orc_unpack_color(int64_t n, const uint32_t* color, float* rgb) {
+  for (int64_t i = 0; i < n; ++i) {
+    F3 c = orc::unpack(color[i]);
+    for (int k = 0; k < 3; ++k) rgb[3 * i + k] = c[k];
+  }
+  return 0;
+}
+
+int orc_reflect(int64_t n, const float* wo, const float* N, float* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    F3 r = orc::reflect(f3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), f3(N[3 * i], N[3 * i + 1], N[3 * i + 2]));
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = r[k];
+  }
+  return 0;
+}
+
+int orc_fr_dielectric(int64_t n, const float* a, float* fr, float* wt) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = a + 9 * i;
+    F3 t = f3(0, 0, 0);
+    fr[i] = orc::frDielectric(p[0], p[1], p[2], f3(p[3], p[4], p[5]), f3(p[6], p[7], p[8]), &t);
+    for (int k = 0; k < 3; ++k) wt[3 * i + k] = t[k];
+  }
+  return 0;
+}
+
+int orc_refract(int64_t n, const float* a, uint8_t* ok, float* wt) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = a + 9 * i;
+    F3 t = f3(0, 0, 0);
+    ok[i] = orc::refract(p[0], p[1], p[2], f3(p[3], p[4], p[5]), f3(p[6], p[7], p[8]), &t) ? 1 : 0;
+    for (int k = 0; k < 3; ++k) wt[3 * i + k] = t[k];
+  }
+  return 0;
 }
 
 int orc_lru_trace(int32_t nd, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits) {

@@ -6,11 +6,16 @@
  * against it.  Only tests, the smoke check and bench.py's CPU-baseline leg
  * call it.  It shares no code with the product.
  *
- * Parity is unpinned against the reference binary: the reference needs
- * Embree 2.17, glm, glog and MPI, none of which are available, and it ships no
- * golden vectors.  The oracle substitutes its own BVH and the published
- * watertight triangle test (Woop, Benthin, Wald, JCGT 2013) for Embree, and
- * its own vector math for glm.
+ * Pinning: the reference binary cannot be built (Embree 2.17, MPI and GLFW
+ * are absent) and it ships no golden vectors, but many of its hot-path
+ * functions compile alone (oracle/build_ref.sh, with stand-ins for the glm,
+ * glog and MPI headers).  The oracle equals them function by function --
+ * sampler, slab test, camera, disk and cosine sampling, lights, Blinn-Phong,
+ * reflection and refraction, colour unpack, LRU cache, tiles, domain scores
+ * (tests/test_reference_vectors.py and tests/golden/).  Traversal and the
+ * loop as a whole stay unpinned: the oracle substitutes its own BVH and the
+ * published watertight triangle test (Woop, Benthin, Wald, JCGT 2013) for
+ * Embree.
  *
  * Two modes:
  *   A  orc_render_speculative: the reference's loop itself -- per-thread
@@ -111,6 +116,29 @@ int orc_triangle(const float org[3], const float dir[3], const float v[9], float
                  float* t, float* u, float* v_out);
 /* replays domain loads through LruCache; hits[i] = 1 on a cache hit */
 int orc_lru_trace(int32_t num_domains, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits);
+
+/* Per-function hooks, n cases each, for the comparison with the reference's
+ * own code (oracle/build_ref.sh).  Vectors are packed float triples.
+ *   camera_rays: Camera::init + generateRay at image coordinates xy[2n]
+ *   disk: ConcentricDiskSampling of u[2n]; local_to_world: localToWorld(N, v)
+ *   cosine_sample: getCosineHemisphereSample(u1, u2, N) -> wi, pdf
+ *   point_light: normalize(light - p), the point-light shadow direction
+ *   blinn_phong: 20 floats per case (costheta, kd, ks, shininess, li, wi,
+ *     n_hat, wo) -> 3
+ *   unpack_color: util::unpack -> rgb
+ *   reflect: Reflect(wo, n); fr_dielectric / refract: 9 floats per case
+ *     (cos_theta_i, eta_i, eta_t, wo, n) -> fr or ok, and wt (0 if unset) */
+int orc_camera_rays(const float pos[3], const float lookat[3], const float up[3], float vfov, int32_t w,
+                    int32_t h, int64_t n, const float* xy, float* dir);
+int orc_disk(int64_t n, const float* u, float* d);
+int orc_local_to_world(int64_t n, const float* normal, const float* v, float* out);
+int orc_cosine_sample(int64_t n, const float* u, const float* normal, float* wi, float* pdf);
+int orc_point_light(int64_t n, const float* light, const float* p, float* wi);
+int orc_blinn_phong(int64_t n, const float* args, float* out);
+int orc_unpack_color(int64_t n, const uint32_t* color, float* rgb);
+int orc_reflect(int64_t n, const float* wo, const float* normal, float* out);
+int orc_fr_dielectric(int64_t n, const float* args, float* fr, float* wt);
+int orc_refract(int64_t n, const float* args, uint8_t* ok, float* wt);
 
 /* Full frames: W*H*4 floats. */
 int orc_render_wavefront(void* o, float* rgba, orc_stats* stats);

@@ -3,8 +3,11 @@
 TEST INFRASTRUCTURE ONLY: the CPU restatement of SpRay's speculative
 domain-parallel ray-tracing loop that the CUDA path is checked against.  Only
 tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
-Parity is unpinned against the reference binary (it cannot be built here:
-Embree 2.17, glm, glog and MPI are absent and it ships no golden vectors).
+The reference binary cannot be built here (Embree 2.17, MPI and GLFW are
+absent) and ships no golden vectors; its hot-path functions that compile alone
+(oracle/build_ref.sh) pin the oracle function by function
+(tests/test_reference_vectors.py).  Traversal and the loop as a whole stay
+unpinned.
 """
 from __future__ import annotations
 
@@ -87,6 +90,12 @@ def lib() -> C.CDLL:
         L.orc_slab.argtypes = [P, P, P, C.c_float, C.c_float, P, P]
         L.orc_triangle.argtypes = [P, P, P, C.c_float, C.c_float, P, P, P]
         L.orc_lru_trace.argtypes = [C.c_int32, C.c_int32, C.c_int64, P, P]
+        L.orc_camera_rays.argtypes = [P, P, P, C.c_float, C.c_int32, C.c_int32, C.c_int64, P, P]
+        for name in ("disk", "unpack_color", "blinn_phong"):
+            getattr(L, "orc_" + name).argtypes = [C.c_int64, P, P]
+        for name in ("local_to_world", "reflect", "fr_dielectric", "refract", "point_light"):
+            getattr(L, "orc_" + name).argtypes = [C.c_int64, P, P, P]
+        L.orc_cosine_sample.argtypes = [C.c_int64, P, P, P, P]
         L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
         L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
         _lib = L
@@ -143,6 +152,87 @@ def lru_trace(num_domains: int, cache_size: int, ids) -> np.ndarray:
     hits = np.zeros(len(ids), np.uint8)
     lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits))
     return hits
+
+
+def camera_rays(pos, lookat, up, vfov, image_w, image_h, xy) -> np.ndarray:
+    """Camera::init + generateRay at image coordinates xy[n, 2] -> dir[n, 3]."""
+    xy = _f32(xy).reshape(-1, 2)
+    out = np.zeros((len(xy), 3), np.float32)
+    lib().orc_camera_rays(_p(_f32(pos)), _p(_f32(lookat)), _p(_f32(up)), vfov, image_w, image_h, len(xy),
+                          _p(xy), _p(out))
+    return out
+
+
+def disk(u) -> np.ndarray:
+    """ConcentricDiskSampling of u[n, 2] -> [n, 2]."""
+    u = _f32(u).reshape(-1, 2)
+    out = np.zeros_like(u)
+    lib().orc_disk(len(u), _p(u), _p(out))
+    return out
+
+
+def local_to_world(normal, v) -> np.ndarray:
+    normal, v = _f32(normal).reshape(-1, 3), _f32(v).reshape(-1, 3)
+    out = np.zeros_like(v)
+    lib().orc_local_to_world(len(v), _p(normal), _p(v), _p(out))
+    return out
+
+
+def cosine_sample(u, normal) -> tuple[np.ndarray, np.ndarray]:
+    """getCosineHemisphereSample(u1, u2, N) -> (wi[n, 3], pdf[n])."""
+    u, normal = _f32(u).reshape(-1, 2), _f32(normal).reshape(-1, 3)
+    wi = np.zeros((len(u), 3), np.float32)
+    pdf = np.zeros(len(u), np.float32)
+    lib().orc_cosine_sample(len(u), _p(u), _p(normal), _p(wi), _p(pdf))
+    return wi, pdf
+
+
+def point_light(light, p) -> np.ndarray:
+    """Shadow-ray direction toward point lights: normalize(light - p)."""
+    light, p = _f32(light).reshape(-1, 3), _f32(p).reshape(-1, 3)
+    out = np.zeros_like(p)
+    lib().orc_point_light(len(p), _p(light), _p(p), _p(out))
+    return out
+
+
+def blinn_phong(args) -> np.ndarray:
+    """args[n, 20] = costheta, kd, ks, shininess, li, wi, n_hat, wo -> [n, 3]."""
+    args = _f32(args).reshape(-1, 20)
+    out = np.zeros((len(args), 3), np.float32)
+    lib().orc_blinn_phong(len(args), _p(args), _p(out))
+    return out
+
+
+def unpack_color(colors) -> np.ndarray:
+    colors = np.ascontiguousarray(colors, np.uint32)
+    out = np.zeros((len(colors), 3), np.float32)
+    lib().orc_unpack_color(len(colors), _p(colors), _p(out))
+    return out
+
+
+def reflect(wo, normal) -> np.ndarray:
+    wo, normal = _f32(wo).reshape(-1, 3), _f32(normal).reshape(-1, 3)
+    out = np.zeros_like(wo)
+    lib().orc_reflect(len(wo), _p(wo), _p(normal), _p(out))
+    return out
+
+
+def fr_dielectric(args) -> tuple[np.ndarray, np.ndarray]:
+    """args[n, 9] = cos_theta_i, eta_i, eta_t, wo, n -> (fr[n], wt[n, 3])."""
+    args = _f32(args).reshape(-1, 9)
+    fr = np.zeros(len(args), np.float32)
+    wt = np.zeros((len(args), 3), np.float32)
+    lib().orc_fr_dielectric(len(args), _p(args), _p(fr), _p(wt))
+    return fr, wt
+
+
+def refract(args) -> tuple[np.ndarray, np.ndarray]:
+    """Same layout as fr_dielectric -> (ok[n] as uint8, wt[n, 3])."""
+    args = _f32(args).reshape(-1, 9)
+    ok = np.zeros(len(args), np.uint8)
+    wt = np.zeros((len(args), 3), np.float32)
+    lib().orc_refract(len(args), _p(args), _p(ok), _p(wt))
+    return ok, wt
 
 
 class Oracle:

@@ -1,0 +1,220 @@
+// TEST INFRASTRUCTURE ONLY.  Exposes hot-path functions of the reference,
+// compiled from its own sources where they lie (oracle/build_ref.sh), through
+// a C ABI, so that the oracle's restatement of each can be compared with the
+// reference's code value for value.  Nothing of the reference is copied: this
+// file only includes its headers and calls the functions they define.
+//
+// The reference's third-party headers are absent, so oracle/ref_shim stands in
+// for them: glm (float vector arithmetic restated in glm's operation order),
+// glog (CHECK aborts), the CMake-generated config header (the CMake cache
+// defaults) and the MPI profiler header.  render/aabb.cc is not compiled (it
+// includes OpenGL); the slab test reads only Aabb::bounds, so the default
+// constructor it would provide is defined empty below.
+//
+// Include order follows src/apps/spray_ooc.cc: the shader headers (light.h,
+// reflection.h, hence sampler.h and <math.h>) come before camera.h, so the
+// unqualified tan() in Camera::init resolves as it does in that program.
+#include <cstdint>
+
+#define __forceinline inline
+#include "render/light.h"
+#include "render/reflection.h"
+#include "render/aabb.h"
+#include "render/camera.h"
+#include "render/lru_cache.h"
+#include "render/tile.h"
+#include "ooc/ooc_domain_stats.h"
+#include "utils/comm.h"
+#include "utils/util.h"
+
+namespace spray {
+Aabb::Aabb() {}
+// The reference's process-wide MPI descriptor (defined with its main
+// programs): one process, rank 0.
+MpiComm global_mpi_comm;
+}  // namespace spray
+
+using namespace spray;
+
+namespace {
+glm::vec3 v3(const float* p) { return glm::vec3(p[0], p[1], p[2]); }
+void put3(const glm::vec3& v, float* p) {
+  p[0] = v.x;
+  p[1] = v.y;
+  p[2] = v.z;
+}
+}  // namespace
+
+extern "C" {
+
+// intersectAabb, float-array form (render/aabb.h:139-169).  tmin/tmax are
+// written only when the slabs overlap; they start at 0 here, as in the oracle.
+int ref_slab(const float b[6], const float org[3], const float dir[3], float t0, float t1, float* tmin,
+             float* tmax) {
+  Aabb box;
+  box.bounds[0] = v3(b);
+  box.bounds[1] = v3(b + 3);
+  float o[3] = {org[0], org[1], org[2]};
+  float d[3] = {dir[0], dir[1], dir[2]};
+  *tmin = *tmax = 0.f;
+  return intersectAabb(box, o, d, t0, t1, tmin, tmax) ? 1 : 0;
+}
+
+// Camera::init then Camera::generateRay(x, y, org, dir) (render/camera.h:128-209)
+int ref_camera_rays(const float pos[3], const float lookat[3], const float up[3], float vfov, int32_t w,
+                    int32_t h, int64_t n, const float* xy, float* dir) {
+  Camera cam;
+  cam.init(v3(pos), v3(lookat), v3(up), vfov, w, h);
+  for (int64_t i = 0; i < n; ++i) {
+    float org[3];
+    cam.generateRay(xy[2 * i], xy[2 * i + 1], org, dir + 3 * i);
+  }
+  return 0;
+}
+
+// ConcentricDiskSampling (render/sampler.h:49-92)
+int ref_disk(int64_t n, const float* u, float* d) {
+  ConcentricDiskSampling disk;
+  for (int64_t i = 0; i < n; ++i) disk(u[2 * i], u[2 * i + 1], &d[2 * i], &d[2 * i + 1]);
+  return 0;
+}
+
+// localToWorld (render/sampler.h:101-110)
+int ref_local_to_world(int64_t n, const float* N, const float* v, float* out) {
+  for (int64_t i = 0; i < n; ++i) put3(localToWorld(v3(N + 3 * i), v3(v + 3 * i)), out + 3 * i);
+  return 0;
+}
+
+// getCosineHemisphereSample (render/sampler.cc:54-60)
+int ref_cosine_sample(int64_t n, const float* u, const float* N, float* wi, float* pdf) {
+  for (int64_t i = 0; i < n; ++i) {
+    glm::vec3 d;
+    getCosineHemisphereSample(u[2 * i], u[2 * i + 1], v3(N + 3 * i), &d, &pdf[i]);
+    put3(d, wi + 3 * i);
+  }
+  return 0;
+}
+
+// DiffuseHemisphereLight::sampleArea (render/light.h:80-85) with a sampler
+// seeded by RandomSampler_init(seed[i])
+int ref_diffuse_light(int64_t n, const int32_t* seed, const float* N, float* wi, float* pdf) {
+  DiffuseHemisphereLight light(glm::vec3(1, 1, 1));
+  for (int64_t i = 0; i < n; ++i) {
+    RandomSampler s;
+    RandomSampler_init(s, seed[i]);
+    glm::vec3 d;
+    light.sampleArea(s, v3(N + 3 * i), &d, &pdf[i]);
+    put3(d, wi + 3 * i);
+  }
+  return 0;
+}
+
+// PointLight::sample (render/light.h:47-52): wi toward the light
+int ref_point_light(int64_t n, const float* light_pos, const float* p, float* wi) {
+  for (int64_t i = 0; i < n; ++i) {
+    PointLight light(v3(light_pos + 3 * i), glm::vec3(1, 1, 1));
+    glm::vec3 d;
+    float pdf;
+    light.sample(v3(p + 3 * i), &d, &pdf);
+    put3(d, wi + 3 * i);
+  }
+  return 0;
+}
+
+// blinnPhong (render/reflection.h:202-214); 20 floats per case: costheta, kd,
+// ks, shininess, li, wi, n_hat, wo
+int ref_blinn_phong(int64_t n, const float* a, float* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = a + 20 * i;
+    put3(blinnPhong(p[0], v3(p + 1), v3(p + 4), p[7], v3(p + 8), v3(p + 11), v3(p + 14), v3(p + 17)),
+         out + 3 * i);
+  }
+  return 0;
+}
+
+// Reflect (render/reflection.h:126-128)
+int ref_reflect(int64_t n, const float* wo, const float* N, float* out) {
+  for (int64_t i = 0; i < n; ++i) put3(Reflect(v3(wo + 3 * i), v3(N + 3 * i)), out + 3 * i);
+  return 0;
+}
+
+// FrDielectric (render/reflection.h:134-158); 9 floats per case:
+// cos_theta_i, eta_i, eta_t, wo, n.  wt stays 0 on total internal reflection.
+int ref_fr_dielectric(int64_t n, const float* a, float* fr, float* wt) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = a + 9 * i;
+    glm::vec3 t(0, 0, 0);
+    fr[i] = FrDielectric(p[0], p[1], p[2], v3(p + 3), v3(p + 6), &t);
+    put3(t, wt + 3 * i);
+  }
+  return 0;
+}
+
+// Refract (render/reflection.h:160-174), same layout as ref_fr_dielectric
+int ref_refract(int64_t n, const float* a, uint8_t* ok, float* wt) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* p = a + 9 * i;
+    glm::vec3 t(0, 0, 0);
+    ok[i] = Refract(p[0], p[1], p[2], v3(p + 3), v3(p + 6), &t) ? 1 : 0;
+    put3(t, wt + 3 * i);
+  }
+  return 0;
+}
+
+// util::unpack(uint32_t, float[3]) (utils/util.h:75-79)
+int ref_unpack_color(int64_t n, const uint32_t* color, float* rgb) {
+  for (int64_t i = 0; i < n; ++i) util::unpack(color[i], rgb + 3 * i);
+  return 0;
+}
+
+// LruCache::init + LruCache::load (render/lru_cache.cc); hits[i] = 1 on a hit
+int ref_lru_trace(int32_t num_domains, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits) {
+  LruCache c;
+  c.init(num_domains, cache_size);
+  for (int64_t i = 0; i < n; ++i) {
+    int block = -1;
+    hits[i] = c.load(ids[i], &block) ? 1 : 0;
+  }
+  return 0;
+}
+
+// ImageScheduleTileList::init (render/tile.cc:317-391): the blocking tiles of
+// rank `rank` of `num_ranks`, four ints (x, y, w, h) each; returns the count.
+// The caller keeps the tile height above 0 (the reference divides by it).
+int32_t ref_tiles(int64_t image_w, int64_t image_h, int64_t spp, int64_t num_ranks, int32_t rank,
+                  int64_t max_samples_per_rank, int32_t* out, int32_t capacity) {
+  global_mpi_comm.size = (int)num_ranks;
+  global_mpi_comm.rank = rank;
+  ImageScheduleTileList list;
+  list.init(image_w, image_h, spp, num_ranks, rank, max_samples_per_rank);
+  int32_t n = 0;
+  for (; !list.empty(); list.pop(), ++n) {
+    if (n < capacity) {
+      const Tile& t = list.front();
+      out[4 * n] = t.x;
+      out[4 * n + 1] = t.y;
+      out[4 * n + 2] = t.w;
+      out[4 * n + 3] = t.h;
+    }
+  }
+  return n;
+}
+
+// DomainStats::resize + increment + schedule (ooc/ooc_domain_stats.cc:34-111)
+// over counts[num_domains * 16] (16 = the list size of the CMake defaults):
+// order[i] = the i-th domain of the schedule.
+int ref_domain_order(int32_t num_domains, const int64_t* counts, int32_t* order) {
+  global_mpi_comm.size = 1;
+  global_mpi_comm.rank = 0;
+  ooc::DomainStats s;
+  s.resize(num_domains, false);
+  s.reset();
+  for (int32_t d = 0; d < num_domains; ++d)
+    for (int k = 0; k < SPRAY_RAY_DOMAIN_LIST_SIZE; ++k)
+      for (int64_t c = 0; c < counts[(int64_t)d * SPRAY_RAY_DOMAIN_LIST_SIZE + k]; ++c) s.increment(d, k);
+  s.schedule();
+  for (int32_t i = 0; i < num_domains; ++i) order[i] = s.getDomainId(i);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,498 @@
+"""Known-answer vectors from the reference's own code, and the rules that
+compare the oracle with them.
+
+TEST INFRASTRUCTURE ONLY.  ``oracle/build_ref.sh`` compiles the reference's
+hot-path functions from its sources (``oracle/_ref/libref_path.so``,
+``oracle/_ref/libref_rng.so``).  This module makes seeded inputs for each
+function, runs them through those libraries (``reference_outputs``) or through
+the oracle (``oracle_outputs``), and checks one against the other
+(``compare``).  ``make_reference_vectors.py`` stores inputs and reference
+outputs in ``reference_vectors.json`` so that the check runs where the
+reference sources are absent.
+
+Each group names the reference function it pins (file:line within the
+reference's ``src/`` or ``deps/``):
+
+============== ==================================================== =========
+group          reference                                            match
+============== ==================================================== =========
+rng            RandomSampler_init/get1D, embree/random_sampler.h    bit-exact
+slab           intersectAabb (float arrays), render/aabb.h:139-169  bit-exact
+camera         Camera::init/generateRay, render/camera.h:128-209    bit-exact
+disk           ConcentricDiskSampling, render/sampler.h:49-92       cos/sin
+local_to_world localToWorld, render/sampler.h:101-110               bit-exact
+cosine         getCosineHemisphereSample, render/sampler.cc:54-60   cos/sin
+diffuse_light  DiffuseHemisphereLight::sampleArea, light.h:80-85    cos/sin
+point_light    PointLight::sample, render/light.h:47-52             bit-exact
+blinn_phong    blinnPhong, render/reflection.h:202-214              pow
+reflect        Reflect, render/reflection.h:126-128                 bit-exact
+fr_dielectric  FrDielectric, render/reflection.h:134-158            bit-exact
+refract        Refract, render/reflection.h:160-174                 bit-exact
+unpack         util::unpack, utils/util.h:75-79                     bit-exact
+lru            LruCache::init/load, render/lru_cache.cc:41-171      exact
+tiles          ImageScheduleTileList::init, render/tile.cc:317-391  exact
+domain_order   DomainStats::schedule, ooc/ooc_domain_stats.cc:60-111 ties
+============== ==================================================== =========
+
+"cos/sin": the reference calls libm's cosf/sinf through glm; the oracle (and
+the CUDA path, which equals the oracle bit for bit) uses its own Cody-Waite +
+Taylor sinCos.  The disk point then differs by at most 2^-23 and everything
+downstream of it is bit-exact wherever the disk point agrees.  "pow": glm::pow
+is powf; the oracle raises to the integral shininess by binary
+exponentiation (relative difference below 1e-5).  "ties": the reference
+orders equal scores with an unstable std::sort, the oracle by domain id; the
+score sequence of the schedule must agree.
+"""
+from __future__ import annotations
+
+import base64
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+REF_DIR = ROOT / "oracle" / "_ref"
+FIXTURE = Path(__file__).resolve().parent / "reference_vectors.json"
+LIST_SIZE = 16  # SPRAY_RAY_DOMAIN_LIST_SIZE in the reference's CMake defaults
+
+P = C.c_void_p
+I64 = C.c_int64
+
+# tolerances of the groups that are not bit-exact (see the module docstring)
+DISK_ABS = 2.0 ** -23
+# A disk point off by e <= 2^-23 moves z = sqrt(1 - x^2 - y^2) by at most
+# sqrt(4 e) at the rim (z -> 0) and by about e * r / z elsewhere; wi is a
+# rotation of (x, y, z) and pdf = z / pi.
+COSINE_RIM_ABS = (4 * DISK_ABS) ** 0.5
+COSINE_ABS = 2e-6      # where z > 0.1 (r / z < 10)
+BLINN_REL = 1e-5
+
+GROUPS = ["rng", "slab", "camera", "disk", "local_to_world", "cosine", "diffuse_light", "point_light",
+          "blinn_phong", "reflect", "fr_dielectric", "refract", "unpack", "lru", "tiles", "domain_order"]
+
+
+def _p(a):
+    return a.ctypes.data_as(P)
+
+
+# ------------------------------------------------------------------ encoding
+def encode(a: np.ndarray) -> dict:
+    a = np.ascontiguousarray(a)
+    return {"dtype": a.dtype.str, "shape": list(a.shape), "b64": base64.b64encode(a.tobytes()).decode()}
+
+
+def decode(d: dict) -> np.ndarray:
+    return np.frombuffer(base64.b64decode(d["b64"]), np.dtype(d["dtype"])).reshape(d["shape"]).copy()
+
+
+# ------------------------------------------------------------------ inputs
+def _unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+
+def make_cases(seed: int = 2024, scale: int = 1) -> dict:
+    """Seeded inputs per group; ``scale`` multiplies the random part."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    c = {}
+
+    seeds = [0, 1, -1, 2 ** 31 - 1, -(2 ** 31), 7, 1023, 123456]
+    seeds += [p * (l + 1) for p in (0, 5, 1919, 2073599) for l in range(8)]  # AO: pixel * (l + 1)
+    seeds += [s * d for s in (3, 4095, 2 ** 20 + 7) for d in range(1, 6)]     # bounces: sample * depth
+    seeds += rng.integers(-(2 ** 31), 2 ** 31, 40 * scale).tolist()
+    c["rng"] = {"seed": np.array([np.int64(s) for s in seeds], np.int64).astype(np.int32)}
+
+    # slab: edge cases first (zero and -0 direction components, origin on a
+    # plane, origin inside, degenerate direction, flat boxes), then random
+    inf = np.inf
+    edge = [
+        ([0, 0, 0, 1, 1, 1], [0.5, 0.5, -1], [0, 0, 1]),
+        ([0, 0, 0, 1, 1, 1], [0.5, 0.5, -1], [-0.0, 0, 1]),
+        ([0, 0, 0, 1, 1, 1], [0.5, 0.5, -1], [0.0, -0.0, 1]),
+        ([0, 0, 0, 1, 1, 1], [0, 0.5, -1], [0, 0, 1]),
+        ([0, 0, 0, 1, 1, 1], [1, 1, -1], [0, 0, 1]),
+        ([0, 0, 0, 1, 1, 1], [0.5, 0.5, 0.5], [1, 2, 3]),
+        ([0, 0, 0, 1, 1, 1], [0.5, 0.5, 0.5], [0, 0, 0]),
+        ([0, 0, 0, 1, 1, 1], [2, 2, 2], [1, 1, 1]),
+        ([0, 0, 0, 1, 1, 1], [-1, -1, -1], [1, 1, 1]),
+        ([0, 0, 0, 1, 0, 1], [0.5, -1, 0.5], [0, 1, 0]),
+        ([0, 0, 0, 0, 0, 0], [-1, 0, 0], [1, 0, 0]),
+        ([-3, -2, -1, 3, 2, 1], [10, 0, 0], [-1, 1e-30, 0]),
+        ([-3, -2, -1, 3, 2, 1], [0, 0, 0], [1e-38, 1, 0]),
+    ]
+    nr = 200 * scale
+    lo = rng.uniform(-4, 4, (nr, 3))
+    hi = lo + rng.uniform(0, 3, (nr, 3)) * (rng.random((nr, 1)) > 0.05)
+    org = rng.uniform(-8, 8, (nr, 3))
+    tgt = rng.uniform(lo, np.maximum(hi, lo + 1e-3))
+    d = tgt - org + rng.normal(0, 0.5, (nr, 3)) * (rng.random((nr, 1)) < 0.5)
+    d[rng.random(nr) < 0.1, rng.integers(0, 3)] = 0.0
+    box = np.concatenate([np.array([e[0] for e in edge]), np.concatenate([lo, hi], 1)]).astype(f32)
+    c["slab"] = {
+        "box": box,
+        "org": np.concatenate([np.array([e[1] for e in edge]), org]).astype(f32),
+        "dir": np.concatenate([np.array([e[2] for e in edge]), d]).astype(f32),
+        "t": np.stack([np.where(rng.random(len(box)) < 0.8, f32(0.001), f32(0.0)),
+                       np.where(rng.random(len(box)) < 0.8, f32(inf), rng.uniform(0.5, 12, len(box)).astype(f32))],
+                      1).astype(f32),
+    }
+
+    # camera: the workload resolutions and odd ones; integer pixels and jitter
+    views = [(1920, 1080, 60.0), (1024, 1024, 90.0), (2048, 2048, 60.0), (64, 48, 45.0), (7, 5, 30.0),
+             (256, 256, 60.0)]
+    cams, xy = [], []
+    for (w, h, fov) in views:
+        pos = rng.uniform(-12, 12, 3)
+        look = rng.uniform(-1, 1, 3)
+        m = 32 * scale
+        odd = np.arange(m) % 2  # odd entries jittered like multi-sample eye rays
+        p = np.stack([rng.integers(0, w, m) + rng.random(m) * odd, rng.integers(0, h, m) + rng.random(m) * odd], 1)
+        p[:4] = [[0, 0], [w - 1, h - 1], [w / 2, h / 2], [0, h - 1]]
+        cams.append(np.concatenate([pos, look, [0, 1, 0], [fov, w, h]]))
+        xy.append(p)
+    c["camera"] = {"view": np.array(cams, f32), "xy": np.array(xy, f32)}
+
+    # disk: the region boundaries (sx = 0, sy = 0, sx = +-sy) and the corners
+    g = np.array([0.0, 0.25, 0.5, 0.75, 1.0], f32)
+    uu = np.stack(np.meshgrid(g, g), -1).reshape(-1, 2)
+    t = rng.random(48 * scale).astype(f32)
+    uu = np.concatenate([uu, np.stack([t, t], 1), np.stack([t, f32(1) - t], 1),
+                         rng.random((160 * scale, 2)).astype(f32)]).astype(f32)
+    c["disk"] = {"u": uu}
+
+    axes = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [-1, 0, 0], [0, -1, 0], [0, 0, -1],
+                     [0.6, 0.8, 0], [0, 0.6, 0.8], [0.8, 0, 0.6]], f32)
+    nn = np.concatenate([axes, _unit(rng, 96 * scale)])
+    c["local_to_world"] = {"n": nn, "v": _unit(rng, len(nn))}
+
+    cu = np.concatenate([uu[:40], rng.random((200 * scale, 2)).astype(f32)])
+    c["cosine"] = {"u": cu, "n": np.concatenate([np.repeat(axes, 5, 0)[:len(cu)], _unit(rng, len(cu))])[:len(cu)]}
+
+    dseeds = np.array([p * (l + 1) for p in rng.integers(0, 2 ** 21, 12 * scale) for l in range(8)], np.int64)
+    c["diffuse_light"] = {"seed": dseeds.astype(np.int32), "n": _unit(rng, len(dseeds))}
+
+    npt = 64 * scale
+    c["point_light"] = {"light": rng.uniform(-100, 1000, (npt, 3)).astype(f32),
+                        "p": rng.uniform(-2, 2, (npt, 3)).astype(f32)}
+
+    nb = 96 * scale
+    shin = np.concatenate([[1, 2, 3, 8, 16, 64, 127, 200], rng.integers(1, 129, nb - 8)]).astype(f32)
+    c["blinn_phong"] = {"args": np.concatenate([
+        rng.random((nb, 1)), rng.random((nb, 3)), rng.random((nb, 3)), shin[:, None],
+        rng.random((nb, 3)) * 3, _unit(rng, nb), _unit(rng, nb), _unit(rng, nb)], 1).astype(f32)}
+
+    nrf = 96 * scale
+    c["reflect"] = {"wo": _unit(rng, nrf), "n": _unit(rng, nrf)}
+
+    nd = 160 * scale
+    cos_i = np.concatenate([[1, -1, 0, 1e-4, -1e-4, 0.5, -0.5, 0.2], rng.uniform(-1, 1, nd - 8)])
+    eta = np.concatenate([np.array([[1, 1.5], [1.5, 1], [1, 1], [2.4, 1], [1, 2.4], [1.33, 1], [1, 1.33],
+                                    [1.5, 1]]), rng.choice([1.0, 1.33, 1.5, 2.4], (nd - 8, 2))])
+    c["fr_dielectric"] = {"args": np.concatenate([cos_i[:, None], eta, _unit(rng, nd), _unit(rng, nd)],
+                                                 1).astype(f32)}
+
+    grey = (np.arange(256, dtype=np.uint32) * 0x010101).astype(np.uint32)
+    c["unpack"] = {"color": np.concatenate([grey, rng.integers(0, 2 ** 32, 64 * scale, dtype=np.uint64)
+                                            .astype(np.uint32)])}
+
+    traces = []
+    for (ndom, cap) in [(8, 1), (8, 3), (8, 8), (8, -1), (64, 16), (512, 57)]:
+        ids = rng.integers(0, ndom, 150 * scale)
+        ids[40:60] = ids[0]  # repeated hits
+        traces.append((ndom, cap, ids))
+    c["lru"] = {"config": np.array([(a, b) for a, b, _ in traces], np.int32),
+                "ids": np.array([t for _, _, t in traces], np.int32)}
+
+    # tiles: (w, h, spp, ranks, rank, max samples per rank), every tile height > 0
+    c["tiles"] = {"config": np.array([
+        (1024, 1024, 1, 1, 0, 1 << 20), (1920, 1080, 16, 1, 0, 1 << 20), (2048, 2048, 8, 1, 0, 1 << 20),
+        (400, 400, 4, 1, 0, 1 << 20), (100, 10, 1, 3, 0, 1 << 20), (100, 10, 1, 3, 1, 1 << 20),
+        (100, 10, 1, 3, 2, 1 << 20), (1920, 1080, 16, 3, 2, 1 << 20), (1000, 7, 4, 2, 1, 5000),
+        (640, 480, 64, 5, 4, 100000), (3, 1000, 1, 8, 7, 17), (7, 5, 2, 1, 0, 30)], np.int64)}
+
+    orders = []
+    for (ndom, hi_, zero) in [(64, 50, 0.0), (64, 3, 0.5), (128, 20, 0.7), (8, 2, 0.3)]:
+        cnt = rng.integers(0, hi_, (ndom, LIST_SIZE)).astype(np.int64)
+        cnt[rng.random(ndom) < zero] = 0
+        orders.append(cnt)
+    c["domain_order"] = {"counts": np.concatenate([o.reshape(-1) for o in orders]),
+                         "ndomains": np.array([len(o) for o in orders], np.int32)}
+    return c
+
+
+# ------------------------------------------------------------------ reference
+def load_reference():
+    """(libref_path, libref_rng) as ctypes libraries, or None where
+    oracle/build_ref.sh has not built them (reference sources absent)."""
+    lp, lr = REF_DIR / "libref_path.so", REF_DIR / "libref_rng.so"
+    if not (lp.exists() and lr.exists()):
+        return None
+    R, G = C.CDLL(str(lp)), C.CDLL(str(lr))
+    G.ref_rng.argtypes = [C.c_int32, C.c_int32, P]
+    R.ref_slab.argtypes = [P, P, P, C.c_float, C.c_float, P, P]
+    R.ref_camera_rays.argtypes = [P, P, P, C.c_float, C.c_int32, C.c_int32, I64, P, P]
+    for name in ("disk", "unpack_color", "blinn_phong"):
+        getattr(R, "ref_" + name).argtypes = [I64, P, P]
+    for name in ("local_to_world", "reflect", "fr_dielectric", "refract", "point_light"):
+        getattr(R, "ref_" + name).argtypes = [I64, P, P, P]
+    for name in ("cosine_sample", "diffuse_light"):
+        getattr(R, "ref_" + name).argtypes = [I64, P, P, P, P]
+    R.ref_lru_trace.argtypes = [C.c_int32, C.c_int32, I64, P, P]
+    R.ref_tiles.argtypes = [I64, I64, I64, I64, C.c_int32, I64, P, C.c_int32]
+    R.ref_tiles.restype = C.c_int32
+    R.ref_domain_order.argtypes = [C.c_int32, P, P]
+    return R, G
+
+
+def _tile_height(w, h, spp, nr, rk, mx):
+    """Tile height ImageScheduleTileList::init would compute (None for an
+    empty stripe), so that no case reaches its division by zero."""
+    sw = max(int(w) // int(nr), 1)
+    x = int(rk) * sw
+    if x >= w:
+        return None
+    vw = w - x if (x + sw > w or rk == nr - 1) else sw
+    ntiles = (vw * h * spp + mx - 1) // mx
+    return int(h) // int(ntiles)
+
+
+def _vec_call(fn, n, *arrays, outs):
+    res = [np.zeros(s, dt) for s, dt in outs]
+    fn(n, *[_p(np.ascontiguousarray(a)) for a in arrays], *[_p(r) for r in res])
+    return res
+
+
+def reference_outputs(cases: dict, libs) -> dict:
+    R, G = libs
+    f32, out = np.float32, {}
+    s = cases["rng"]["seed"]
+    r = np.zeros((len(s), 16), f32)
+    for i, sd in enumerate(s):
+        G.ref_rng(int(sd), 16, _p(r[i]))
+    out["rng"] = {"floats": r}
+
+    b = cases["slab"]
+    n = len(b["box"])
+    hit, tt = np.zeros(n, np.uint8), np.zeros((n, 2), f32)
+    for i in range(n):
+        lo, hi = np.zeros(1, f32), np.zeros(1, f32)
+        hit[i] = R.ref_slab(_p(b["box"][i]), _p(b["org"][i]), _p(b["dir"][i]), b["t"][i, 0], b["t"][i, 1],
+                            _p(lo), _p(hi))
+        tt[i] = lo[0], hi[0]
+    out["slab"] = {"hit": hit, "tmin_tmax": tt}
+
+    cm = cases["camera"]
+    dirs = np.zeros(cm["xy"].shape[:2] + (3,), f32)
+    for k, v in enumerate(cm["view"]):
+        R.ref_camera_rays(_p(v[0:3].copy()), _p(v[3:6].copy()), _p(v[6:9].copy()), v[9], int(v[10]), int(v[11]),
+                          cm["xy"].shape[1], _p(cm["xy"][k]), _p(dirs[k]))
+    out["camera"] = {"dir": dirs}
+
+    u = cases["disk"]["u"]
+    out["disk"] = {"d": _vec_call(R.ref_disk, len(u), u, outs=[((len(u), 2), f32)])[0]}
+
+    lw = cases["local_to_world"]
+    out["local_to_world"] = {"out": _vec_call(R.ref_local_to_world, len(lw["n"]), lw["n"], lw["v"],
+                                              outs=[((len(lw["n"]), 3), f32)])[0]}
+
+    cs = cases["cosine"]
+    m = len(cs["u"])
+    wi, pdf = _vec_call(R.ref_cosine_sample, m, cs["u"], cs["n"], outs=[((m, 3), f32), (m, f32)])
+    dd = _vec_call(R.ref_disk, m, cs["u"], outs=[((m, 2), f32)])[0]
+    out["cosine"] = {"wi": wi, "pdf": pdf, "disk": dd}
+
+    dl = cases["diffuse_light"]
+    m = len(dl["seed"])
+    wi, pdf = _vec_call(R.ref_diffuse_light, m, dl["seed"], dl["n"], outs=[((m, 3), f32), (m, f32)])
+    uu = np.zeros((m, 2), f32)
+    for i, sd in enumerate(dl["seed"]):
+        G.ref_rng(int(sd), 2, _p(uu[i]))
+    dd = _vec_call(R.ref_disk, m, uu, outs=[((m, 2), f32)])[0]
+    out["diffuse_light"] = {"wi": wi, "pdf": pdf, "disk": dd}
+
+    pl = cases["point_light"]
+    out["point_light"] = {"wi": _vec_call(R.ref_point_light, len(pl["p"]), pl["light"], pl["p"],
+                                          outs=[((len(pl["p"]), 3), f32)])[0]}
+
+    a = cases["blinn_phong"]["args"]
+    out["blinn_phong"] = {"out": _vec_call(R.ref_blinn_phong, len(a), a, outs=[((len(a), 3), f32)])[0]}
+
+    rf = cases["reflect"]
+    out["reflect"] = {"out": _vec_call(R.ref_reflect, len(rf["wo"]), rf["wo"], rf["n"],
+                                       outs=[((len(rf["wo"]), 3), f32)])[0]}
+
+    a = cases["fr_dielectric"]["args"]
+    fr, wt = _vec_call(R.ref_fr_dielectric, len(a), a, outs=[(len(a), f32), ((len(a), 3), f32)])
+    ok, wt2 = _vec_call(R.ref_refract, len(a), a, outs=[(len(a), np.uint8), ((len(a), 3), f32)])
+    out["fr_dielectric"] = {"fr": fr, "wt": wt}
+    out["refract"] = {"ok": ok, "wt": wt2}
+
+    col = cases["unpack"]["color"]
+    out["unpack"] = {"rgb": _vec_call(R.ref_unpack_color, len(col), col, outs=[((len(col), 3), f32)])[0]}
+
+    lr = cases["lru"]
+    hits = np.zeros(lr["ids"].shape, np.uint8)
+    for k, (ndom, cap) in enumerate(lr["config"]):
+        R.ref_lru_trace(int(ndom), int(cap), lr["ids"].shape[1], _p(np.ascontiguousarray(lr["ids"][k])), _p(hits[k]))
+    out["lru"] = {"hits": hits}
+
+    tiles = []
+    for (w, h, spp, nr, rk, mx) in cases["tiles"]["config"]:
+        if _tile_height(w, h, spp, nr, rk, mx) == 0:
+            raise ValueError("tile height 0: the reference divides by it")
+        buf = np.zeros(4 * 4096, np.int32)
+        k = R.ref_tiles(int(w), int(h), int(spp), int(nr), int(rk), int(mx), _p(buf), 4096)
+        tiles.append(buf[:4 * k].reshape(-1, 4))
+    out["tiles"] = {"count": np.array([len(t) for t in tiles], np.int32),
+                    "tiles": np.concatenate(tiles).astype(np.int32)}
+
+    do = cases["domain_order"]
+    orders, off = [], 0
+    for ndom in do["ndomains"]:
+        cnt = np.ascontiguousarray(do["counts"][off:off + ndom * LIST_SIZE])
+        od = np.zeros(ndom, np.int32)
+        R.ref_domain_order(int(ndom), _p(cnt), _p(od))
+        orders.append(od)
+        off += ndom * LIST_SIZE
+    out["domain_order"] = {"order": np.concatenate(orders)}
+    return out
+
+
+# ------------------------------------------------------------------ oracle
+def oracle_outputs(cases: dict) -> dict:
+    from oracle import oracle as O
+    from spray_gb300 import scenes
+
+    f32, out = np.float32, {}
+    out["rng"] = {"floats": np.stack([O.rng_floats(int(s), 16) for s in cases["rng"]["seed"]])}
+
+    b = cases["slab"]
+    res = [O.slab(b["box"][i], b["org"][i], b["dir"][i], b["t"][i, 0], b["t"][i, 1]) for i in range(len(b["box"]))]
+    out["slab"] = {"hit": np.array([r[0] for r in res], np.uint8),
+                   "tmin_tmax": np.array([(r[1], r[2]) for r in res], f32)}
+
+    cm = cases["camera"]
+    out["camera"] = {"dir": np.stack([O.camera_rays(v[0:3], v[3:6], v[6:9], v[9], int(v[10]), int(v[11]), cm["xy"][k])
+                                      for k, v in enumerate(cm["view"])])}
+    out["disk"] = {"d": O.disk(cases["disk"]["u"])}
+    lw = cases["local_to_world"]
+    out["local_to_world"] = {"out": O.local_to_world(lw["n"], lw["v"])}
+
+    cs = cases["cosine"]
+    wi, pdf = O.cosine_sample(cs["u"], cs["n"])
+    out["cosine"] = {"wi": wi, "pdf": pdf, "disk": O.disk(cs["u"])}
+
+    # the hemisphere light draws two floats from RandomSampler_init(seed)
+    # (RandomSampler_get2D) and takes a cosine sample around the normal
+    dl = cases["diffuse_light"]
+    uu = np.stack([O.rng_floats(int(s), 2) for s in dl["seed"]])
+    wi, pdf = O.cosine_sample(uu, dl["n"])
+    out["diffuse_light"] = {"wi": wi, "pdf": pdf, "disk": O.disk(uu)}
+
+    pl = cases["point_light"]
+    out["point_light"] = {"wi": O.point_light(pl["light"], pl["p"])}
+
+    out["blinn_phong"] = {"out": O.blinn_phong(cases["blinn_phong"]["args"])}
+    rf = cases["reflect"]
+    out["reflect"] = {"out": O.reflect(rf["wo"], rf["n"])}
+    fr, wt = O.fr_dielectric(cases["fr_dielectric"]["args"])
+    out["fr_dielectric"] = {"fr": fr, "wt": wt}
+    ok, wt2 = O.refract(cases["fr_dielectric"]["args"])
+    out["refract"] = {"ok": ok, "wt": wt2}
+    out["unpack"] = {"rgb": O.unpack_color(cases["unpack"]["color"])}
+
+    lr = cases["lru"]
+    out["lru"] = {"hits": np.stack([O.lru_trace(int(nd), int(cap), lr["ids"][k])
+                                    for k, (nd, cap) in enumerate(lr["config"])])}
+
+    sc = scenes.wavelet_grid(1, 8)
+    tiles = []
+    for (w, h, spp, nr, rk, mx) in cases["tiles"]["config"]:
+        o = O.Oracle(_config(image_w=int(w), image_h=int(h), pixel_samples=int(spp), num_ranks=int(nr),
+                             rank=int(rk), max_samples_per_rank=int(mx)), sc)
+        tiles.append(np.asarray(o.tiles(), np.int32).reshape(-1, 4))
+    out["tiles"] = {"count": np.array([len(t) for t in tiles], np.int32),
+                    "tiles": np.concatenate(tiles).astype(np.int32)}
+
+    do = cases["domain_order"]
+    orders, scores, off = [], [], 0
+    for ndom in do["ndomains"]:
+        cnt = do["counts"][off:off + ndom * LIST_SIZE]
+        grid = scenes.wavelet_grid(1, 8)
+        grid.domains = grid.domains * int(ndom)
+        o = O.Oracle(_config(list_size=LIST_SIZE), grid)
+        s, od = o.scores(cnt)
+        orders.append(od)
+        scores.append(s)
+        off += ndom * LIST_SIZE
+    out["domain_order"] = {"order": np.concatenate(orders), "score": np.concatenate(scores)}
+    return out
+
+
+def _config(**kw):
+    cfg = dict(image_w=64, image_h=48, ao_mode=1, ao_samples=1, pixel_samples=1, bounces=1, fov=60.0,
+               cache_size=-1, max_samples_per_rank=1 << 20, list_size=16, history_size=4, num_ranks=1, rank=0)
+    cfg.update(kw)
+    return cfg
+
+
+# ------------------------------------------------------------------ comparison
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def _same(a, b):
+    return np.array_equal(_bits(np.asarray(a, np.float32)), _bits(np.asarray(b, np.float32)))
+
+
+def compare(group: str, cases: dict, ref: dict, orc: dict) -> None:
+    """Asserts the oracle's outputs `orc` against the reference's `ref` for one
+    group, by the rule the module docstring gives for it."""
+    r, o = ref[group], orc[group]
+    if group in ("rng", "camera", "local_to_world", "point_light", "reflect", "unpack"):
+        (k,) = [k for k in r]
+        assert _same(r[k], o[k]), f"{group}: {np.sum(_bits(r[k]) != _bits(o[k]))} values differ"
+    elif group == "slab":
+        assert np.array_equal(r["hit"], o["hit"])
+        assert _same(r["tmin_tmax"], o["tmin_tmax"])
+    elif group == "disk":
+        assert np.all(np.abs(r["d"] - o["d"]) <= DISK_ABS), np.abs(r["d"] - o["d"]).max()
+    elif group in ("cosine", "diffuse_light"):
+        assert np.all(np.abs(r["disk"] - o["disk"]) <= DISK_ABS)
+        agree = np.all(_bits(r["disk"]) == _bits(o["disk"]), axis=1)
+        assert agree.mean() > 0.5  # most sin/cos values agree; those cases are bit-exact downstream
+        assert _same(r["wi"][agree], o["wi"][agree]) and _same(r["pdf"][agree], o["pdf"][agree])
+        dw = np.abs(r["wi"] - o["wi"]).max(axis=1)
+        dp = np.abs(r["pdf"] - o["pdf"])
+        assert np.all(dw <= COSINE_RIM_ABS) and np.all(dp <= COSINE_RIM_ABS)
+        inner = r["pdf"] * np.float32(np.pi) > 0.1
+        assert np.all(dw[inner] <= COSINE_ABS) and np.all(dp[inner] <= COSINE_ABS)
+    elif group == "blinn_phong":
+        rel = np.abs(r["out"] - o["out"]) / np.maximum(np.abs(r["out"]), np.float32(1e-30))
+        assert np.all(rel <= BLINN_REL), rel.max()
+    elif group == "fr_dielectric":
+        assert _same(r["fr"], o["fr"]) and _same(r["wt"], o["wt"])
+    elif group == "refract":
+        assert np.array_equal(r["ok"], o["ok"]) and _same(r["wt"], o["wt"])
+    elif group == "lru":
+        assert np.array_equal(r["hits"], o["hits"])
+    elif group == "tiles":
+        assert np.array_equal(r["count"], o["count"]) and np.array_equal(r["tiles"], o["tiles"])
+    elif group == "domain_order":
+        off = 0
+        for ndom in cases["domain_order"]["ndomains"]:
+            ro, oo = r["order"][off:off + ndom], o["order"][off:off + ndom]
+            sc = o["score"][off:off + ndom]
+            assert np.array_equal(np.sort(ro), np.arange(ndom))
+            # the same score at every position of the schedule; equal scores
+            # in any order (unstable sort in the reference, by id in the oracle)
+            assert np.array_equal(sc[ro], sc[oo])
+            assert np.all(np.diff(sc[oo]) <= 0)
+            # no ties: the same order
+            if len(np.unique(sc)) == ndom:
+                assert np.array_equal(ro, oo)
+            off += ndom
+    else:
+        raise KeyError(group)
