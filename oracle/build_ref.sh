@@ -3,7 +3,8 @@
 # they lie (read-only), the two libraries the oracle is checked against:
 #   oracle/_ref/libref_rng.so   deps/embree/random_sampler.h (ref_rng.cpp)
 #   oracle/_ref/libref_path.so  render/{sampler,lru_cache,tile}.cc,
-#                               ooc/ooc_domain_stats.cc and the inline code of
+#                               ooc/ooc_domain_stats.cc,
+#                               io/{scene_loader,ply_loader}.cc and the inline code of
 #                               render/{aabb,camera,light,reflection}.h and
 #                               utils/util.h (ref_path.cpp)
 # oracle/ref_shim stands in for glm, glog, mpi.h, the CMake-generated config
@@ -21,10 +22,11 @@ g++ $FLAGS -I "$HERE/ref_shim" -I "$REF/deps/embree" \
 # the reference's own language level (cmake/pbrt_compile.cmake) and the
 # definitions its compiler probes give on Linux/g++ (cmake/pbrt_flags.cmake);
 # deps/pbrt's BlockedArray needs -fpermissive with current g++
-g++ $FLAGS -std=gnu++11 -fpermissive -DPBRT_HAVE_CONSTEXPR -DPBRT_CONSTEXPR=constexpr \
+# (__forceinline: what Embree's platform header defines for random_sampler.h)
+g++ $FLAGS -std=gnu++11 -fpermissive -DPBRT_HAVE_CONSTEXPR -DPBRT_CONSTEXPR=constexpr -D__forceinline=inline \
     -DPBRT_HAVE_ALIGNAS -DPBRT_HAVE_ALIGNOF -DPBRT_HAVE_POSIX_MEMALIGN \
     -I "$HERE/ref_shim" -I "$REF/src" -I "$REF/deps" \
     "$HERE/ref_path.cpp" "$REF/src/render/sampler.cc" "$REF/src/render/lru_cache.cc" "$REF/src/render/tile.cc" \
-    "$REF/src/ooc/ooc_domain_stats.cc" \
+    "$REF/src/ooc/ooc_domain_stats.cc" "$REF/src/io/scene_loader.cc" "$REF/src/io/ply_loader.cc" \
     -o "$HERE/_ref/libref_path.so"
 echo "$HERE/_ref/libref_rng.so $HERE/_ref/libref_path.so"

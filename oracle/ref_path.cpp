@@ -16,11 +16,12 @@
 // unqualified tan() in Camera::init resolves as it does in that program.
 #include <cstdint>
 
-#define __forceinline inline
 #include "render/light.h"
 #include "render/reflection.h"
 #include "render/aabb.h"
 #include "render/camera.h"
+#include "io/ply_loader.h"
+#include "io/scene_loader.h"
 #include "render/lru_cache.h"
 #include "render/tile.h"
 #include "ooc/ooc_domain_stats.h"
@@ -214,6 +215,95 @@ int ref_domain_order(int32_t num_domains, const int64_t* counts, int32_t* order)
       for (int64_t c = 0; c < counts[(int64_t)d * SPRAY_RAY_DOMAIN_LIST_SIZE + k]; ++c) s.increment(d, k);
   s.schedule();
   for (int32_t i = 0; i < num_domains; ++i) order[i] = s.getDomainId(i);
+  return 0;
+}
+
+// SceneLoader::load (io/scene_loader.cc:311-358), then per domain: its
+// transform (16 floats, column-major), object and world bounds (min xyz, max
+// xyz), vertex and face counts and material kind (-1 none, 0 diffuse,
+// 1 mirror, 2 glass, 3 transmission); per light: kind (0 point, 1 diffuse)
+// and radiance.  Returns the domain count, or -1 when `cap` or `light_cap` is
+// too small.
+int32_t ref_scene_load(const char* spray, const char* ply_dir, int32_t cap, float* transform, float* obj_bounds,
+                       float* world_bounds, int64_t* counts, int32_t* bsdf_kind, int32_t light_cap,
+                       int32_t* num_lights, int32_t* light_kind, float* light_radiance) {
+  std::vector<Domain> doms;
+  std::vector<Light*> lights;
+  SceneLoader loader;
+  loader.load(spray, ply_dir ? ply_dir : "", &doms, &lights);
+  int32_t n = (int32_t)doms.size();
+  *num_lights = (int32_t)lights.size();
+  int32_t ret = (n > cap || *num_lights > light_cap) ? -1 : n;
+  if (ret >= 0) {
+    for (int32_t i = 0; i < n; ++i) {
+      const Domain& d = doms[i];
+      for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k) transform[16 * i + 4 * c + k] = d.transform[c][k];
+      for (int b = 0; b < 2; ++b) {
+        put3(d.object_aabb.bounds[b], obj_bounds + 6 * i + 3 * b);
+        put3(d.world_aabb.bounds[b], world_bounds + 6 * i + 3 * b);
+      }
+      counts[2 * i] = (int64_t)d.num_vertices;
+      counts[2 * i + 1] = (int64_t)d.num_faces;
+      const Bsdf* b = d.bsdf;
+      bsdf_kind[i] = !b ? -1
+                     : dynamic_cast<const DiffuseBsdf*>(b)      ? 0
+                     : dynamic_cast<const MirrorBsdf*>(b)       ? 1
+                     : dynamic_cast<const GlassBsdf*>(b)        ? 2
+                     : dynamic_cast<const TransmissionBsdf*>(b) ? 3
+                                                                : -2;
+    }
+    for (int32_t l = 0; l < *num_lights; ++l) {
+      glm::vec3 wi, rad;
+      float pdf;
+      if (lights[l]->isAreaLight()) {
+        RandomSampler s;
+        RandomSampler_init(s, 1);
+        rad = lights[l]->sampleArea(s, glm::vec3(0, 0, 1), &wi, &pdf);
+        light_kind[l] = 1;
+      } else {
+        rad = lights[l]->sample(glm::vec3(0, 0, 0), &wi, &pdf);
+        light_kind[l] = 0;
+      }
+      put3(rad, light_radiance + 3 * l);
+    }
+  }
+  for (Light* l : lights) delete l;
+  return ret;
+}
+
+// PlyLoader::load (io/ply_loader.cc:179-204): vertices (3 floats), faces
+// (3 indices) and packed RGB colours of a PLY file.  Returns the vertex count
+// and writes the face count, or -1 when the capacities are too small.
+int64_t ref_ply_load(const char* file, int64_t vcap, int64_t fcap, float* vertices, uint32_t* faces,
+                     uint32_t* colors, int64_t* num_faces) {
+  PlyLoader::Header h;
+  PlyLoader::quickHeaderRead(file, &h);
+  if ((int64_t)h.num_vertices > vcap || (int64_t)h.num_faces > fcap) return -1;
+  PlyLoader loader;
+  PlyLoader::Data d;
+  d.vertices_capacity = (size_t)vcap * 3;
+  d.faces_capacity = (size_t)fcap * 3;
+  d.colors_capacity = (size_t)vcap;
+  d.vertices = vertices;
+  d.faces = faces;
+  d.colors = colors;
+  loader.load(file, &d);
+  *num_faces = (int64_t)d.num_faces;
+  return (int64_t)d.num_vertices;
+}
+
+// The vertex loop of TriMeshBuffer::load (render/trimesh_buffer.cc:141-153,
+// which needs Embree to compile): v = transform * vec4(v, 1), in place.
+int ref_transform_points(const float* m16, int64_t n, float* v) {
+  glm::mat4 x;
+  for (int c = 0; c < 4; ++c) x[c] = glm::vec4(m16[4 * c], m16[4 * c + 1], m16[4 * c + 2], m16[4 * c + 3]);
+  for (int64_t i = 0; i < 3 * n; i += 3) {
+    glm::vec4 r = x * glm::vec4(v[i], v[i + 1], v[i + 2], 1.0f);
+    v[i] = r.x;
+    v[i + 1] = r.y;
+    v[i + 2] = r.z;
+  }
   return 0;
 }
 

@@ -13,9 +13,17 @@
 //     clamp(x, lo, hi) = min(max(x, lo), hi);
 //   * mat3 is three columns; (m * v)[i] = (m[0][i]*v.x + m[1][i]*v.y) + m[2][i]*v.z;
 //   * sqrt, pow, cos, sin, abs forward to the float overloads of <cmath>;
-//   * radians(x) = x * 0.01745329251994329576923690768489f.
-// Anything else the compiled headers name but the oracle never calls (mat4,
-// rotate) aborts if it is ever reached.
+//   * radians(x) = x * T(0.01745329251994329576923690768489) in x's type;
+//   * mat4 is four vec4 columns, mat4(s) the diagonal s, mat4() the identity;
+//   * (m * v) = (m[0]*v.x + m[1]*v.y) + (m[2]*v.z + m[3]*v.w), the pairwise
+//     sum glm has evaluated mat4 * vec4 with since 0.9.5 (type_mat4x4.inl);
+//   * translate(m, v)[3] = ((m[0]*v.x + m[1]*v.y) + m[2]*v.z) + m[3];
+//     scale(m, v)[i] = m[i] * v[i] (i < 3); rotate(m, a, v) builds R from
+//     c = cos(a), s = sin(a), axis = normalize(v), temp = (1 - c) * axis as
+//     glm's matrix_transform.inl does and returns
+//     [i] = (m[0]*R[i][0] + m[1]*R[i][1]) + m[2]*R[i][2], [3] = m[3].
+// mat4 * mat4, which the compiled headers name but the oracle never reaches,
+// aborts.
 #pragma once
 
 #include <cmath>
@@ -98,7 +106,10 @@ inline float abs(float x) { return std::fabs(x); }
 inline float pow(float x, float y) { return std::pow(x, y); }
 inline float cos(float x) { return std::cos(x); }
 inline float sin(float x) { return std::sin(x); }
-inline float radians(float deg) { return deg * 0.01745329251994329576923690768489f; }
+template <typename T>
+inline T radians(T deg) {
+  return deg * static_cast<T>(0.01745329251994329576923690768489);
+}
 
 struct mat3 {
   vec3 c[3];
@@ -114,13 +125,27 @@ inline vec3 operator*(const mat3& m, const vec3& v) {
               m[0][2] * v.x + m[1][2] * v.y + m[2][2] * v.z);
 }
 
-// Named by headers the oracle compiles (Camera::rotate, data partitions) but
-// never reached from the functions it calls.
+inline vec4 operator+(const vec4& a, const vec4& b) { return vec4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+inline vec4 operator*(const vec4& a, float s) { return vec4(a.x * s, a.y * s, a.z * s, a.w * s); }
+
 struct mat4 {
-  mat4() {}
-  explicit mat4(float) {}
+  vec4 c[4];
+  mat4() : mat4(1.0f) {}
+  explicit mat4(float s) {
+    c[0] = vec4(s, 0, 0, 0);
+    c[1] = vec4(0, s, 0, 0);
+    c[2] = vec4(0, 0, s, 0);
+    c[3] = vec4(0, 0, 0, s);
+  }
+  vec4& operator[](int i) { return c[i]; }
+  const vec4& operator[](int i) const { return c[i]; }
 };
-inline vec4 operator*(const mat4&, const vec4&) { std::abort(); }
+
+inline vec4 operator*(const mat4& m, const vec4& v) {
+  const vec4 add0 = m[0] * v.x + m[1] * v.y;
+  const vec4 add1 = m[2] * v.z + m[3] * v.w;
+  return add0 + add1;
+}
 inline mat4 operator*(const mat4&, const mat4&) { std::abort(); }
 
 }  // namespace glm

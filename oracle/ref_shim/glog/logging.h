@@ -1,10 +1,15 @@
 // TEST INFRASTRUCTURE ONLY.  Compile shim for glog, which the reference's
 // hot-path sources use for assertions and logging: a failed CHECK and
-// LOG(FATAL) abort, other log lines are discarded.
+// LOG(FATAL) abort, other log lines are discarded.  Like glog's own header
+// it brings in the stream headers the reference's sources rely on.
 #pragma once
 
 #include <cstdlib>
 #include <iostream>
+#include <ostream>
+#include <sstream>
+#include <string>
+#include <vector>
 
 namespace ref_shim {
 struct NullLog {

@@ -13,9 +13,12 @@
 namespace sg {
 
 // ---------------------------------------------------------------- transforms
-// The column-major 4x4 helpers below evaluate products in the same order as
-// the transform code SpRay builds its domain matrices with, so a translate-only
-// matrix moves a vertex by exactly one float add per coordinate.
+// The column-major 4x4 helpers below evaluate products in the order of glm's
+// translate/scale/rotate and mat4 * vec4, which SpRay builds and applies its
+// domain matrices with (src/io/scene_loader.cc:149-186, 351-357;
+// src/render/trimesh_buffer.cc:141-153), so a translate-only matrix moves a
+// vertex by exactly one float add per coordinate.  Like SpRay
+// (src/render/scene.inl:151), an identity matrix is not applied.
 
 Mat4 Mat4::identity() {
   Mat4 r;
@@ -85,13 +88,15 @@ Mat4 rotate(const Mat4& m, float a, int axis_id) {
   return r;
 }
 
+// m * vec4(in, 1) as glm evaluates mat4 * vec4 (type_mat4x4.inl, since glm
+// 0.9.5): the pairwise sum (m[0]*x + m[1]*y) + (m[2]*z + m[3]*w).  SpRay
+// transforms domain vertices (src/render/trimesh_buffer.cc:141-153) and the
+// object-bound corners (src/io/scene_loader.cc:351-357) with it.
 void transformPoint(const Mat4& m, const float in[3], float out[3]) {
   for (int k = 0; k < 3; ++k) {
-    float v = m.m[0][k] * in[0];
-    v = v + m.m[1][k] * in[1];
-    v = v + m.m[2][k] * in[2];
-    v = v + m.m[3][k] * 1.0f;
-    out[k] = v;
+    const float add0 = m.m[0][k] * in[0] + m.m[1][k] * in[1];
+    const float add1 = m.m[2][k] * in[2] + m.m[3][k] * 1.0f;
+    out[k] = add0 + add1;
   }
 }
 
@@ -123,14 +128,8 @@ SceneDesc loadSceneFile(const std::string& filename, const std::string& ply_path
     std::vector<std::string> t;
     {
       // tokens are separated by single spaces exactly like strtok(" ")
-      char* buf = &line[0];
       std::string copy(line);
-      char* tok = std::strtok(&copy[0], " ");
-      while (tok) {
-        t.emplace_back(tok);
-        tok = std::strtok(nullptr, " ");
-      }
-      (void)buf;
+      for (char* tok = std::strtok(&copy[0], " "); tok; tok = std::strtok(nullptr, " ")) t.emplace_back(tok);
     }
     if (t.empty()) continue;
     const std::string& tag = t[0];

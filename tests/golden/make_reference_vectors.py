@@ -1,5 +1,7 @@
-"""Writes reference_vectors.json: seeded inputs and what the reference's own
-code returns for them, per hot-path function (the groups of refvec.py).
+"""Writes reference_vectors.json (seeded inputs and what the reference's own
+code returns for them, per hot-path function: the groups of refvec.py) and
+reference_scene.json (a .spray scene with its PLY files, and what the
+reference's scene and PLY loaders make of them).
 
 TEST INFRASTRUCTURE ONLY.  Run it where the reference sources are present:
 
@@ -17,12 +19,15 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(HERE.parent))
+
+import numpy as np  # noqa: E402
 
 from golden import refvec as V  # noqa: E402
 
@@ -53,6 +58,18 @@ def main() -> int:
     doc["groups"]["refract"]["in"] = {}
     V.FIXTURE.write_text(json.dumps(doc, indent=1, sort_keys=True) + "\n")
     print(f"{V.FIXTURE}: {V.FIXTURE.stat().st_size} bytes, {len(V.GROUPS)} groups")
+
+    files = V.make_scene_files()
+    with tempfile.TemporaryDirectory() as tmp:
+        out = V.reference_scene_outputs(V.write_scene_files(files, Path(tmp)), libs)
+    scene = {
+        "about": "a .spray scene and its PLY files, and what the reference's SceneLoader, PlyLoader and "
+                 "TriMeshBuffer vertex transform make of them; made by tests/golden/make_reference_vectors.py",
+        "files": {k: V.encode(np.frombuffer(b, np.uint8)) for k, b in files.items()},
+        "out": {k: V.encode(a) for k, a in out.items()},
+    }
+    V.SCENE_FIXTURE.write_text(json.dumps(scene, indent=1, sort_keys=True) + "\n")
+    print(f"{V.SCENE_FIXTURE}: {V.SCENE_FIXTURE.stat().st_size} bytes")
     return 0
 
 

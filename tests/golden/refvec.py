@@ -496,3 +496,168 @@ def compare(group: str, cases: dict, ref: dict, orc: dict) -> None:
             off += ndom
     else:
         raise KeyError(group)
+
+
+# ------------------------------------------------------------------ scene files
+# SceneLoader::load (io/scene_loader.cc:311-358), PlyLoader::load
+# (io/ply_loader.cc:179-204) and the vertex transform of TriMeshBuffer::load
+# (render/trimesh_buffer.cc:141-153) against the product's scene loader
+# (spray_scene_load): world-space vertices and world bounds bit-exact, faces,
+# colours, materials and light radiance equal.
+SCENE_FIXTURE = Path(__file__).resolve().parent / "reference_scene.json"
+_XFORMS = ["", "translate 1.5 -2.25 3", "scale 2 0.5 3|rotate x 30|translate 0.1 0.2 0.3",
+           "rotate y 47.5|translate -4 5 6.125", "rotate z 90", "rotate x 13|rotate y -71|rotate z 200|"
+           "scale 1.1 1.2 1.3|translate 7 8 9", "translate 3 3 3|rotate y 33", "scale -1 1 1|rotate x -90"]
+_MTLS = ["", "mtl diffuse 0.5 0.25 0.75", "mtl mirror 1 1 1", "mtl glass 1 1.5", "mtl transmission 1 1.33"]
+
+
+def _sphere(nt=10, nph=20, r=1.3, c=(0.2, -0.1, 0.05)):
+    th = np.linspace(0.15, np.pi - 0.15, nt)
+    ph = np.linspace(0, 2 * np.pi, nph, endpoint=False)
+    T, PH = np.meshgrid(th, ph, indexing="ij")
+    v = np.stack([np.sin(T) * np.cos(PH), np.cos(T), np.sin(T) * np.sin(PH)], -1).reshape(-1, 3) * r + c
+    f = []
+    for i in range(nt - 1):
+        for j in range(nph):
+            a, b = i * nph + j, i * nph + (j + 1) % nph
+            f += [(a, b, a + nph), (b, b + nph, a + nph)]
+    return v.astype(np.float32), np.array(f, np.uint32)
+
+
+def _ply_binary(v, f, col):
+    head = ("ply\nformat binary_little_endian 1.0\nelement vertex %d\nproperty float x\nproperty float y\n"
+            "property float z\nproperty uchar red\nproperty uchar green\nproperty uchar blue\n"
+            "element face %d\nproperty list uchar int vertex_indices\nend_header\n" % (len(v), len(f))).encode()
+    vr = np.zeros(len(v), [("p", "<f4", 3), ("c", "u1", 3)])
+    vr["p"] = v
+    vr["c"] = np.stack([(col >> 16) & 255, (col >> 8) & 255, col & 255], 1)
+    fr = np.zeros(len(f), [("n", "u1"), ("i", "<i4", 3)])
+    fr["n"] = 3
+    fr["i"] = f
+    return head + vr.tobytes() + fr.tobytes()
+
+
+def _ply_ascii(v, f, col=None):
+    lines = ["ply", "format ascii 1.0", f"element vertex {len(v)}", "property float x", "property float y",
+             "property float z"]
+    if col is not None:
+        lines += ["property uchar red", "property uchar green", "property uchar blue"]
+    lines += [f"element face {len(f)}", "property list uchar int vertex_indices", "end_header"]
+    for k, p in enumerate(v):
+        s = " ".join(repr(float(x)) for x in p)
+        if col is not None:
+            s += " %d %d %d" % ((col[k] >> 16) & 255, (col[k] >> 8) & 255, col[k] & 255)
+        lines.append(s)
+    lines += ["3 %d %d %d" % tuple(t) for t in f]
+    return ("\n".join(lines) + "\n").encode()
+
+
+def make_scene_files(seed: int = 5) -> dict:
+    """A .spray scene (every material kind, translate/scale/rotate chains,
+    point and hemisphere lights) and the PLY files it names: binary
+    little-endian with colour, ASCII with and without colour."""
+    rng = np.random.default_rng(seed)
+    v, f = _sphere()
+    col = rng.integers(0, 1 << 24, len(v)).astype(np.uint32)
+    jitter = (v + rng.normal(0, 0.01, v.shape)).astype(np.float32)
+    files = {"bin.ply": _ply_binary(v, f, col), "asc.ply": _ply_ascii(jitter, f, col),
+             "plain.ply": _ply_ascii(v[:40], f[(f < 40).all(1)])}
+    plys = ["bin.ply", "asc.ply", "plain.ply"]
+    txt = ["# scene for the loader comparison", "light point 1 2 3 0.5 0.25 0.125", "light diffuse .1 .2 .3", ""]
+    for i, x in enumerate(_XFORMS):
+        name = plys[i % 3]
+        vv = v if name == "bin.ply" else (jitter if name == "asc.ply" else v[:40])
+        lo, hi = vv.min(0), vv.max(0)
+        txt += ["domain", f"file {name}"] + ([_MTLS[i % 5]] if _MTLS[i % 5] else [])
+        txt += ["bound " + " ".join(repr(float(a)) for a in np.concatenate([lo, hi]))]
+        txt += [t for t in x.split("|") if t]
+        nf = len(f) if name != "plain.ply" else int((f < 40).all(1).sum())
+        txt += [f"face {nf}", f"vertex {len(vv)}", ""]
+    files["scene.spray"] = ("\n".join(txt) + "\n").encode()
+    return files
+
+
+def write_scene_files(files: dict, where: Path) -> Path:
+    for name, data in files.items():
+        (where / name).write_bytes(data)
+    return where / "scene.spray"
+
+
+def reference_scene_outputs(spray: Path, libs, ply_dir: Path | None = None) -> dict:
+    R, _ = libs
+    R.ref_scene_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int32, P, P, P, P, P, C.c_int32, P, P, P]
+    R.ref_scene_load.restype = C.c_int32
+    R.ref_ply_load.argtypes = [C.c_char_p, I64, I64, P, P, P, P]
+    R.ref_ply_load.restype = I64
+    R.ref_transform_points.argtypes = [P, I64, P]
+    cap, lcap = 4096, 64
+    T = np.zeros((cap, 16), np.float32)
+    ob, wb = np.zeros((cap, 6), np.float32), np.zeros((cap, 6), np.float32)
+    cnt, kind = np.zeros((cap, 2), np.int64), np.zeros(cap, np.int32)
+    nl, lk, lr = np.zeros(1, np.int32), np.zeros(lcap, np.int32), np.zeros((lcap, 3), np.float32)
+    ply_dir = Path(ply_dir or spray.parent)
+    n = R.ref_scene_load(str(spray).encode(), str(ply_dir).encode(), cap, _p(T), _p(ob), _p(wb), _p(cnt), _p(kind), lcap,
+                         _p(nl), _p(lk), _p(lr))
+    if n < 0:
+        raise ValueError("scene larger than the comparison buffers")
+    names = [ln.split()[1] for ln in spray.read_text().splitlines() if ln.startswith("file ")]
+    verts, faces, cols = [], [], []
+    for i in range(n):
+        path = str(ply_dir / names[i]).encode()
+        nvh, nfh = _ply_counts(ply_dir / names[i])
+        vb = np.zeros((nvh + 1, 3), np.float32)
+        fb = np.zeros((nfh + 1, 3), np.uint32)
+        cb = np.zeros(nvh + 1, np.uint32)
+        nf = np.zeros(1, np.int64)
+        nv = R.ref_ply_load(path, len(vb), len(fb), _p(vb), _p(fb), _p(cb), _p(nf))
+        vb, fb, cb = vb[:nv], fb[:nf[0]], cb[:nv]
+        mat = np.ascontiguousarray(T[i])
+        if not np.array_equal(mat.reshape(4, 4), np.eye(4, dtype=np.float32)):  # render/scene.inl:151
+            R.ref_transform_points(_p(mat), len(vb), _p(vb))
+        verts.append(vb)
+        faces.append(fb)
+        cols.append(cb)
+    return {"world_bounds": wb[:n], "object_bounds": ob[:n], "transform": T[:n], "counts": cnt[:n],
+            "bsdf_kind": kind[:n], "light_kind": lk[:nl[0]], "light_radiance": lr[:nl[0]],
+            "nverts": np.array([len(v) for v in verts], np.int64), "vertices": np.concatenate(verts),
+            "faces": np.concatenate(faces), "colors": np.concatenate(cols)}
+
+
+def _ply_counts(path: Path) -> tuple[int, int]:
+    nv = nf = 0
+    with open(path, "rb") as fh:
+        for line in fh:
+            w = line.split()
+            if w[:2] == [b"element", b"vertex"]:
+                nv = int(w[2])
+            elif w[:2] == [b"element", b"face"]:
+                nf = int(w[2])
+            elif w[:1] == [b"end_header"]:
+                break
+    return nv, nf
+
+
+def product_scene_outputs(spray: Path, ply_dir: Path | None = None) -> dict:
+    import spray_gb300 as sg
+    s = sg.Scene.load(spray, ply_dir or spray.parent)
+    return {"world_bounds": np.stack([d.bounds for d in s.domains]),
+            "bsdf_kind": np.array([d.bsdf_type for d in s.domains], np.int32),
+            "light_kind": np.array([l.type for l in s.lights], np.int32),
+            "light_radiance": np.stack([l.radiance for l in s.lights]).astype(np.float32),
+            "nverts": np.array([len(d.vertices) for d in s.domains], np.int64),
+            "vertices": np.concatenate([d.vertices for d in s.domains]),
+            "faces": np.concatenate([d.faces for d in s.domains]),
+            "colors": np.concatenate([d.colors for d in s.domains])}
+
+
+def compare_scene(ref: dict, prod: dict) -> None:
+    assert np.array_equal(ref["nverts"], prod["nverts"])
+    assert _same(ref["vertices"], prod["vertices"]), \
+        f"{int(np.sum(np.any(_bits(ref['vertices']) != _bits(prod['vertices']), 1)))} vertices differ"
+    assert _same(ref["world_bounds"], prod["world_bounds"])
+    assert np.array_equal(ref["faces"], prod["faces"]) and np.array_equal(ref["colors"], prod["colors"])
+    # no mtl line: the reference leaves the BSDF unset, the product takes the diffuse default
+    assert np.array_equal(np.maximum(ref["bsdf_kind"], 0), prod["bsdf_kind"])
+    # light kinds: the reference's point / hemisphere, the product's POINT = 0, DIFFUSE = 1
+    assert np.array_equal(ref["light_kind"], prod["light_kind"])
+    assert _same(ref["light_radiance"], prod["light_radiance"])
