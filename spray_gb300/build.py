@@ -80,7 +80,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         os.replace(tmp, LIB)
     film_src = CSRC / "film_main.cpp"
     if force or not FILM.exists() or _needs(FILM, [film_src, LIB]):
-        cmd = ["g++", "-O2", "-std=c++17", "-o", str(FILM), str(film_src), "-L" + str(PKG),
+        # no contraction here either: the default camera's distance is an a*b + c
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-o", str(FILM), str(film_src), "-L" + str(PKG),
                "-lspray_gpu", "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
