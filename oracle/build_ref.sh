@@ -4,9 +4,10 @@
 #   oracle/_ref/libref_rng.so   deps/embree/random_sampler.h (ref_rng.cpp)
 #   oracle/_ref/libref_path.so  render/{sampler,lru_cache,tile}.cc,
 #                               ooc/ooc_domain_stats.cc,
-#                               io/{scene_loader,ply_loader}.cc and the inline code of
-#                               render/{aabb,camera,light,reflection}.h and
-#                               utils/util.h (ref_path.cpp)
+#                               io/{scene_loader,ply_loader}.cc,
+#                               deps/pbrt/memory.cpp and the inline code of
+#                               render/{aabb,camera,light,reflection}.h,
+#                               display/image.h and utils/util.h (ref_path.cpp)
 # oracle/ref_shim stands in for glm, glog, mpi.h, the CMake-generated config
 # header and the MPI profiler header, none of which exist here.  Nothing of the
 # reference is copied.  Exits 0 without building when the reference tree is
@@ -28,5 +29,6 @@ g++ $FLAGS -std=gnu++11 -fpermissive -DPBRT_HAVE_CONSTEXPR -DPBRT_CONSTEXPR=cons
     -I "$HERE/ref_shim" -I "$REF/src" -I "$REF/deps" \
     "$HERE/ref_path.cpp" "$REF/src/render/sampler.cc" "$REF/src/render/lru_cache.cc" "$REF/src/render/tile.cc" \
     "$REF/src/ooc/ooc_domain_stats.cc" "$REF/src/io/scene_loader.cc" "$REF/src/io/ply_loader.cc" \
+    "$REF/deps/pbrt/memory.cpp" \
     -o "$HERE/_ref/libref_path.so"
 echo "$HERE/_ref/libref_rng.so $HERE/_ref/libref_path.so"

@@ -492,6 +492,14 @@ F3 blinnPhong(float costheta, F3 kd, F3 ks, float shininess, F3 li, F3 wi, F3 n_
   return mul(li, add(cd, cs));
 }
 
+// HdrImage::add(pixid, rgb, double scale) (src/display/image.h:99-109): each
+// channel += scale * rgb in double, rounded once to float
+inline void hdrAdd(float* px, F3 rgb, double scale) {
+  px[0] = (float)((double)px[0] + scale * (double)rgb.x);
+  px[1] = (float)((double)px[1] + scale * (double)rgb.y);
+  px[2] = (float)((double)px[2] + scale * (double)rgb.z);
+}
+
 // Reflect (src/render/reflection.h:126-128)
 F3 reflect(F3 wo, F3 normal_ff) { return add(neg(wo), muls(normal_ff, 2.0f * dot(wo, normal_ff))); }
 
@@ -911,9 +919,7 @@ struct Oracle {
           for (int k = 0; k < spp; ++k)
             for (auto& c : contrib[p * spp + k]) {
               if (!c.second) continue;
-              px[0] = (float)((double)px[0] + scale * (double)c.first.x);
-              px[1] = (float)((double)px[1] + scale * (double)c.first.y);
-              px[2] = (float)((double)px[2] + scale * (double)c.first.z);
+              hdrAdd(px, c.first, scale);
             }
         }
         if (b + 1 < cfg.bounces) {
@@ -1324,9 +1330,7 @@ struct TContext {
       retire_q->pop();
       if (!r->occluded && vbuf.correct(*r)) {
         float* px = image + 4 * (size_t)r->pixid;
-        px[0] = (float)((double)px[0] + scale * (double)r->w[0]);
-        px[1] = (float)((double)px[1] + scale * (double)r->w[1]);
-        px[2] = (float)((double)px[2] + scale * (double)r->w[2]);
+        hdrAdd(px, f3(r->w[0], r->w[1], r->w[2]), scale);
       }
     }
   }
@@ -1874,6 +1878,12 @@ int orc_refract(int64_t n, const float* a, uint8_t* ok, float* wt) {
     ok[i] = orc::refract(p[0], p[1], p[2], f3(p[3], p[4], p[5]), f3(p[6], p[7], p[8]), &t) ? 1 : 0;
     for (int k = 0; k < 3; ++k) wt[3 * i + k] = t[k];
   }
+  return 0;
+}
+
+int orc_hdr_add(int64_t n, const int32_t* pixid, const float* rgb, double scale, float* rgba) {
+  for (int64_t i = 0; i < n; ++i)
+    orc::hdrAdd(rgba + 4 * (size_t)pixid[i], f3(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]), scale);
   return 0;
 }
 

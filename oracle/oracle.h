@@ -139,6 +139,8 @@ int orc_unpack_color(int64_t n, const uint32_t* color, float* rgb);
 int orc_reflect(int64_t n, const float* wo, const float* normal, float* out);
 int orc_fr_dielectric(int64_t n, const float* args, float* fr, float* wt);
 int orc_refract(int64_t n, const float* args, uint8_t* ok, float* wt);
+/* HdrImage::add in order: rgba[4 * pixid[i] + c] += scale * rgb[3 * i + c] */
+int orc_hdr_add(int64_t n, const int32_t* pixid, const float* rgb, double scale, float* rgba);
 
 /* Full frames: W*H*4 floats. */
 int orc_render_wavefront(void* o, float* rgba, orc_stats* stats);

@@ -96,6 +96,7 @@ def lib() -> C.CDLL:
         for name in ("local_to_world", "reflect", "fr_dielectric", "refract", "point_light"):
             getattr(L, "orc_" + name).argtypes = [C.c_int64, P, P, P]
         L.orc_cosine_sample.argtypes = [C.c_int64, P, P, P, P]
+        L.orc_hdr_add.argtypes = [C.c_int64, P, P, C.c_double, P]
         L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
         L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
         _lib = L
@@ -192,6 +193,14 @@ def point_light(light, p) -> np.ndarray:
     light, p = _f32(light).reshape(-1, 3), _f32(p).reshape(-1, 3)
     out = np.zeros_like(p)
     lib().orc_point_light(len(p), _p(light), _p(p), _p(out))
+    return out
+
+
+def hdr_add(rgba, pixid, rgb, scale: float) -> np.ndarray:
+    """HdrImage::add(pixid[i], rgb[i], scale) in order on a copy of rgba[P, 4]."""
+    out = np.array(rgba, np.float32, copy=True).reshape(-1, 4)
+    pixid, rgb = _i32(pixid), _f32(rgb).reshape(-1, 3)
+    lib().orc_hdr_add(len(pixid), _p(pixid), _p(rgb), scale, _p(out))
     return out
 
 

@@ -15,11 +15,13 @@
 // reflection.h, hence sampler.h and <math.h>) come before camera.h, so the
 // unqualified tan() in Camera::init resolves as it does in that program.
 #include <cstdint>
+#include <cstring>
 
 #include "render/light.h"
 #include "render/reflection.h"
 #include "render/aabb.h"
 #include "render/camera.h"
+#include "display/image.h"
 #include "io/ply_loader.h"
 #include "io/scene_loader.h"
 #include "render/lru_cache.h"
@@ -304,6 +306,27 @@ int ref_transform_points(const float* m16, int64_t n, float* v) {
     v[i + 1] = r.y;
     v[i + 2] = r.z;
   }
+  return 0;
+}
+
+// HdrImage::add(pixid, rgb, double scale) (display/image.h:99-109), n times
+// in order, on a w x h image that starts as `rgba` (4 floats per pixel)
+int ref_hdr_add(int32_t w, int32_t h, int64_t n, const int32_t* pixid, const float* rgb, double scale,
+                float* rgba) {
+  HdrImage img;
+  img.resize(w, h);
+  std::memcpy(img.buf, rgba, sizeof(float) * 4 * (size_t)w * h);
+  for (int64_t i = 0; i < n; ++i) img.add(pixid[i], rgb + 3 * i, scale);
+  std::memcpy(rgba, img.buf, sizeof(float) * 4 * (size_t)w * h);
+  return 0;
+}
+
+// HdrImage::writePpm (display/image.h:183-204) of a w x h float4 image
+int ref_write_ppm(int32_t w, int32_t h, const float* rgba, const char* filename) {
+  HdrImage img;
+  img.resize(w, h);
+  std::memcpy(img.buf, rgba, sizeof(float) * 4 * (size_t)w * h);
+  img.writePpm(filename);
   return 0;
 }
 

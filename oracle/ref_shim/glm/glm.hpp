@@ -14,6 +14,7 @@
 //   * mat3 is three columns; (m * v)[i] = (m[0][i]*v.x + m[1][i]*v.y) + m[2][i]*v.z;
 //   * sqrt, pow, cos, sin, abs forward to the float overloads of <cmath>;
 //   * radians(x) = x * T(0.01745329251994329576923690768489) in x's type;
+//   * vec4 names its components x y z w or r g b a;
 //   * mat4 is four vec4 columns, mat4(s) the diagonal s, mat4() the identity;
 //   * (m * v) = (m[0]*v.x + m[1]*v.y) + (m[2]*v.z + m[3]*v.w), the pairwise
 //     sum glm has evaluated mat4 * vec4 with since 0.9.5 (type_mat4x4.inl);
@@ -57,7 +58,10 @@ struct vec3 {
 };
 
 struct vec4 {
-  float x, y, z, w;
+  union { float x, r; };
+  union { float y, g; };
+  union { float z, b; };
+  union { float w, a; };
   vec4() : x(0), y(0), z(0), w(0) {}
   vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
   vec4(const vec3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}

@@ -32,7 +32,12 @@ unpack         util::unpack, utils/util.h:75-79                     bit-exact
 lru            LruCache::init/load, render/lru_cache.cc:41-171      exact
 tiles          ImageScheduleTileList::init, render/tile.cc:317-391  exact
 domain_order   DomainStats::schedule, ooc/ooc_domain_stats.cc:60-111 ties
+hdr_add        HdrImage::add (double scale), display/image.h:99-109 bit-exact
+ppm            HdrImage::writePpm, display/image.h:183-204         bytes (*)
 ============== ==================================================== =========
+
+(*) ppm holds the product's writer (spray_gb300.image), not the oracle, to the
+reference's bytes; NaN is included (the reference writes 0 on x86).
 
 "cos/sin": the reference calls libm's cosf/sinf through glm; the oracle (and
 the CUDA path, which equals the oracle bit for bit) uses its own Cody-Waite +
@@ -69,7 +74,9 @@ COSINE_ABS = 2e-6      # where z > 0.1 (r / z < 10)
 BLINN_REL = 1e-5
 
 GROUPS = ["rng", "slab", "camera", "disk", "local_to_world", "cosine", "diffuse_light", "point_light",
-          "blinn_phong", "reflect", "fr_dielectric", "refract", "unpack", "lru", "tiles", "domain_order"]
+          "blinn_phong", "reflect", "fr_dielectric", "refract", "unpack", "lru", "tiles", "domain_order",
+          "hdr_add", "ppm"]
+HDR_W, HDR_H = 13, 7
 
 
 def _p(a):
@@ -219,6 +226,21 @@ def make_cases(seed: int = 2024, scale: int = 1) -> dict:
         orders.append(cnt)
     c["domain_order"] = {"counts": np.concatenate([o.reshape(-1) for o in orders]),
                          "ndomains": np.array([len(o) for o in orders], np.int32)}
+
+    # retire: radiance of every magnitude added into few pixels, at the 1/spp
+    # scales of the workloads (and 1/7, inexact in binary)
+    nh = 1500 * scale
+    c["hdr_add"] = {"pixid": rng.integers(0, HDR_W * HDR_H, nh).astype(np.int32),
+                    "rgb": (rng.random((nh, 3)) * rng.choice([1e-4, 1, 1e3, 1e6], (nh, 1))).astype(f32),
+                    "scale": np.array([1.0, 1 / 8, 1 / 16, 1 / 7], np.float64)}
+
+    # PPM: truncation boundaries k / 1023, clamping, infinities and NaN
+    img = rng.uniform(-0.2, 1.3, (HDR_H, HDR_W, 4)).astype(f32)
+    k = rng.integers(0, 1024, 24)
+    edge = np.concatenate([k / 1023.0, np.nextafter((k / 1023.0).astype(f32), f32(0)), [0, -0.0, 1, 1.0000001,
+                           np.inf, -np.inf, np.nan, 1e-30, 0.99999994]]).astype(f32)
+    img.reshape(-1)[:len(edge)] = edge
+    c["ppm"] = {"rgba": img}
     return c
 
 
@@ -357,6 +379,23 @@ def reference_outputs(cases: dict, libs) -> dict:
         orders.append(od)
         off += ndom * LIST_SIZE
     out["domain_order"] = {"order": np.concatenate(orders)}
+
+    R.ref_hdr_add.argtypes = [C.c_int32, C.c_int32, I64, P, P, C.c_double, P]
+    R.ref_write_ppm.argtypes = [C.c_int32, C.c_int32, P, C.c_char_p]
+    hd = cases["hdr_add"]
+    imgs = []
+    for sc_ in hd["scale"]:
+        buf = np.zeros((HDR_W * HDR_H, 4), f32)
+        R.ref_hdr_add(HDR_W, HDR_H, len(hd["pixid"]), _p(hd["pixid"]), _p(hd["rgb"]), float(sc_), _p(buf))
+        imgs.append(buf)
+    out["hdr_add"] = {"rgba": np.stack(imgs)}
+
+    import tempfile
+    img = np.ascontiguousarray(cases["ppm"]["rgba"])
+    with tempfile.TemporaryDirectory() as tmp:
+        path = Path(tmp) / "ref.ppm"
+        R.ref_write_ppm(img.shape[1], img.shape[0], _p(img), str(path).encode())
+        out["ppm"] = {"bytes": np.frombuffer(path.read_bytes(), np.uint8).copy()}
     return out
 
 
@@ -428,6 +467,12 @@ def oracle_outputs(cases: dict) -> dict:
         scores.append(s)
         off += ndom * LIST_SIZE
     out["domain_order"] = {"order": np.concatenate(orders), "score": np.concatenate(scores)}
+
+    hd = cases["hdr_add"]
+    out["hdr_add"] = {"rgba": np.stack([O.hdr_add(np.zeros((HDR_W * HDR_H, 4), f32), hd["pixid"], hd["rgb"],
+                                                  float(sc_)) for sc_ in hd["scale"]])}
+    from spray_gb300 import image
+    out["ppm"] = {"bytes": np.frombuffer(image.ppm_bytes(cases["ppm"]["rgba"]), np.uint8).copy()}
     return out
 
 
@@ -472,6 +517,10 @@ def compare(group: str, cases: dict, ref: dict, orc: dict) -> None:
     elif group == "blinn_phong":
         rel = np.abs(r["out"] - o["out"]) / np.maximum(np.abs(r["out"]), np.float32(1e-30))
         assert np.all(rel <= BLINN_REL), rel.max()
+    elif group == "hdr_add":
+        assert _same(r["rgba"], o["rgba"])
+    elif group == "ppm":
+        assert r["bytes"].tobytes() == o["bytes"].tobytes()
     elif group == "fr_dielectric":
         assert _same(r["fr"], o["fr"]) and _same(r["wt"], o["wt"])
     elif group == "refract":
