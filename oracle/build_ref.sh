@@ -3,7 +3,7 @@
 # they lie (read-only), the two libraries the oracle is checked against:
 #   oracle/_ref/libref_rng.so   deps/embree/random_sampler.h (ref_rng.cpp)
 #   oracle/_ref/libref_path.so  render/{sampler,lru_cache,tile}.cc,
-#                               ooc/ooc_domain_stats.cc,
+#                               ooc/{ooc_domain_stats,ooc_vbuf}.cc,
 #                               io/{scene_loader,ply_loader}.cc,
 #                               deps/pbrt/memory.cpp and the inline code of
 #                               render/{aabb,camera,light,reflection}.h,
@@ -29,6 +29,6 @@ g++ $FLAGS -std=gnu++11 -fpermissive -DPBRT_HAVE_CONSTEXPR -DPBRT_CONSTEXPR=cons
     -I "$HERE/ref_shim" -I "$REF/src" -I "$REF/deps" \
     "$HERE/ref_path.cpp" "$REF/src/render/sampler.cc" "$REF/src/render/lru_cache.cc" "$REF/src/render/tile.cc" \
     "$REF/src/ooc/ooc_domain_stats.cc" "$REF/src/io/scene_loader.cc" "$REF/src/io/ply_loader.cc" \
-    "$REF/deps/pbrt/memory.cpp" \
+    "$REF/src/ooc/ooc_vbuf.cc" "$REF/deps/pbrt/memory.cpp" \
     -o "$HERE/_ref/libref_path.so"
 echo "$HERE/_ref/libref_rng.so $HERE/_ref/libref_path.so"

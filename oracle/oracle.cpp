@@ -1887,6 +1887,22 @@ int orc_hdr_add(int64_t n, const int32_t* pixid, const float* rgb, double scale,
   return 0;
 }
 
+int orc_vbuf_trace(int32_t nsamples, int32_t H, int64_t n, const uint8_t* op, const int32_t* samid,
+                   const int32_t* depth, float* hist, const float* t, uint8_t* result) {
+  if (H < 1 || H > orc::kMaxHistory) return 1;
+  orc::VBuf vb;
+  vb.resize((size_t)nsamples, H);
+  for (int64_t i = 0; i < n; ++i) {
+    orc::Ray r{};
+    r.samid = samid[i];
+    r.depth = depth[i];
+    for (int k = 0; k < H; ++k) r.history[k] = hist[H * i + k];
+    result[i] = (op[i] == 0 ? vb.update(t[i], &r) : vb.correct(r)) ? 1 : 0;
+    for (int k = 0; k < H; ++k) hist[H * i + k] = r.history[k];
+  }
+  return 0;
+}
+
 int orc_lru_trace(int32_t nd, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits) {
   orc::LruCache c;
   c.init(nd, cache_size);

@@ -139,6 +139,11 @@ int orc_unpack_color(int64_t n, const uint32_t* color, float* rgb);
 int orc_reflect(int64_t n, const float* wo, const float* normal, float* out);
 int orc_fr_dielectric(int64_t n, const float* args, float* fr, float* wt);
 int orc_refract(int64_t n, const float* args, uint8_t* ok, float* wt);
+/* VBuf over nsamples samples of history H: op 0 = update(t[i], ray),
+ * op 1 = correct(ray), for rays (samid, depth, hist[H * i ...]); result[i]
+ * is the returned flag, hist the ray's history afterwards */
+int orc_vbuf_trace(int32_t nsamples, int32_t H, int64_t n, const uint8_t* op, const int32_t* samid,
+                   const int32_t* depth, float* hist, const float* t, uint8_t* result);
 /* HdrImage::add in order: rgba[4 * pixid[i] + c] += scale * rgb[3 * i + c] */
 int orc_hdr_add(int64_t n, const int32_t* pixid, const float* rgb, double scale, float* rgba);
 

@@ -97,6 +97,7 @@ def lib() -> C.CDLL:
             getattr(L, "orc_" + name).argtypes = [C.c_int64, P, P, P]
         L.orc_cosine_sample.argtypes = [C.c_int64, P, P, P, P]
         L.orc_hdr_add.argtypes = [C.c_int64, P, P, C.c_double, P]
+        L.orc_vbuf_trace.argtypes = [C.c_int32, C.c_int32, C.c_int64, P, P, P, P, P, P]
         L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
         L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
         _lib = L
@@ -194,6 +195,17 @@ def point_light(light, p) -> np.ndarray:
     out = np.zeros_like(p)
     lib().orc_point_light(len(p), _p(light), _p(p), _p(out))
     return out
+
+
+def vbuf_trace(nsamples: int, history: int, op, samid, depth, hist, t) -> tuple[np.ndarray, np.ndarray]:
+    """VBuf operations in order (op 0 = update(t, ray), 1 = correct(ray)) ->
+    (returned flags, ray histories afterwards)."""
+    op = np.ascontiguousarray(op, np.uint8)
+    hist = np.array(hist, np.float32, copy=True).reshape(-1, history)
+    res = np.zeros(len(op), np.uint8)
+    lib().orc_vbuf_trace(nsamples, history, len(op), _p(op), _p(_i32(samid)), _p(_i32(depth)), _p(hist),
+                         _p(_f32(t)), _p(res))
+    return res, hist
 
 
 def hdr_add(rgba, pixid, rgb, scale: float) -> np.ndarray:

@@ -27,6 +27,7 @@
 #include "render/lru_cache.h"
 #include "render/tile.h"
 #include "ooc/ooc_domain_stats.h"
+#include "ooc/ooc_vbuf.h"
 #include "utils/comm.h"
 #include "utils/util.h"
 
@@ -305,6 +306,26 @@ int ref_transform_points(const float* m16, int64_t n, float* v) {
     v[i] = r.x;
     v[i + 1] = r.y;
     v[i + 2] = r.z;
+  }
+  return 0;
+}
+
+// VBuf::update / VBuf::correct (ooc/ooc_vbuf.cc:41-112) over nsamples samples
+// (one tile of nsamples x 1 pixels, one sample each) with the history size of
+// the CMake defaults; same layout as the oracle's orc_vbuf_trace
+int ref_vbuf_trace(int32_t nsamples, int64_t n, const uint8_t* op, const int32_t* samid, const int32_t* depth,
+                   float* hist, const float* t, uint8_t* result) {
+  const int H = SPRAY_SPECU_HISTORY_SIZE;
+  ooc::VBuf vb;
+  vb.resize(Tile(0, 0, nsamples, 1), 1);
+  for (int64_t i = 0; i < n; ++i) {
+    ooc::Ray r;
+    std::memset(&r, 0, sizeof(r));
+    r.samid = samid[i];
+    r.depth = depth[i];
+    for (int k = 0; k < H; ++k) r.history[k] = hist[H * i + k];
+    result[i] = (op[i] == 0 ? vb.update(t[i], &r) : vb.correct(r)) ? 1 : 0;
+    for (int k = 0; k < H; ++k) hist[H * i + k] = r.history[k];
   }
   return 0;
 }

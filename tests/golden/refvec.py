@@ -32,6 +32,7 @@ unpack         util::unpack, utils/util.h:75-79                     bit-exact
 lru            LruCache::init/load, render/lru_cache.cc:41-171      exact
 tiles          ImageScheduleTileList::init, render/tile.cc:317-391  exact
 domain_order   DomainStats::schedule, ooc/ooc_domain_stats.cc:60-111 ties
+vbuf           VBuf::update/correct, ooc/ooc_vbuf.cc:41-112          exact
 hdr_add        HdrImage::add (double scale), display/image.h:99-109 bit-exact
 ppm            HdrImage::writePpm, display/image.h:183-204         bytes (*)
 ============== ==================================================== =========
@@ -75,7 +76,8 @@ BLINN_REL = 1e-5
 
 GROUPS = ["rng", "slab", "camera", "disk", "local_to_world", "cosine", "diffuse_light", "point_light",
           "blinn_phong", "reflect", "fr_dielectric", "refract", "unpack", "lru", "tiles", "domain_order",
-          "hdr_add", "ppm"]
+          "vbuf", "hdr_add", "ppm"]
+VBUF_SAMPLES, HISTORY = 8, 4  # SPRAY_SPECU_HISTORY_SIZE in the reference's CMake defaults
 HDR_W, HDR_H = 13, 7
 
 
@@ -226,6 +228,16 @@ def make_cases(seed: int = 2024, scale: int = 1) -> dict:
         orders.append(cnt)
     c["domain_order"] = {"counts": np.concatenate([o.reshape(-1) for o in orders]),
                          "ndomains": np.array([len(o) for o in orders], np.int32)}
+
+    # speculation history: few samples and few distinct t values, so that
+    # equal, smaller and larger histories all occur
+    nv_ = 600 * scale
+    tv = np.array([0.5, 1, 2, 3, np.inf], f32)
+    c["vbuf"] = {"op": (rng.random(nv_) < 0.3).astype(np.uint8),
+                 "samid": rng.integers(0, VBUF_SAMPLES, nv_).astype(np.int32),
+                 "depth": rng.integers(0, HISTORY, nv_).astype(np.int32),
+                 "hist": tv[rng.integers(0, len(tv), (nv_, HISTORY))],
+                 "t": np.array([0.25, 0.5, 1, 1.5, 2, 3], f32)[rng.integers(0, 6, nv_)]}
 
     # retire: radiance of every magnitude added into few pixels, at the 1/spp
     # scales of the workloads (and 1/7, inexact in binary)
@@ -380,6 +392,14 @@ def reference_outputs(cases: dict, libs) -> dict:
         off += ndom * LIST_SIZE
     out["domain_order"] = {"order": np.concatenate(orders)}
 
+    vb = cases["vbuf"]
+    R.ref_vbuf_trace.argtypes = [C.c_int32, I64, P, P, P, P, P, P]
+    hist = np.array(vb["hist"], f32, copy=True)
+    res = np.zeros(len(vb["op"]), np.uint8)
+    R.ref_vbuf_trace(VBUF_SAMPLES, len(vb["op"]), _p(vb["op"]), _p(vb["samid"]), _p(vb["depth"]), _p(hist),
+                     _p(vb["t"]), _p(res))
+    out["vbuf"] = {"result": res, "hist": hist}
+
     R.ref_hdr_add.argtypes = [C.c_int32, C.c_int32, I64, P, P, C.c_double, P]
     R.ref_write_ppm.argtypes = [C.c_int32, C.c_int32, P, C.c_char_p]
     hd = cases["hdr_add"]
@@ -468,6 +488,10 @@ def oracle_outputs(cases: dict) -> dict:
         off += ndom * LIST_SIZE
     out["domain_order"] = {"order": np.concatenate(orders), "score": np.concatenate(scores)}
 
+    vb = cases["vbuf"]
+    res, hist = O.vbuf_trace(VBUF_SAMPLES, HISTORY, vb["op"], vb["samid"], vb["depth"], vb["hist"], vb["t"])
+    out["vbuf"] = {"result": res, "hist": hist}
+
     hd = cases["hdr_add"]
     out["hdr_add"] = {"rgba": np.stack([O.hdr_add(np.zeros((HDR_W * HDR_H, 4), f32), hd["pixid"], hd["rgb"],
                                                   float(sc_)) for sc_ in hd["scale"]])}
@@ -517,6 +541,9 @@ def compare(group: str, cases: dict, ref: dict, orc: dict) -> None:
     elif group == "blinn_phong":
         rel = np.abs(r["out"] - o["out"]) / np.maximum(np.abs(r["out"]), np.float32(1e-30))
         assert np.all(rel <= BLINN_REL), rel.max()
+    elif group == "vbuf":
+        assert np.array_equal(r["result"], o["result"]) and _same(r["hist"], o["hist"])
+        assert 0 < r["result"].mean() < 1  # both outcomes occur
     elif group == "hdr_add":
         assert _same(r["rgba"], o["rgba"])
     elif group == "ppm":
