@@ -332,24 +332,34 @@ int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void
  * No counterpart in the reference.  The scheduler (slab test of every ray
  * against every domain AABB, (t, id)-sorted domain lists, stable partition
  * into per-domain queues, as Isector::isectAll builds them) for callers that
- * cannot allocate device memory while they run -- a fixed device budget
- * reserved at start-up, another framework's stream capture (cudaMalloc is not
- * capturable, cudaFree synchronises the device), a host runtime that hands
- * out GPU memory from its own pool.  All scratch lives in one static device
- * array (about 13 MB, kept on each device that used it until exit); this call
- * allocates nothing.
+ * cannot allocate device memory while they run -- a renderer holding a fixed
+ * device budget reserved at start-up, a host runtime that hands out GPU
+ * memory from its own pool (a cudaMalloc behind its back breaks its
+ * accounting; cudaFree synchronises the device).  All scratch lives in one
+ * static device array (about 13 MB, kept on each device that used it until
+ * exit); this call allocates nothing.
  *   domain_bounds  device, 6 floats per domain (min xyz, max xyz), <= 256 domains
  *   ray_org/dir    device, 4 floats per ray (xyz + unused), 16-byte aligned,
  *                  <= 262144 rays, tnear 1e-3, tfar infinity
+ *   list_size      checked to lie in [1, 32]; it does not cap the lists (it
+ *                  only sizes the domain statistics, which this call does not
+ *                  keep): a ray's list holds up to 32 domains, and a ray that
+ *                  overlaps more fails the call with SPRAY_GPU_EOVERFLOW
  *   entries        device output, 2 words per entry: ray | depth << 26, tdom
  *                  bits; grouped by domain, ray order inside a domain
+ *   entry_capacity entries the output holds; fewer than the rays produce
+ *                  fails with SPRAY_GPU_EOVERFLOW ("entry_capacity")
  *   domain_start   device output, num_domains + 1 entry offsets
  *   num_entries    host output
  *   stream         cudaStream_t to run on (NULL = legacy default stream)
  * At most 1048576 entries; larger requests fail with SPRAY_GPU_EINVAL or
- * SPRAY_GPU_EOVERFLOW.  Blocks until the stream finished the call.  The first
- * call on a device looks up the scratch address; make it before any stream
- * capture.  Calls share the scratch: calls that overlap on the GPU race. */
+ * SPRAY_GPU_EOVERFLOW.  The call reads its entry count back and synchronises
+ * `stream` before it returns, so it must not be made while that stream or the
+ * device is being captured into a CUDA graph.  The first call on a device
+ * looks up the scratch array's device address and keeps it for the process;
+ * after cudaDeviceReset on that device the kept address is stale, so a
+ * process that resets a device must not call this again on it.  Calls share
+ * the scratch: calls that overlap on the GPU race. */
 int spray_gpu_schedule_static(const float* domain_bounds, int32_t num_domains, const float* ray_org,
                               const float* ray_dir, int32_t num_rays, int32_t list_size,
                               uint32_t* entries, int64_t entry_capacity, uint32_t* domain_start,

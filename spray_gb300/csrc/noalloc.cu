@@ -1,14 +1,15 @@
 // Allocation-free scheduling entry point.
 //
 // Some callers cannot allocate device memory while they run: a renderer that
-// owns a fixed device budget carved out at start-up, code running inside
-// another framework's stream capture (cudaMalloc is not capturable and
-// cudaFree synchronises the device), or a host runtime whose GPU memory is
-// handed out by its own pool.  spray_gpu_schedule_static lets such callers
-// run the speculative scheduler -- slab test of every ray against every domain
-// box, (t, id)-sorted domain lists, stable partition into per-domain queues --
-// with no allocation: the scheduler's scratch lives in one file-scope device
-// array of fixed size, and the caller passes only inputs and outputs.
+// owns a fixed device budget carved out at start-up (cudaMalloc could fail or
+// push it over its share), or a host runtime whose GPU memory is handed out by
+// its own pool (a cudaMalloc behind its back breaks its accounting, and
+// cudaFree synchronises the whole device).  spray_gpu_schedule_static lets
+// such callers run the speculative scheduler -- slab test of every ray against
+// every domain box, (t, id)-sorted domain lists, stable partition into
+// per-domain queues -- with no allocation: the scheduler's scratch lives in
+// one file-scope device array of fixed size, and the caller passes only inputs
+// and outputs.
 //
 // Limits and sharing:
 //  * at most kStaticMaxRays rays, kStaticMaxDomains domains and
@@ -20,13 +21,19 @@
 //    counters that must start at zero are cleared by each call, so calls that
 //    overlap on the GPU (different streams, or different host threads on one
 //    device) race and corrupt each other -- serialise them;
+//  * the call reads its entry count back and synchronises the caller's
+//    stream before it returns, so it must not be made while that stream (or
+//    the device) is being captured into a CUDA graph;
 //  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.
+//    (cudaGetSymbolAddress) with that device current and keeps it for the
+//    life of the process; after a cudaDeviceReset the kept address is stale,
+//    so do not call this entry point again in a process that reset a device
+//    it used.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <mutex>
+#include <stdexcept>
 #include <string>
 
 #include "../../include/spray_gpu.h"
@@ -100,6 +107,7 @@ extern "C" int spray_gpu_schedule_static(const float* domain_bounds, int32_t num
                                          int64_t entry_capacity, uint32_t* domain_start,
                                          int64_t* num_entries, void* stream) {
   using namespace spray;
+  try {
   if (!domain_bounds || !ray_org || !ray_dir || !entries || !domain_start || !num_entries)
     return fail(SPRAY_GPU_EINVAL, "null argument");
   if (num_domains <= 0 || num_domains > kStaticMaxDomains)
@@ -166,4 +174,9 @@ extern "C" int spray_gpu_schedule_static(const float* domain_bounds, int32_t num
   if (ctr.entry_overflows) return fail(SPRAY_GPU_EOVERFLOW, "entry_capacity too small");
   *num_entries = (int64_t)ne;
   return SPRAY_GPU_OK;
+  } catch (const std::exception& ex) {
+    // no C++ exception crosses the C boundary (launch configuration errors,
+    // allocation failures of the error strings)
+    return fail(SPRAY_GPU_ECUDA, ex.what());
+  }
 }

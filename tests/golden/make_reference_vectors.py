@@ -36,7 +36,7 @@ SEED, SCALE = 2024, 1
 
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--reference-dir", default=os.environ.get("SPRAY_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--reference-dir", default=str(V.REFERENCE_SOURCES))
     args = ap.parse_args()
     env = dict(os.environ, SPRAY_REFERENCE_DIR=args.reference_dir)
     subprocess.run(["sh", str(ROOT / "oracle" / "build_ref.sh")], check=True, env=env)

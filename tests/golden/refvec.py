@@ -53,11 +53,14 @@ from __future__ import annotations
 
 import base64
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
+# the reference source tree these helpers read (oracle/build_ref.sh uses the same variable)
+REFERENCE_SOURCES = Path(os.environ.get("SPRAY_REFERENCE_DIR", "/root/reference"))
 REF_DIR = ROOT / "oracle" / "_ref"
 FIXTURE = Path(__file__).resolve().parent / "reference_vectors.json"
 LIST_SIZE = 16  # SPRAY_RAY_DOMAIN_LIST_SIZE in the reference's CMake defaults

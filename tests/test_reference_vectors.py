@@ -127,7 +127,7 @@ def test_scene_fixture_matches_the_reference_libraries(scene_vectors, tmp_path):
         assert np.array_equal(np.ascontiguousarray(live[k]).view(np.uint8), np.ascontiguousarray(a).view(np.uint8)), k
 
 
-REF_EXAMPLES = Path(os.environ.get("SPRAY_REFERENCE_DIR", "/root/reference")) / "examples"
+REF_EXAMPLES = V.REFERENCE_SOURCES / "examples"
 
 
 @needs_ref

@@ -8,8 +8,9 @@ import pytest
 
 import spray_gb300 as sg
 from spray_gb300 import scenes
+from golden import refvec
 
-REF_EXAMPLES = Path("/root/reference/examples")
+REF_EXAMPLES = refvec.REFERENCE_SOURCES / "examples"
 
 
 def test_wavelet_mesh_is_watertight_and_oriented(lib_built):

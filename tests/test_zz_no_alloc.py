@@ -1,9 +1,9 @@
 """The allocation-free scheduling entry point against the regular one.
 
 spray_gpu_schedule_static serves callers that cannot allocate device memory
-while they run (a fixed budget reserved at start-up, another framework's
-stream capture, a runtime with its own device pool): its scratch is one static
-device array.  Its queues must equal, entry for entry, the queues the regular
+while they run (a renderer with a fixed device budget reserved at start-up, a
+runtime that hands out GPU memory from its own pool): its scratch is one
+static device array.  Its queues must equal, entry for entry, the queues the regular
 path (spray_gpu_trace, read back through spray_gpu_debug_copy) builds from the
 same rays -- on two calls in a row, since calls share and reuse the scratch.
 This file is collected last so that a failure here does not hide the others.
@@ -66,3 +66,61 @@ def test_static_scratch_rejects_oversize_requests(lib_built):
     with pytest.raises(sg.SprayError) as e:
         sg.schedule_static(16, 8, 16, 16, (1 << 18) + 1, 16, 16, 1, 16)
     assert e.value.code == sg.EINVAL and "num_rays" in str(e.value)
+
+
+def _device_rays(torch, n):
+    dev = torch.device("cuda:0")
+    return (torch.zeros((max(n, 1), 4), dtype=torch.float32, device=dev),
+            torch.zeros((max(n, 1), 4), dtype=torch.float32, device=dev))
+
+
+def test_static_scratch_reports_small_entry_capacity(lib_built):
+    # the device detects that the queues need more entries than the caller's
+    # output holds; the scatter never writes past entry_capacity
+    torch = pytest.importorskip("torch")
+    scene = scenes.wavelet_grid(2, 24, colors="albedo", light="point")
+    cfg = small_config(image_w=48, image_h=32, cull=0, debug_capture=1)
+    t = sg.Tracer(cfg)
+    t.set_scene(scene)
+    t.set_camera(*scenes.orbit_camera(scene))
+    t.trace()
+    rays = t.debug(sg.DBG_RAYS, 0)
+    want = t.debug(sg.DBG_RQUEUES, 0)
+    n, D = len(rays), len(scene.domains)
+    dev = torch.device("cuda:0")
+    org, dr = _device_rays(torch, n)
+    org[:, :3] = torch.from_numpy(np.ascontiguousarray(rays["org"])).to(dev)
+    dr[:, :3] = torch.from_numpy(np.ascontiguousarray(rays["dir"])).to(dev)
+    bounds = torch.from_numpy(np.stack([d.bounds for d in scene.domains]).astype(np.float32)).to(dev)
+    cap = len(want) - 1
+    entries = torch.full((cap + 1, 2), -7, dtype=torch.int32, device=dev)
+    starts = torch.zeros(D + 1, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    with pytest.raises(sg.SprayError) as e:
+        sg.schedule_static(bounds.data_ptr(), D, org.data_ptr(), dr.data_ptr(), n, cfg["list_size"],
+                           entries.data_ptr(), cap, starts.data_ptr())
+    assert e.value.code == sg.EOVERFLOW and "entry_capacity" in str(e.value)
+    # the guard row past the capacity is untouched
+    assert entries[cap].cpu().tolist() == [-7, -7]
+    # and the scratch is usable again afterwards with a large enough output
+    entries = torch.zeros((len(want), 2), dtype=torch.int32, device=dev)
+    k = sg.schedule_static(bounds.data_ptr(), D, org.data_ptr(), dr.data_ptr(), n, cfg["list_size"],
+                           entries.data_ptr(), len(want), starts.data_ptr())
+    assert k == len(want)
+
+
+def test_static_scratch_zero_rays(lib_built):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    D = 8
+    bounds = torch.zeros((D, 6), dtype=torch.float32, device=dev)
+    bounds[:, 3:] = 1.0
+    org, dr = _device_rays(torch, 0)
+    entries = torch.zeros((4, 2), dtype=torch.int32, device=dev)
+    starts = torch.full((D + 1,), -1, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        k = sg.schedule_static(bounds.data_ptr(), D, org.data_ptr(), dr.data_ptr(), 0, 16,
+                               entries.data_ptr(), 4, starts.data_ptr())
+        assert k == 0
+        assert np.array_equal(starts.cpu().numpy(), np.zeros(D + 1, np.int32))
