@@ -5,23 +5,31 @@ Default workload (the configuration the headline metric is quoted on): the
 1920x1080, 16 spp, 5 bounces with Russian roulette from bounce 3, per-domain
 albedo, one emissive quad light, seeded orbit camera.  Prints one JSON line.
 
-  value      Mrays/s of all logical rays (primary + shadow + bounce), frames
-             timed with CUDA events on the tracer's stream, scene resident
-  e2e        the same metric through spray_gpu_trace with the image copied to
-             pinned host memory every frame (wall clock around the C ABI call)
-  roofline   closest-hit traversal kernel: algorithmic bytes / kernel time
+  value         Mrays/s of all logical rays (primary + shadow + bounce), frames
+                timed with CUDA events on the tracer's stream, scene resident
+  e2e           the same metric through spray_gpu_trace with the image copied
+                to pinned host memory every frame (wall clock around the call)
+  roofline      closest-hit traversal kernel: algorithmic bytes / kernel time
+  accuracy      the GPU renders the CPU baseline's reduced frame too: image
+                RMSE against the reference loop restated on the CPU (oracle
+                mode A), bit equality with the wavefront restatement (mode B),
+                hit and occlusion agreement of every depth's rays
+  the benchmark spec    the 512-domain out-of-core workload (C3) under the plain
+                speculative order, batched passes and the learned proposal:
+                Mrays/s by ray class, domain loads, bytes copied and bytes read
+                in place from host memory per frame
   cpu_baseline  the CPU restatement of the reference loop (speculative queues,
-             DomainStats order, VBuf history) on a downscaled frame, all cores
+                DomainStats order, VBuf history) on a downscaled frame, all cores
 
---impl reference times that CPU restatement alone on the same workload (the
-reference binary itself needs Embree 2.17, glm, glog and MPI, which are not
-available), rank 0 only.
+--impl reference times that CPU restatement alone on the same workload and the
+same full frame.  It loads the scene with the oracle's own reader and never
+loads the CUDA library (the reference binary itself needs Embree 2.17, glm,
+glog and MPI, which are not available).  Rank 0 only.
 """
 from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -45,11 +53,6 @@ FALLBACK_HBM_GBS = 6800.0
 NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
 
 
-def workload(name: str, scene=None):
-    from spray_gb300 import scenes
-    return scenes.workload_config(name, scene)
-
-
 def describe(name: str, spec: dict, cfg: dict) -> str:
     g = spec["grid"]
     if name == "c5":
@@ -59,6 +62,38 @@ def describe(name: str, spec: dict, cfg: dict) -> str:
     mode = "AO" if cfg.get("ao_mode") else "path tracing"
     return (f"{name}: {g}x{g}x{g} wavelet domains ({spec['samples']}^3 isosurfaces), {mode}, "
             f"{cfg['image_w']}x{cfg['image_h']}, {cfg['pixel_samples']} spp, {cfg['bounces']} bounces")
+
+
+def scene_file(name: str) -> Path:
+    """The workload's .spray file, generated once.  Generation uses the
+    library's wavelet generator; a process that must not load the library
+    (the reference arm) runs it in a child process."""
+    from spray_gb300 import scenes
+    spec = scenes.CONFIGS[name]
+    d = scenes.scene_dir(name)
+    if not (d / "scene.spray").exists():
+        subprocess.run([sys.executable, "-c",
+                        f"import sys; sys.path.insert(0, {str(ROOT)!r}); "
+                        f"from spray_gb300 import scenes; scenes.benchmark_scene({name!r})"], check=True)
+    return d / "scene.spray"
+
+
+def bench_config(name: str, spec: dict, cfg: dict, scene, policy: str, tuned, world: int,
+                 views=None) -> dict:
+    """The `config` object of the JSON line, from host-side facts only, so
+    that both arms print the same one."""
+    W, H = cfg["image_w"], cfg["image_h"]
+    c = {"workload": describe(name, spec, cfg), "scheduler": POLICIES[policy][1],
+         "domains": len(scene.domains), "triangles": int(sum(len(d.faces) for d in scene.domains)),
+         "image": [W, H], "spp": cfg["pixel_samples"], "bounces": cfg["bounces"],
+         "l2": "256 MiB buffer written before every timed frame; ray state > L2",
+         "parallelism": f"replicas x{world} (one view per GPU)", "tuned": tuned}
+    if views is not None:
+        c["views"] = {"count": len(views), "pixels": sum(v["image_w"] * v["image_h"] for v in views),
+                      "samples": sum(v["image_w"] * v["image_h"] * v["pixel_samples"] for v in views),
+                      "ao_views": sum(1 for v in views if v["ao_mode"]),
+                      "sizes": sorted({v["image_w"] for v in views})}
+    return c
 
 
 def clock_sampler(out: Path):
@@ -109,19 +144,12 @@ def load_profile_traffic(name: str):
     """DRAM bytes per algorithmic byte of the closest-hit kernel, from the committed ncu summary."""
     p = ROOT / "profiles" / f"trace_closest_{name}.json"
     try:
-        d = json.loads(p.read_text())
-        return d
+        return json.loads(p.read_text())
     except Exception:
         return None
 
 
-def cpu_speculative(name, spec, cfg, threads: int, scale: int, frame: int = 0):
-    """The reference loop restated on the CPU, on a frame downscaled by `scale`."""
-    from oracle import oracle as O
-    from spray_gb300 import scenes
-    import spray_gb300 as sg
-    path, _ = scenes.benchmark_scene(name)
-    scene = sg.Scene.load(path, path.parent)
+def oracle_config(cfg: dict, scale: int) -> dict:
     c = dict(cfg)
     c["image_w"] = max(8, cfg["image_w"] // scale)
     c["image_h"] = max(8, cfg["image_h"] // scale)
@@ -131,45 +159,190 @@ def cpu_speculative(name, spec, cfg, threads: int, scale: int, frame: int = 0):
     c.setdefault("max_samples_per_rank", 1 << 20)
     c.setdefault("num_ranks", 1)
     c.setdefault("rank", 0)
+    return c
+
+
+def cpu_speculative(scene, cfg, threads: int, scale: int, frame: int = 0):
+    """The reference loop restated on the CPU (oracle mode A), on a frame
+    downscaled by `scale` per axis.  Returns (rays, seconds, config, stats,
+    image, oracle)."""
+    from oracle import oracle as O
+    from spray_gb300 import scenes
+    c = oracle_config(cfg, scale)
     o = O.Oracle(c, scene)
     o.set_camera(*scenes.orbit_camera(scene, frame=frame))
     t0 = time.perf_counter()
     img, st = o.render_speculative(threads)
     dt = time.perf_counter() - t0
     rays = st["rays_primary"] + st["rays_shadow"] + st["rays_bounce"]
-    return rays, dt, c, st
+    return rays, dt, c, st, img, o
 
 
-def run_reference(args, spec, cfg, rank):
+def run_reference(args, rank):
+    """Times the CPU restatement of the reference loop on the full workload
+    frame.  Never loads the CUDA library: the scene comes from the oracle's
+    own .spray/PLY reader."""
     if rank != 0:
         return
+    from oracle import scene_io
+    from spray_gb300 import autotune, scenes
+    path = scene_file(args.config)
+    scene = scene_io.load(path, path.parent)
+    spec, cfg = scenes.workload_config(args.config, scene)
+    if args.config == "c5":
+        print(json.dumps({"impl": "reference", "unavailable": "the multi-view batch has no counterpart in "
+                          "the reference loop (one camera per renderer)"}), flush=True)
+        return
+    t = autotune.load(args.config, POLICIES[args.policy][0]) if args.tuned else None
+    tuned = dict(t["params"]) if t else None
     threads = os.cpu_count() or 1
-    scale = args.cpu_scale
+    scale = args.ref_scale
     for _ in range(args.warmup):
-        cpu_speculative(args.config, spec, cfg, threads, scale)
-    rays_t, secs = 0, 0.0
-    st_last = None
-    for k in range(args.steps):
-        rays, dt, c, st = cpu_speculative(args.config, spec, cfg, threads, scale)
+        cpu_speculative(scene, cfg, threads, scale)
+    rays_t, secs, st_last, c = 0, 0.0, None, None
+    for _ in range(args.steps):
+        rays, dt, c, st, _, o = cpu_speculative(scene, cfg, threads, scale)
+        o.close()
         rays_t += rays
         secs += dt
         st_last = st
     v = rays_t / secs / 1e6
-    sample = (f"{c['image_w']}x{c['image_h']} frame of the same scene, camera, spp and bounces "
-              f"(1/{scale} of each image dimension), speculative loop with {threads} OpenMP threads")
+    sample = (f"the full {c['image_w']}x{c['image_h']} frame per step" if scale == 1 else
+              f"{c['image_w']}x{c['image_h']} frame (1/{scale} per axis)") + \
+        f" of the same scene, camera, spp and bounces; speculative loop with {threads} OpenMP threads"
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": describe(args.config, spec, cfg)},
-        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+        "data": "synthetic (seeded wavelet isosurface scene, seeded orbit camera)",
+        "config": bench_config(args.config, spec, cfg, scene, args.policy, tuned, args.gpus),
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "domain_loads_per_frame": st_last["domain_loads"] if st_last else None,
-        "note": "reference binary unbuildable here (Embree 2.17, glm, glog, MPI absent); "
-                "timed the CPU restatement of its speculative loop",
+        "rays_per_frame": {k: st_last[f"rays_{k}"] for k in ("primary", "shadow", "bounce")},
+        "domain_loads_per_frame": st_last["domain_loads"],
+        "note": "reference binary unbuildable here (Embree 2.17, glm, glog, MPI absent); timed the CPU "
+                "restatement of its speculative loop (oracle mode A), scene read by the oracle's own loader",
     }
     print(json.dumps(line), flush=True)
+
+
+def accuracy_report(scene, cfg, cam, mode_a_img, oracle_obj, device: int) -> dict:
+    """The GPU renders the CPU baseline's reduced frame with its stage
+    buffers kept, and is compared with the oracle (image, hits, occlusion)."""
+    import spray_gb300 as sg
+    from oracle import accuracy as A
+    c = dict(cfg)
+    c["debug_capture"] = 1
+    t = sg.Tracer(c, device=device)
+    t.set_scene(scene)
+    t.set_camera(*cam)
+    img, st = t.trace()
+    mode_b, _ = oracle_obj.render_wavefront()
+    hits, shadows = {}, {}
+    for b in range(cfg["bounces"]):
+        rays = t.debug(sg.DBG_RAYS, b)
+        if len(rays) == 0:
+            break
+        h = t.debug(sg.DBG_HITS, b)
+        hits[str(b)] = A.hit_agreement(rays, h, oracle_obj)
+        shadows[str(b)] = A.shadow_agreement(t.debug(sg.DBG_SHADOWS, b), h, oracle_obj)
+    t.close()
+    rep = A.frame_report(img, mode_a_img, mode_b, hits, shadows)
+    rep["frame"] = [c["image_w"], c["image_h"]]
+    return rep
+
+
+def north_star_block(args, device: int) -> dict:
+    """C3 (512 domains out of core) under the plain speculative order, the
+    batched passes and the learned proposal: the metric's comparison."""
+    import spray_gb300 as sg
+    from spray_gb300 import autotune, scenes
+    from oracle import accuracy as A
+    path, spec = scenes.benchmark_scene("c3")
+    scene = sg.Scene.load(path, path.parent)
+    _, cfg0 = scenes.workload_config("c3", scene)
+    cam = scenes.orbit_camera(scene)
+    prep = Path(tempfile.gettempdir()) / f"spray_c3_prepared_{os.getpid()}"
+    sg.prepare_scene(scene, prep)
+    out = {"workload": describe("c3", spec, cfg0), "policies": {}}
+    frames = max(args.steps, args.ns_frames)
+    ref_img = None
+    small = None
+    for name in ("plain", "batched", "learned"):
+        cfg = dict(cfg0)
+        pol = POLICIES[name][0]
+        cfg["schedule_policy"] = pol
+        t = autotune.load("c3", pol) if args.tuned else None
+        if t and t.get("policy") == pol:
+            cfg.update(t["params"])
+        if name == "learned":
+            cfg["learn_frames"] = 1
+        tr = sg.Tracer(cfg, device=device)
+        tr.set_scene_prepared(prep, len(scene.domains), scene.lights)
+        tr.set_camera(*cam)
+        img = np.empty((cfg["image_h"], cfg["image_w"], 4), np.float32)
+        warm = [tr.trace(img)[1] for _ in range(max(args.warmup, 3))]
+        sts = [tr.trace(img)[1] for _ in range(frames)]
+        if ref_img is None:
+            ref_img = img.copy()
+        ms = sum(s["frame_ms"] for s in sts)
+        rays = {k: sum(s[f"rays_{k}"] for s in sts) for k in ("primary", "shadow", "bounce")}
+        n = len(sts)
+        vis = sum(s["visits_radiance"] + s["visits_shadow"] for s in sts)
+        r = {"scheduler": POLICIES[name][1], "frames": n, "ms_per_frame": ms / n,
+             "mrays_per_s": sum(rays.values()) / (ms * 1e-3) / 1e6,
+             "mrays_per_s_by_class": {k: v / (ms * 1e-3) / 1e6 for k, v in rays.items()},
+             "visits_per_ray": vis / max(sum(rays.values()), 1),
+             "domain_loads_per_frame": sum(s["domain_loads"] for s in sts) / n,
+             "h2d_bytes_per_frame": sum(s["h2d_bytes"] for s in sts) / n,
+             "inplace_bytes_per_frame": sum(s["inplace_bytes"] for s in sts) / n,
+             "inplace_domains_per_frame": sum(s["inplace_domains"] for s in sts) / n,
+             "image_equals_plain": bool(A.bit_exact(img, ref_img)),
+             "tuned": t["params"] if t and t.get("policy") == pol else None}
+        if name == "learned":
+            w0 = next((w for w in warm if w["learn_ms"] > 0), None)
+            r["learn"] = {"trained_before_timing": bool(warm[-1]["learn_trained"]),
+                          "pairs": warm[-1]["learn_pairs"], "train_ms": w0["learn_ms"] if w0 else None,
+                          "loss": w0["learn_loss"] if w0 else None}
+        s0 = sts[-1]
+        out["cache"] = {"slots": s0["cache_slots"], "slot_bytes": s0["cache_slot_bytes"],
+                        "cache_bytes": s0["cache_slots"] * s0["cache_slot_bytes"],
+                        "scene_bytes": s0["scene_bytes"], "scene_triangles": s0["scene_triangles"],
+                        "fraction_of_scene": s0["cache_slots"] * s0["cache_slot_bytes"] / max(s0["scene_bytes"], 1),
+                        "note": "the cache holds half of the domains, the 8 GiB of ~16 GB ratio of the "
+                                "workload description; the generated scene is smaller than its estimate"}
+        out["policies"][name] = r
+        tr.close()
+    p, b, l = (out["policies"][k] for k in ("plain", "batched", "learned"))
+    out["learned_vs_plain"] = {"speedup": l["mrays_per_s"] / p["mrays_per_s"],
+                               "domain_load_reduction": 1 - l["domain_loads_per_frame"] / max(p["domain_loads_per_frame"], 1e-9),
+                               "bytes_moved_reduction": 1 - (l["h2d_bytes_per_frame"] + l["inplace_bytes_per_frame"]) /
+                               max(p["h2d_bytes_per_frame"] + p["inplace_bytes_per_frame"], 1e-9)}
+    out["learned_vs_batched"] = {"speedup": l["mrays_per_s"] / b["mrays_per_s"],
+                                 "visits_per_ray_ratio": l["visits_per_ray"] / b["visits_per_ray"]}
+    # accuracy at this scene's settings on a reduced frame (all 512 domains,
+    # list size 22, 8 spp, 4 bounces): the learned order against the oracle
+    if not args.no_cpu_baseline:
+        cfg = dict(cfg0)
+        cfg["schedule_policy"] = POLICIES["learned"][0]
+        cfg["learn_frames"] = 1
+        threads = os.cpu_count() or 1
+        scale = max(1, cfg0["image_w"] // args.ns_accuracy_size)
+        _, _, c, _, mode_a, o = cpu_speculative(scene, cfg, threads, scale)
+        tr = sg.Tracer(dict(c, schedule_policy=3, learn_frames=1), device=device)
+        tr.set_scene_prepared(prep, len(scene.domains), scene.lights)
+        tr.set_camera(*cam)
+        tr.trace()
+        img, _ = tr.trace()  # trained after the first frame
+        tr.close()
+        mode_b, _ = o.render_wavefront()
+        out["accuracy"] = {"frame": [c["image_w"], c["image_h"]],
+                           "image_rmse_vs_oracle": A.image_rmse(img, mode_a),
+                           "bit_exact_vs_wavefront_oracle": A.bit_exact(img, mode_b)}
+        o.close()
+    import shutil
+    shutil.rmtree(prep, ignore_errors=True)
+    return out
 
 
 def main():
@@ -180,6 +353,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
     ap.add_argument("--cpu-scale", type=int, default=2, help="CPU baseline frame downscale per axis")
+    ap.add_argument("--ref-scale", type=int, default=1,
+                    help="--impl reference: frame downscale per axis (1 = the workload's full frame)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--policy", default="plain", choices=list(POLICIES),
@@ -195,6 +370,12 @@ def main():
                     help="apply the committed autotuner result for the workload (spray_gb300/tuned)")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide the image size (profiling captures on a small frame only)")
+    ap.add_argument("--north-star", type=int, default=1, choices=[0, 1],
+                    help="1: also run the C3 plain / batched / learned comparison (rank 0 of a single-GPU run)")
+    ap.add_argument("--ns-frames", type=int, default=15, help="timed C3 frames per scheduler")
+    ap.add_argument("--ns-accuracy-size", type=int, default=256, help="C3 accuracy frame width")
+    ap.add_argument("--accuracy", type=int, default=1, choices=[0, 1],
+                    help="1: compare the GPU with the oracle on the CPU baseline's reduced frame")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -204,12 +385,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
     if args.impl == "reference":
-        if rank == 0:
-            import spray_gb300 as sg
-            from spray_gb300 import scenes
-            path, _ = scenes.benchmark_scene(args.config)
-            spec, cfg = workload(args.config, sg.Scene.load(path, path.parent))
-            run_reference(args, spec, cfg, rank)
+        run_reference(args, rank)
         return
 
     import torch
@@ -244,7 +420,8 @@ def main():
     barrier()
     path, _ = scenes.benchmark_scene(args.config)
     scene = sg.Scene.load(path, path.parent)
-    spec, cfg = workload(args.config, scene)
+    spec, cfg = scenes.workload_config(args.config, scene)
+    base_cfg = dict(cfg)
     if args.scale > 1:
         cfg["image_w"] = max(8, cfg["image_w"] // args.scale)
         cfg["image_h"] = max(8, cfg["image_h"] // args.scale)
@@ -266,7 +443,8 @@ def main():
     tracer = sg.Tracer(cfg, device=local)
     tracer.set_scene(scene)
     # weak scaling: each rank renders its own seeded view of the scene
-    tracer.set_camera(*scenes.orbit_camera(scene, frame=rank))
+    cam = scenes.orbit_camera(scene, frame=rank)
+    tracer.set_camera(*cam)
     W, H = cfg["image_w"], cfg["image_h"]
     views = None
     if args.config == "c5":
@@ -336,6 +514,8 @@ def main():
         proc.wait()
         fh.close()
     clocks = clock_summary(clk_path, smi_index(local))
+    tracer.close()
+    del flush
 
     s0 = stats[-1]
     peak, peak_kind = hbm_peak()
@@ -345,8 +525,12 @@ def main():
                   + s0["nodes_shadow"] * NODE_BYTES + s0["tris_shadow"] * TRI_BYTES)
     if s0["trace_ms"] >= s0["occlude_ms"]:
         kname, kbytes, kms, klaunch = "closest-hit traversal", trace_bytes, s0["trace_ms"], s0["trace_launches"]
+        kvisits = s0["visits_radiance"]
+        kmin = kvisits * (RAY_BYTES + ENTRY_BYTES + HIT_BYTES)
     else:
         kname, kbytes, kms, klaunch = "occlusion traversal", occl_bytes, s0["occlude_ms"], s0["occlude_launches"]
+        kvisits = s0["visits_shadow"]
+        kmin = kvisits * (RAY_BYTES + ENTRY_BYTES)
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
     prof = load_profile_traffic(args.config)
     traffic = None
@@ -360,12 +544,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": allmax(dev_ms / args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded wavelet isosurface scene, seeded orbit camera)",
-        "config": {"workload": describe(args.config, spec, cfg), "scheduler": POLICIES[args.policy][1],
-                   "domains": len(scene.domains), "triangles": s0["scene_triangles"],
-                   "image": [W, H], "spp": cfg["pixel_samples"], "bounces": cfg["bounces"],
-                   "l2": "256 MiB buffer written before every timed frame; ray state > L2",
-                   "parallelism": f"replicas x{world} (one view per GPU)",
-                   "tuned": tuned},
+        "config": bench_config(args.config, spec, cfg, scene, args.policy, tuned, world, views),
         "rays_per_frame": {"primary": s0["rays_primary"], "shadow": s0["rays_shadow"],
                            "bounce": s0["rays_bounce"]},
         "mrays_per_s_by_class": {k: s0[f"rays_{k}"] / (s0["frame_ms"] * 1e-3) / 1e6
@@ -374,31 +553,44 @@ def main():
         "visits_culled": s0["visits_culled"],
         "domain_loads_per_frame": s0["domain_loads"],
         "inplace_domains_per_frame": s0["inplace_domains"],
+        "inplace_bytes_per_frame": s0["inplace_bytes"],
         "breakdown_ms_per_frame": {k: s0[f"{k}_ms"] for k in ("frame", "schedule", "trace", "occlude", "h2d")},
         "h2d_bytes_per_frame": s0["h2d_bytes"],
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+        # The traversal is bound by latency and SIMT divergence, not by DRAM:
+        # its node and triangle reads are served mostly by L1/L2.  `achieved`
+        # is the algorithmic bytes the walk requested (its own node and
+        # triangle counts) per second against the HBM copy peak;
+        # `achieved_floor` counts only the bytes every visit must move (ray,
+        # queue entry, hit record), a lower bound independent of the walk.
+        "roofline": {"bound": "latency", "peak_kind": "hbm", "kernel": kname, "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_frame": kbytes,
+                     "achieved_floor": kmin / (kms * 1e-3) / 1e9 if kms > 0 else 0.0,
+                     "frac_floor": (kmin / (kms * 1e-3) / 1e9) / peak if kms > 0 else 0.0,
                      "launches_per_frame": klaunch, "kernel_ms_per_frame": kms},
         "clocks": clocks,
     }
     if learn is not None:
         out["learn"] = learn
-    if views is not None:
-        out["config"]["views"] = {"count": len(views), "pixels": npix,
-                                  "samples": sum(v["image_w"] * v["image_h"] * v["pixel_samples"] for v in views),
-                                  "ao_views": sum(1 for v in views if v["ao_mode"]),
-                                  "sizes": sorted({v["image_w"] for v in views})}
     if rank == 0 and not args.no_cpu_baseline and views is None:
         threads = os.cpu_count() or 1
-        r, dt, c, _ = cpu_speculative(args.config, spec, cfg, threads, args.cpu_scale)
+        ocfg = dict(base_cfg)
+        ocfg["schedule_policy"] = POLICIES[args.policy][0]
+        r, dt, c, _, mode_a, o = cpu_speculative(scene, ocfg, threads, args.cpu_scale)
         out["cpu_baseline"] = {
             "value": r / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
             "sample": f"{c['image_w']}x{c['image_h']} frame (1/{args.cpu_scale} per axis), same scene, "
                       f"camera, spp and bounces; speculative loop, {threads} OpenMP threads"}
+        if args.accuracy:
+            gcfg = dict(cfg)
+            gcfg.update(image_w=c["image_w"], image_h=c["image_h"], graphs=0)
+            out["accuracy"] = accuracy_report(scene, gcfg, cam, mode_a, o, local)
+        o.close()
+    if rank == 0 and world == 1 and args.north_star and args.config == "c2":
+        out["north_star"] = north_star_block(args, local)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -190,6 +190,11 @@ typedef struct spray_gpu_stats {
   double learn_ms;          /* policy 3: device time spent training after this frame */
   double learn_loss;        /* policy 3: mean loss of the last training batch */
   int64_t inplace_domains;  /* out of core: (domain, batch) pairs traced in place from host memory */
+  int64_t inplace_bytes;    /* out of core: bytes those traversals requested from pinned host memory
+                               (128 per BVH node, 48 per triangle, 60 per closest hit's faces,
+                               colours and normals); not included in h2d_bytes */
+  int64_t cache_slots;      /* out of core: device domain-cache capacity in domains (0 in core) */
+  int64_t cache_slot_bytes; /* out of core: bytes of one cache slot (sized by the largest domain) */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

@@ -80,6 +80,7 @@ class StatsC(C.Structure):
         ("tris_shadow", C.c_int64), ("scene_triangles", C.c_int64), ("scene_bytes", C.c_int64),
         ("h2d_ms", C.c_double), ("learn_pairs", C.c_int64), ("learn_trained", C.c_int64),
         ("learn_ms", C.c_double), ("learn_loss", C.c_double), ("inplace_domains", C.c_int64),
+        ("inplace_bytes", C.c_int64), ("cache_slots", C.c_int64), ("cache_slot_bytes", C.c_int64),
     ]
 
     def asdict(self) -> dict:

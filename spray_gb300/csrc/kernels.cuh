@@ -116,6 +116,11 @@ struct Counters {
   unsigned long long tris_radiance;   // triangles tested by closest-hit traversal
   unsigned long long nodes_shadow;
   unsigned long long tris_shadow;
+  // out of core: work done in domains traced in place from pinned host memory
+  // (resident == 2), whose node, triangle and shading reads cross the host link
+  unsigned long long nodes_inplace;
+  unsigned long long tris_inplace;
+  unsigned long long hits_inplace;    // closest hits whose faces, colours and normals were read there
 };
 
 // Radiance rays of a wave, indexed by sample.

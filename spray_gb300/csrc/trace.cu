@@ -383,6 +383,21 @@ __device__ __forceinline__ uint32_t lanesBelow() {
   return m;
 }
 
+// Adds a warp's in-place counts (nodes, triangles, hits) to the counters.
+__device__ __forceinline__ void warpAddInplace(Counters* ctr, uint32_t n, uint32_t t, uint32_t h, int lane) {
+  unsigned long long sn = n, st = t, sh = h;
+  for (int o = 16; o; o >>= 1) {
+    sn += __shfl_down_sync(0xffffffffu, sn, o);
+    st += __shfl_down_sync(0xffffffffu, st, o);
+    sh += __shfl_down_sync(0xffffffffu, sh, o);
+  }
+  if (lane == 0) {
+    if (sn) atomicAdd(&ctr->nodes_inplace, sn);
+    if (st) atomicAdd(&ctr->tris_inplace, st);
+    if (sh) atomicAdd(&ctr->hits_inplace, sh);
+  }
+}
+
 // Closest hits: warps take 32 consecutive entries at a time, so the lanes of a
 // warp walk coherent rays (consecutive samples of the same domain queue).
 // kPack: culled entries are dropped before the warp's lanes are assigned
@@ -407,6 +422,8 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
   // per-thread counts in 32 bits (entries are 32-bit indices); node and
   // triangle counts go to the global counters before they could wrap
   uint32_t visits = 0, culled = 0, nnodes = 0, ntris = 0;
+  // out of core: nodes, triangles and hits of the entries traced in place
+  uint32_t ipn = 0, ipt = 0, iph = 0;
   // Live entries waiting for a lane, in queue order: a warp takes 32 entries
   // at a time, drops the ones the culling test rejects (kPack) and traces 32
   // live ones together, so that culled entries leave no lane idle.
@@ -481,7 +498,14 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
     TravRay r = makeTravRay(v3(o.x, o.y, o.z), v3(dd.x, dd.y, dd.z));
     uint32_t prim = 0;
     float u = 0.f, v = 0.f;
-    if (traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v, a.ctr, nnodes, ntris)) {
+    const uint32_t n0 = nnodes, t0 = ntris;
+    const bool hit = traverseClosest(a.scene, dom, r, best_key, best_t, prim, u, v, a.ctr, nnodes, ntris);
+    if (!kPack && dom.resident == 2) {
+      ipn += nnodes - n0;
+      ipt += ntris - t0;
+      iph += hit ? 1u : 0u;
+    }
+    if (hit) {
       atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
       const DomArrays g = domArrays(a.scene, dom);
       const uint32_t* f = g.faces + 3 * (size_t)prim;
@@ -502,6 +526,11 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
       atomicAdd(&a.ctr->tris_radiance, (unsigned long long)ntris);
       nnodes = ntris = 0;
     }
+    if (!kPack && ((ipn | ipt) & 0x80000000u)) {
+      atomicAdd(&a.ctr->nodes_inplace, (unsigned long long)ipn);
+      atomicAdd(&a.ctr->tris_inplace, (unsigned long long)ipt);
+      ipn = ipt = 0;
+    }
   }
   unsigned long long sv = visits, sc = culled, sn = nnodes, st = ntris;
   for (int o = 16; o; o >>= 1) {
@@ -516,6 +545,7 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
     if (sn) atomicAdd(&a.ctr->nodes_radiance, sn);
     if (st) atomicAdd(&a.ctr->tris_radiance, st);
   }
+  if (!kPack) warpAddInplace(a.ctr, ipn, ipt, iph, lane);
 }
 
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks) {
@@ -554,6 +584,9 @@ void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nbloc
 // every busy lane advances its walk by one while-while round.  Used for AO
 // frames, whose short bounded rays end early and unevenly; path-traced frames
 // use kTraceOccludedBatch (measured faster there).
+// kOoc: out-of-core batch launch, which also counts the work of domains traced
+// in place from host memory (the in-core launch leaves that out).
+template <bool kOoc>
 __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
@@ -563,13 +596,13 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(Tr
   const uint32_t E = a.nseg > 0 ? spre[a.nseg] : *a.num_entries;
   const int lane = threadIdx.x & 31;
   const uint32_t below = lanesBelow();
-  unsigned long long visits = 0, nnodes = 0, ntris = 0;
+  unsigned long long visits = 0, nnodes = 0, ntris = 0, ipn = 0, ipt = 0;
   int stack[kStack];
   Walk w{};
   TravRay r{};
   float tfar = 0.0f;
   uint32_t ray = 0;
-  bool has = false, exhausted = false;
+  bool has = false, exhausted = false, inplace = false;
   while (true) {
     const unsigned idle = __ballot_sync(0xffffffffu, !has);
     if (idle && !exhausted) {
@@ -590,6 +623,7 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(Tr
           r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
           tfar = dd.w;
           w = startWalk(a.scene, a.scene.domains[d]);
+          inplace = kOoc && a.scene.domains[d].resident == 2;
           has = true;
         }
       }
@@ -599,20 +633,31 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccluded(Tr
       continue;
     }
     bool hit = false;
+    const unsigned long long n0 = kOoc ? nnodes : 0ull, t0 = kOoc ? ntris : 0ull;
     if (has && anyRound(w, stack, r, tfar, &hit, a.ctr, nnodes, ntris)) {
       has = false;
       if (hit) a.sh.occluded[ray] = 1;
+    }
+    if (kOoc && inplace) {
+      ipn += nnodes - n0;
+      ipt += ntris - t0;
     }
   }
   for (int o = 16; o; o >>= 1) {
     visits += __shfl_down_sync(0xffffffffu, visits, o);
     nnodes += __shfl_down_sync(0xffffffffu, nnodes, o);
     ntris += __shfl_down_sync(0xffffffffu, ntris, o);
+    if (kOoc) {
+      ipn += __shfl_down_sync(0xffffffffu, ipn, o);
+      ipt += __shfl_down_sync(0xffffffffu, ipt, o);
+    }
   }
   if (lane == 0) {
     if (visits) atomicAdd(&a.ctr->visits_shadow, visits);
     if (nnodes) atomicAdd(&a.ctr->nodes_shadow, nnodes);
     if (ntris) atomicAdd(&a.ctr->tris_shadow, ntris);
+    if (kOoc && ipn) atomicAdd(&a.ctr->nodes_inplace, ipn);
+    if (kOoc && ipt) atomicAdd(&a.ctr->tris_inplace, ipt);
   }
 }
 
@@ -680,6 +725,7 @@ __device__ bool traverseAny(const SceneDev& sc, const DomainDev& dom, const Trav
 // Occlusion in batches: a warp takes 32 entries at a time, drops those whose
 // shadow ray is already occluded, queues the rest in a per-warp FIFO (queue
 // order kept) and walks 32 of them together, each lane to the end of its walk.
+template <bool kOoc>
 __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccludedBatch(TraceArgs a) {
   extern __shared__ uint32_t skeys[];
   const int D = a.scene.num_domains;
@@ -691,7 +737,7 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccludedBat
   const uint32_t below = lanesBelow();
   __shared__ uint32_t sbuf[8][64];
   uint32_t* buf = sbuf[threadIdx.x >> 5];
-  uint32_t visits = 0, nnodes = 0, ntris = 0;
+  uint32_t visits = 0, nnodes = 0, ntris = 0, ipn = 0, ipt = 0;
   int nbuf = 0;
   bool exhausted = false;
   while (true) {
@@ -734,11 +780,21 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccludedBat
     const float4 hp = a.sh.hitpos[ray / a.slots];
     const float4 dd = a.sh.dir[ray];
     const TravRay r = makeTravRay(v3(hp.x, hp.y, hp.z), v3(dd.x, dd.y, dd.z));
+    const uint32_t n0 = nnodes, t0 = ntris;
     if (traverseAny(a.scene, a.scene.domains[d], r, dd.w, a.ctr, nnodes, ntris)) a.sh.occluded[ray] = 1;
+    if (kOoc && a.scene.domains[d].resident == 2) {
+      ipn += nnodes - n0;
+      ipt += ntris - t0;
+    }
     if ((nnodes | ntris) & 0x80000000u) {
       atomicAdd(&a.ctr->nodes_shadow, (unsigned long long)nnodes);
       atomicAdd(&a.ctr->tris_shadow, (unsigned long long)ntris);
       nnodes = ntris = 0;
+    }
+    if (kOoc && ((ipn | ipt) & 0x80000000u)) {
+      atomicAdd(&a.ctr->nodes_inplace, (unsigned long long)ipn);
+      atomicAdd(&a.ctr->tris_inplace, (unsigned long long)ipt);
+      ipn = ipt = 0;
     }
   }
   unsigned long long sv = visits, sn = nnodes, st = ntris;
@@ -752,12 +808,19 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceOccludedBat
     if (sn) atomicAdd(&a.ctr->nodes_shadow, sn);
     if (st) atomicAdd(&a.ctr->tris_shadow, st);
   }
+  if (kOoc) warpAddInplace(a.ctr, ipn, ipt, 0u, lane);
 }
 
 void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks) {
   size_t smem = (size_t)(a.nkeys + 2 + 2 * a.nseg) * 4;
-  if (a.refill) kTraceOccluded<<<nblocks, 256, smem, s>>>(a);
-  else kTraceOccludedBatch<<<nblocks, 256, smem, s>>>(a);
+  const bool ooc = a.nseg > 0;
+  if (a.refill) {
+    if (ooc) kTraceOccluded<true><<<nblocks, 256, smem, s>>>(a);
+    else kTraceOccluded<false><<<nblocks, 256, smem, s>>>(a);
+  } else {
+    if (ooc) kTraceOccludedBatch<true><<<nblocks, 256, smem, s>>>(a);
+    else kTraceOccludedBatch<false><<<nblocks, 256, smem, s>>>(a);
+  }
 }
 
 // One block per listed domain; the same cull test as kTraceClosest.  The

@@ -2043,6 +2043,10 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->learn_ms = learn_ms;
       st->learn_loss = learn_loss;
       st->inplace_domains = inplace_domains;
+      st->inplace_bytes = (int64_t)(ctr.nodes_inplace * sizeof(BvhNode4) + ctr.tris_inplace * 3 * sizeof(float4) +
+                                    ctr.hits_inplace * (3 * 4 + 3 * 4 + 9 * 4));
+      st->cache_slots = ooc ? cache_capacity : 0;
+      st->cache_slot_bytes = ooc ? (int64_t)cache_slot_bytes : 0;
     }
     return;
   }

@@ -221,11 +221,16 @@ def write_wavelet_grid(out_dir: Path, grid: int = 4, samples: int = 64, colors: 
     return spray
 
 
+def scene_dir(name: str) -> Path:
+    """Directory of a benchmark workload's generated .spray and PLY files."""
+    spec = CONFIGS[name]
+    return SCENE_CACHE / f"{name}_g{spec['grid']}_s{spec['samples']}_{spec['colors']}_{spec['light']}_packed"
+
+
 def benchmark_scene(name: str) -> tuple[Path, dict]:
     """Generates (once) and returns the .spray file of a benchmark workload."""
     spec = CONFIGS[name]
-    d = SCENE_CACHE / f"{name}_g{spec['grid']}_s{spec['samples']}_{spec['colors']}_{spec['light']}_packed"
-    path = write_wavelet_grid(d, spec["grid"], spec["samples"], spec["colors"], spec["light"],
+    path = write_wavelet_grid(scene_dir(name), spec["grid"], spec["samples"], spec["colors"], spec["light"],
                               spec["phase_seed"])
     return path, spec
 

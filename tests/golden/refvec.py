@@ -729,6 +729,20 @@ def product_scene_outputs(spray: Path, ply_dir: Path | None = None) -> dict:
             "colors": np.concatenate([d.colors for d in s.domains])}
 
 
+def oracle_scene_outputs(spray: Path, ply_dir: Path | None = None) -> dict:
+    """The same fields from the oracle's own reader (oracle/scene_io.py)."""
+    from oracle import scene_io
+    s = scene_io.load(spray, ply_dir or spray.parent)
+    return {"world_bounds": np.stack([d.bounds for d in s.domains]),
+            "bsdf_kind": np.array([d.bsdf_type for d in s.domains], np.int32),
+            "light_kind": np.array([l.type for l in s.lights], np.int32),
+            "light_radiance": np.stack([l.radiance for l in s.lights]).astype(np.float32),
+            "nverts": np.array([len(d.vertices) for d in s.domains], np.int64),
+            "vertices": np.concatenate([d.vertices for d in s.domains]),
+            "faces": np.concatenate([d.faces for d in s.domains]),
+            "colors": np.concatenate([d.colors for d in s.domains])}
+
+
 def compare_scene(ref: dict, prod: dict) -> None:
     assert np.array_equal(ref["nverts"], prod["nverts"])
     assert _same(ref["vertices"], prod["vertices"]), \

@@ -44,3 +44,43 @@ def test_clock_summary_reads_only_its_device(bench, tmp_path):
     assert c1["samples"] == 1 and c1["sm_mhz"] == 1200.0 and c1["reasons"] == ["hw_slowdown"]
     assert bench.clock_summary(f, 7) is None
     assert bench.clock_summary(tmp_path / "missing.csv", 0) is None
+
+
+def test_both_arms_describe_the_same_workload(bench, lib_built):
+    # the GPU arm loads the scene with the library, the reference arm with the
+    # oracle's own reader; the `config` objects they print must be identical
+    import spray_gb300 as sg
+    from oracle import scene_io
+    from spray_gb300 import autotune, scenes
+    path = bench.scene_file("c2")
+    t = autotune.load("c2", 0)
+    tuned = dict(t["params"]) if t else None
+    got = []
+    for scene in (sg.Scene.load(path, path.parent), scene_io.load(path, path.parent)):
+        spec, cfg = scenes.workload_config("c2", scene)
+        got.append(bench.bench_config("c2", spec, cfg, scene, "plain", tuned, 1))
+    want = got[0]
+    assert got[1] == want
+    assert want["image"] == [1920, 1080] and want["spp"] == 16 and want["bounces"] == 5
+    assert want["domains"] == 64 and want["triangles"] > 1_000_000
+
+
+def test_reference_arm_runs_without_the_cuda_library(tmp_path):
+    # a child process runs the reference arm on a small frame and lists the
+    # repository libraries it mapped: the oracle's, never libspray_gpu.so
+    import subprocess
+    import sys
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '0', '--ref-scale', '16'];\n"
+            "runpy.run_path(%r, run_name='__main__')\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('MAPPED', sorted({l.split()[-1] for l in maps.splitlines() if l.endswith('.so')}))"
+            % str(ROOT / "bench.py"))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = next(l for l in r.stdout.splitlines() if l.startswith("{"))
+    import json
+    d = json.loads(line)
+    assert d["impl"] == "reference" and d["value"] > 0 and d["cpu_baseline"]["kind"] == "port"
+    mapped = next(l for l in r.stdout.splitlines() if l.startswith("MAPPED"))
+    assert "libspray_gpu.so" not in mapped and "liboracle.so" in mapped
