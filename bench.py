@@ -268,7 +268,7 @@ def north_star_block(args, device: int) -> dict:
     frames = max(args.steps, args.ns_frames)
     ref_img = None
     small = None
-    for name in ("plain", "batched", "learned"):
+    for name in ("plain", "batched", "learned", "nonspec"):
         cfg = dict(cfg0)
         pol = POLICIES[name][0]
         cfg["schedule_policy"] = pol
@@ -293,6 +293,8 @@ def north_star_block(args, device: int) -> dict:
              "mrays_per_s": sum(rays.values()) / (ms * 1e-3) / 1e6,
              "mrays_per_s_by_class": {k: v / (ms * 1e-3) / 1e6 for k, v in rays.items()},
              "visits_per_ray": vis / max(sum(rays.values()), 1),
+             "radiance_visits_per_frame": sum(s["visits_radiance"] for s in sts) / n,
+             "shadow_visits_per_frame": sum(s["visits_shadow"] for s in sts) / n,
              "domain_loads_per_frame": sum(s["domain_loads"] for s in sts) / n,
              "h2d_bytes_per_frame": sum(s["h2d_bytes"] for s in sts) / n,
              "inplace_bytes_per_frame": sum(s["inplace_bytes"] for s in sts) / n,
@@ -303,7 +305,10 @@ def north_star_block(args, device: int) -> dict:
             w0 = next((w for w in warm if w["learn_ms"] > 0), None)
             r["learn"] = {"trained_before_timing": bool(warm[-1]["learn_trained"]),
                           "pairs": warm[-1]["learn_pairs"], "train_ms": w0["learn_ms"] if w0 else None,
-                          "loss": w0["learn_loss"] if w0 else None}
+                          "loss": w0["learn_loss"] if w0 else None,
+                          "held_out_pairs": w0["learn_eval_pairs"] if w0 else 0,
+                          "top1_accuracy": w0["learn_top1"] if w0 else None,
+                          "top1_accuracy_nearest_candidate": w0["learn_top1_nearest"] if w0 else None}
         s0 = sts[-1]
         out["cache"] = {"slots": s0["cache_slots"], "slot_bytes": s0["cache_slot_bytes"],
                         "cache_bytes": s0["cache_slots"] * s0["cache_slot_bytes"],
@@ -314,6 +319,7 @@ def north_star_block(args, device: int) -> dict:
         out["policies"][name] = r
         tr.close()
     p, b, l = (out["policies"][k] for k in ("plain", "batched", "learned"))
+    out["nonspec_vs_plain"] = {"speedup": out["policies"]["nonspec"]["mrays_per_s"] / p["mrays_per_s"]}
     out["learned_vs_plain"] = {"speedup": l["mrays_per_s"] / p["mrays_per_s"],
                                "domain_load_reduction": 1 - l["domain_loads_per_frame"] / max(p["domain_loads_per_frame"], 1e-9),
                                "bytes_moved_reduction": 1 - (l["h2d_bytes_per_frame"] + l["inplace_bytes_per_frame"]) /

@@ -109,6 +109,10 @@ typedef struct spray_gpu_config {
   int32_t bucket_launches;      /* in core with culling: closest-hit launches per depth, 1 = one
                                    launch over the depth buckets in order (fastest), 4 = one per
                                    bucket (visit counts repeat exactly); 0 = 1 (0) */
+  int32_t learn_buckets;        /* policy 3: 1 = also trace each ray's candidates up to the
+                                   predicted one first (in core and inside an out-of-core batch);
+                                   0 = the prediction only orders the out-of-core domain loads,
+                                   every ray keeps its front-to-back order (0) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as
@@ -195,6 +199,10 @@ typedef struct spray_gpu_stats {
                                colours and normals); not included in h2d_bytes */
   int64_t cache_slots;      /* out of core: device domain-cache capacity in domains (0 in core) */
   int64_t cache_slot_bytes; /* out of core: bytes of one cache slot (sized by the largest domain) */
+  int64_t learn_eval_pairs; /* policy 3: held-out pairs (>= 2 candidates) the proposal was scored on */
+  double learn_top1;        /* policy 3: share of them whose predicted candidate holds the hit */
+  double learn_top1_nearest;/* policy 3: share whose hit is in the nearest candidate (the
+                               front-to-back order's guess) */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

@@ -3,8 +3,10 @@
 TEST INFRASTRUCTURE ONLY: the checker of the tensor-core MLP kernels in
 spray_gb300/csrc/mlp.cu.  SpRay has no learned component, so there is no
 reference file to follow; the network, its features and its training rule
-are the ones the CUDA path states: 54 features (normalised origin,
-direction, min/max corners of the first eight candidate boxes), three ReLU
+are the ones the CUDA path states: 54 features (normalised origin and
+direction, then six per candidate of the first eight: distance along the ray
+to the point closest to the box centre, distance from the centre there, box
+half diagonal, their two ratios, presence), three ReLU
 layers of 64, eight logits masked to the present candidates, mean softmax
 cross-entropy over labelled rows, Adam (beta1 0.9, beta2 0.999, eps 1e-8).
 
@@ -67,22 +69,40 @@ def unpack(p: np.ndarray):
 
 
 def features(samples: np.ndarray, boxes: np.ndarray, norm) -> np.ndarray:
-    """(n, 64) float32 features, the same float32 operations as the kernel."""
+    """(n, 64) float32 features, the same float32 operations as the kernel:
+    normalised origin, direction, and per candidate (zeros when absent) the
+    distance along the ray to the point closest to the box centre, the ray's
+    distance from the centre there, the box half diagonal, their two ratios
+    (miss / r at most 4, along / r within [-4, 4]) and a presence flag."""
     n = len(samples)
     c = np.asarray(norm[:3], np.float32)
     s = np.float32(norm[3])
     f = np.zeros((n, K), np.float32)
-    f[:, 0:3] = (samples["org"] - c) * s
-    f[:, 3:6] = samples["dir"]
+    on = ((samples["org"] - c) * s).astype(np.float32)
+    d = np.asarray(samples["dir"], np.float32)
+    f[:, 0:3] = on
+    f[:, 3:6] = d
     nc = np.minimum(samples["ncand"], CAND)
     bx = np.asarray(boxes, np.float32).reshape(-1, 6)
+    half = np.float32(0.5)
     for j in range(CAND):
-        on = j < nc
-        b = bx[samples["cand"][:, j].astype(np.int64)]
-        lo = (b[:, 0:3] - c) * s
-        hi = (b[:, 3:6] - c) * s
-        f[:, 6 + 6 * j:9 + 6 * j] = np.where(on[:, None], lo, 0.0)
-        f[:, 9 + 6 * j:12 + 6 * j] = np.where(on[:, None], hi, 0.0)
+        present = j < nc
+        b = bx[np.where(present, samples["cand"][:, j].astype(np.int64), 0)]
+        lo = ((b[:, 0:3] - c) * s).astype(np.float32)
+        hi = ((b[:, 3:6] - c) * s).astype(np.float32)
+        pc = ((lo + hi) * half - on).astype(np.float32)
+        hh = ((hi - lo) * half).astype(np.float32)
+        along = (pc[:, 0] * d[:, 0] + pc[:, 1] * d[:, 1]) + pc[:, 2] * d[:, 2]
+        pp = (pc[:, 0] * pc[:, 0] + pc[:, 1] * pc[:, 1]) + pc[:, 2] * pc[:, 2]
+        miss = np.sqrt(np.maximum(pp - along * along, np.float32(0.0))).astype(np.float32)
+        r = np.sqrt((hh[:, 0] * hh[:, 0] + hh[:, 1] * hh[:, 1]) + hh[:, 2] * hh[:, 2]).astype(np.float32)
+        with np.errstate(divide="ignore"):
+            ir = np.where(r > 0, np.float32(1.0) / np.where(r > 0, r, np.float32(1.0)), np.float32(0.0))
+        ir = ir.astype(np.float32)
+        cols = [along, miss, r, np.minimum(miss * ir, np.float32(4.0)),
+                np.minimum(np.maximum(along * ir, np.float32(-4.0)), np.float32(4.0)), np.ones(n, np.float32)]
+        for k, v in enumerate(cols):
+            f[:, 6 + 6 * j + k] = np.where(present, v, np.float32(0.0))
     return f
 
 

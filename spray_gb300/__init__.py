@@ -43,7 +43,7 @@ class ConfigC(C.Structure):
         ("learn_epochs", C.c_int32), ("learn_lr", C.c_float), ("learn_seed", C.c_int32),
         ("learn_frames", C.c_int32), ("graphs", C.c_int32), ("ooc_inplace", C.c_int32),
         ("trace_blocks_per_sm", C.c_int32), ("sched_chunks_per_warp", C.c_int32),
-        ("bucket_launches", C.c_int32),
+        ("bucket_launches", C.c_int32), ("learn_buckets", C.c_int32),
     ]
 
 
@@ -81,6 +81,7 @@ class StatsC(C.Structure):
         ("h2d_ms", C.c_double), ("learn_pairs", C.c_int64), ("learn_trained", C.c_int64),
         ("learn_ms", C.c_double), ("learn_loss", C.c_double), ("inplace_domains", C.c_int64),
         ("inplace_bytes", C.c_int64), ("cache_slots", C.c_int64), ("cache_slot_bytes", C.c_int64),
+        ("learn_eval_pairs", C.c_int64), ("learn_top1", C.c_double), ("learn_top1_nearest", C.c_double),
     ]
 
     def asdict(self) -> dict:

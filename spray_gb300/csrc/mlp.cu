@@ -175,24 +175,49 @@ __device__ void stageWeights(uint8_t* op, const float* w, int out, int in, bool 
   }
 }
 
-// The 64 features of a ray: normalised origin, direction, then min and max
-// corners of each candidate box (zero for absent candidates), zero padding.
+// Features of a ray and its candidates, in the scene box normalised to
+// [-1, 1]: the origin and direction, then per candidate j (zeros when absent)
+//   along  distance along the ray to the point closest to the box centre
+//   miss   distance of the ray from the box centre there
+//   r      half diagonal of the box
+//   miss / r (at most 4), along / r (within [-4, 4]), 1 (present)
+// Whether a ray meets a domain's surface depends mostly on how close it
+// passes the domain's centre relative to its size, which a small ReLU network
+// cannot form from box corners; these are the same inputs (origin,
+// direction, boxes) put in that form.  Every operation rounds once
+// (-fmad=false; IEEE division and square root), as the numpy restatement does.
 __device__ __forceinline__ void features(const float* o, const float* d, const uint16_t* cand, int ncand,
                                          const float* boxes, const Norm& nm, float* f) {
+  float on[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    f[c] = (o[c] - nm.centre[c]) * nm.scale;
+    on[c] = (o[c] - nm.centre[c]) * nm.scale;
+    f[c] = on[c];
     f[3 + c] = d[c];
   }
 #pragma unroll
   for (int j = 0; j < kCand; ++j) {
-    const bool on = j < ncand;
-    const float* b = boxes + 6 * (on ? cand[j] : 0);
+    const bool present = j < ncand;
+    const float* b = boxes + 6 * (present ? cand[j] : 0);
+    float pc[3], hh[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      f[6 + 6 * j + c] = on ? (b[c] - nm.centre[c]) * nm.scale : 0.0f;
-      f[9 + 6 * j + c] = on ? (b[3 + c] - nm.centre[c]) * nm.scale : 0.0f;
+      const float lo = (b[c] - nm.centre[c]) * nm.scale;
+      const float hi = (b[3 + c] - nm.centre[c]) * nm.scale;
+      pc[c] = (lo + hi) * 0.5f - on[c];
+      hh[c] = (hi - lo) * 0.5f;
     }
+    const float along = (pc[0] * d[0] + pc[1] * d[1]) + pc[2] * d[2];
+    const float pp = (pc[0] * pc[0] + pc[1] * pc[1]) + pc[2] * pc[2];
+    const float miss = sqrtf(fmaxf(pp - along * along, 0.0f));
+    const float r = sqrtf((hh[0] * hh[0] + hh[1] * hh[1]) + hh[2] * hh[2]);
+    const float ir = r > 0.0f ? 1.0f / r : 0.0f;
+    f[6 + 6 * j] = present ? along : 0.0f;
+    f[7 + 6 * j] = present ? miss : 0.0f;
+    f[8 + 6 * j] = present ? r : 0.0f;
+    f[9 + 6 * j] = present ? fminf(miss * ir, 4.0f) : 0.0f;
+    f[10 + 6 * j] = present ? fminf(fmaxf(along * ir, -4.0f), 4.0f) : 0.0f;
+    f[11 + 6 * j] = present ? 1.0f : 0.0f;
   }
 #pragma unroll
   for (int k = kIn; k < kK; ++k) f[k] = 0.0f;
@@ -214,6 +239,28 @@ struct SampleRows {
 #pragma unroll
     for (int c = 0; c < kCand; ++c) logits[i * kCand + c] = lg[c];
     pred[i] = best;
+  }
+};
+
+// Held-out evaluation: counts[0] += labelled rows with at least two
+// candidates, counts[1] += those whose argmax is the label, counts[2] +=
+// those whose label is the nearest candidate (position 0).
+struct EvalRows {
+  const Sample* s;
+  int64_t n;
+  unsigned long long* counts;
+  __device__ int64_t rows() const { return n; }
+  __device__ int load(int64_t i, const Net& net, float* f) const {
+    const Sample q = s[i];
+    features(q.org, q.dir, q.cand, q.ncand, net.boxes, net.norm, f);
+    return q.ncand;
+  }
+  __device__ void store(int64_t i, const float*, int ncand, int best) const {
+    const int label = s[i].label;
+    if (label < 0 || ncand < 2) return;
+    atomicAdd(&counts[0], 1ull);
+    if (best == label) atomicAdd(&counts[1], 1ull);
+    if (label == 0) atomicAdd(&counts[2], 1ull);
   }
 };
 
@@ -653,6 +700,13 @@ void launchPredictSamples(cudaStream_t s, const Net& net, const Sample* samples,
   SampleRows r{samples, n, logits, pred};
   cudaFuncSetAttribute(kForward<SampleRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
   kForward<SampleRows><<<nblocks, kTile, kFwdSmem, s>>>(net, r);
+}
+
+void launchEvaluate(cudaStream_t s, const Net& net, const Sample* samples, int64_t n, unsigned long long* counts,
+                    int nblocks) {
+  EvalRows r{samples, n, counts};
+  cudaFuncSetAttribute(kForward<EvalRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
+  kForward<EvalRows><<<nblocks, kTile, kFwdSmem, s>>>(net, r);
 }
 
 void launchGrad(cudaStream_t s, const Net& net, const Sample* batch, int64_t n, float inv_count, float* partial,

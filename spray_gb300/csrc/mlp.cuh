@@ -75,6 +75,12 @@ void launchPredictArena(cudaStream_t s, const Net& net, const ArenaSource& src, 
 // -inf) and the argmax.
 void launchPredictSamples(cudaStream_t s, const Net& net, const Sample* samples, int64_t n,
                           float* logits, int32_t* pred, int nblocks);
+// Top-1 accuracy on held-out samples: counts[3] (zeroed by the caller) +=
+// labelled samples with at least two candidates, those whose argmax is the
+// label, and those whose label is the nearest candidate (the accuracy of
+// always predicting position 0, i.e. the front-to-back order).
+void launchEvaluate(cudaStream_t s, const Net& net, const Sample* samples, int64_t n, unsigned long long* counts,
+                    int nblocks);
 // Gradient of the mean cross-entropy over the labelled rows of a batch:
 // every CTA writes a partial [kPartial] (gradient, loss sum, labelled rows).
 // `inv_count` scales the loss gradient (1 / labelled rows of the whole batch).

@@ -1173,7 +1173,7 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
     record(s0);
     schedule(false, order_by_depth, d_alive_count, d_alive_list, S, b == 0, false,
-             learned() && proposal_trained && order_by_depth && !capture);
+             learned() && proposal_trained && order_by_depth && !capture && cfg.learn_buckets);
     record(s1);
     sched_events.push_back({s0, s1});
     if (capture) {
@@ -1551,10 +1551,13 @@ void Tracer::traceWaveBatched(const Wave& w) {
     cudaEvent_t s0 = poolEvent(), s1 = poolEvent();
     record(s0);
     const bool pred = learned() && proposal_trained;
-    schedule(false, order_by_depth, d_alive_count, d_alive_list, S, primary, false, pred && order_by_depth);
+    // with learn_buckets the schedule already ran the prediction (bucket
+    // boundaries); otherwise the prediction only orders the domain loads
+    const bool buckets = pred && order_by_depth && cfg.learn_buckets;
+    schedule(false, order_by_depth, d_alive_count, d_alive_list, S, primary, false, buckets);
     record(s1);
     sched_events.push_back({s0, s1});
-    if (pred) predictDomainCounts(!order_by_depth);
+    if (pred) predictDomainCounts(!buckets);
   };
   scheduleRadiance(true);
   oocPass(true, false, S, rb);
@@ -1608,6 +1611,7 @@ void Tracer::freeProposal() {
   devFree(d_pairs_filled);
   devFree(d_predcount);
   devFree(d_mlp_err);
+  devFree(d_mlp_eval);
   proposal_trained = false;
   frames_collected = 0;
   adam_step = 0;
@@ -1660,6 +1664,7 @@ void Tracer::setupProposal() {
   devAlloc(&d_predcount, D);
   devAlloc(&d_mlp_err, 1);
   CK(cudaMemset(d_mlp_err, 0, sizeof(int)));
+  devAlloc(&d_mlp_eval, 3);
 }
 
 mlp::ArenaSource Tracer::arenaSource() const {
@@ -1696,6 +1701,8 @@ void Tracer::collectPairs() {
 // is already in d_pred when the schedule used it).
 void Tracer::predictDomainCounts(bool run_predict) {
   CK(cudaMemsetAsync(d_predcount, 0, (size_t)D * 4, stream));
+  // (atomics folded into the inference epilogue measured slower: they stall
+  // the tensor-core tile loop more than this pass costs)
   if (run_predict) {
     mlp::launchPredictArena(stream, proposalNet(), arenaSource(), d_pred, num_sms * 5);
     launches += 1;
@@ -1708,7 +1715,11 @@ void Tracer::predictDomainCounts(bool run_predict) {
 // learn_epochs passes of Adam (batch learn_batch) over the collected pairs.
 void Tracer::trainProposal() {
   namespace ml = mlp;
-  const int64_t n = std::min<int64_t>(pairs_filled, (int64_t)pairs_cap);
+  const int64_t all = std::min<int64_t>(pairs_filled, (int64_t)pairs_cap);
+  // the last sixteenth of the pairs (at most 2^18) is held out to score the
+  // trained proposal; the rest trains it
+  const int64_t held = all >= 64 ? std::min<int64_t>(all / 16, 1 << 18) : 0;
+  const int64_t n = all - held;
   cudaEvent_t e0 = poolEvent(), e1 = poolEvent();
   CK(cudaEventRecord(e0, stream));
   float* params = d_mlp;
@@ -1728,11 +1739,20 @@ void Tracer::trainProposal() {
     }
   }
   CK(cudaEventRecord(e1, stream));
+  unsigned long long ev[3] = {0ull, 0ull, 0ull};
+  if (held > 0) {
+    CK(cudaMemsetAsync(d_mlp_eval, 0, 3 * sizeof(unsigned long long), stream));
+    ml::launchEvaluate(stream, proposalNet(), d_pairs + n, held, d_mlp_eval, num_sms * 5);
+    CK(cudaMemcpyAsync(ev, d_mlp_eval, sizeof(ev), cudaMemcpyDeviceToHost, stream));
+  }
   CK(cudaStreamSynchronize(stream));
   CK(cudaGetLastError());
   int err = 0;
   CK(cudaMemcpy(&err, d_mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) throw std::runtime_error("a tensor-core wait of the learned proposal gave up");
+  learn_eval_pairs = (int64_t)ev[0];
+  learn_top1 = ev[0] ? (double)ev[1] / (double)ev[0] : 0.0;
+  learn_top1_nearest = ev[0] ? (double)ev[2] / (double)ev[0] : 0.0;
   float tail[2] = {0.f, 0.f};
   if (n > 0) CK(cudaMemcpy(tail, grad + ml::kParams, sizeof(tail), cudaMemcpyDeviceToHost));
   learn_loss = tail[1] > 0.f ? tail[0] / tail[1] : 0.0;
@@ -2047,6 +2067,9 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
                                     ctr.hits_inplace * (3 * 4 + 3 * 4 + 9 * 4));
       st->cache_slots = ooc ? cache_capacity : 0;
       st->cache_slot_bytes = ooc ? (int64_t)cache_slot_bytes : 0;
+      st->learn_eval_pairs = learn_eval_pairs;
+      st->learn_top1 = learn_top1;
+      st->learn_top1_nearest = learn_top1_nearest;
     }
     return;
   }

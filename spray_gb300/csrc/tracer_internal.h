@@ -260,13 +260,15 @@ class Tracer {
   uint32_t* d_lnsel = nullptr;
   uint32_t* d_predcount = nullptr;
   int* d_mlp_err = nullptr;
+  unsigned long long* d_mlp_eval = nullptr;  // held-out evaluation counters
   mlp::Norm mlp_norm{};
   uint64_t pairs_cap = 0;
   bool proposal_trained = false;
   bool use_pred_order = false;  // this pass orders domains by predicted hits
   int frames_collected = 0;
   int adam_step = 0;
-  double learn_ms = 0.0, learn_loss = 0.0;
+  double learn_ms = 0.0, learn_loss = 0.0, learn_top1 = 0.0, learn_top1_nearest = 0.0;
+  int64_t learn_eval_pairs = 0;
   int64_t pairs_filled = 0;
   uint2* d_sentries = nullptr;     // batched out of core: shadow queues beside the radiance ones
   uint32_t* d_skey_start = nullptr;
