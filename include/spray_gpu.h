@@ -203,6 +203,7 @@ typedef struct spray_gpu_stats {
   double learn_top1;        /* policy 3: share of them whose predicted candidate holds the hit */
   double learn_top1_nearest;/* policy 3: share whose hit is in the nearest candidate (the
                                front-to-back order's guess) */
+  int64_t exchange_bytes;   /* domain-parallel: bytes this rank passed to the reductions */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */
@@ -340,6 +341,46 @@ typedef struct spray_gpu_dbg_score {
 int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int64_t* count);
 int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void* out,
                          int64_t capacity);
+
+/* ---------------------------------------------------------------- domain-parallel
+ * SpRay's in-situ tracer (insitu::MultiThreadTracer,
+ * src/insitu/insitu_multithread_tracer.inl:313-442) pins each domain to one
+ * MPI rank (InsituPartition::partition, src/render/data_partition.h:60-137:
+ * Morton order of the domain centres, ndomains / ranks consecutive domains
+ * per rank) and composites every bounce's closest-hit distances with an MPI
+ * MIN all-reduce and its occlusion bits with a BOR all-reduce
+ * (VBuf::compositeTbuf / compositeObuf, src/insitu/insitu_vbuf.h:109-129).
+ * With spray_gpu_set_insitu each rank's tracer holds and traverses only the
+ * domains the same partition gives it; every rank keeps the whole ray state
+ * (camera rays, shading, compaction and retirement run on each), and per
+ * depth the tracer calls, in this order, on every rank:
+ *   min_u64  over every sample's packed hit key (t bits << 32 | triangle):
+ *            element-wise minimum of unsigned 64-bit values across ranks;
+ *   max_u8   over the resolved hit records (16 bytes per sample; the rank
+ *            holding the winning hit wrote it, the others zeros);
+ *   max_u8   over the shadow rays' occlusion flags (0 or 1).
+ * Each call reduces `n` elements in place and returns 0 (nonzero aborts the
+ * frame with SPRAY_GPU_ECUDA).  With host_buffers = 1 the tracer copies the
+ * data to pinned host memory first and passes host pointers (MPI, gloo; the
+ * stream argument is NULL); with 0 it passes device pointers and its stream,
+ * on which the call must order its work (NCCL).  Every rank ends the frame
+ * with the single-rank image.  Call before spray_gpu_set_scene (the partition
+ * needs the domain boxes, and only owned domains are built); the scene must
+ * fit each rank's device (no out-of-core cache) and schedule_policy must be 0
+ * or 1.  num_ranks = 1 switches it off. */
+typedef struct spray_gpu_reduce_ops {
+  void* user;
+  int32_t host_buffers;
+  int (*min_u64)(void* user, uint64_t* data, int64_t n, void* stream);
+  int (*max_u8)(void* user, uint8_t* data, int64_t n, void* stream);
+} spray_gpu_reduce_ops;
+
+int spray_gpu_set_insitu(spray_gpu_tracer* t, int32_t num_ranks, int32_t rank,
+                         const spray_gpu_reduce_ops* ops);
+/* The partition itself (host only, no device needed): rank of each of the
+ * num_domains domains given their world boxes (6 floats each). */
+int spray_gpu_insitu_partition(const float* domain_bounds, int32_t num_domains, int32_t num_ranks,
+                               int32_t* owner);
 
 /* ---------------------------------------------------------------- no allocation
  * No counterpart in the reference.  The scheduler (slab test of every ray

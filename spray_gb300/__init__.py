@@ -82,10 +82,22 @@ class StatsC(C.Structure):
         ("learn_ms", C.c_double), ("learn_loss", C.c_double), ("inplace_domains", C.c_int64),
         ("inplace_bytes", C.c_int64), ("cache_slots", C.c_int64), ("cache_slot_bytes", C.c_int64),
         ("learn_eval_pairs", C.c_int64), ("learn_top1", C.c_double), ("learn_top1_nearest", C.c_double),
+        ("exchange_bytes", C.c_int64),
     ]
 
     def asdict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# spray_gpu_reduce_ops: element-wise reductions across the ranks of a
+# domain-parallel tracer (pointer, count, stream) -> 0 on success
+REDUCE_U64 = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint64), C.c_int64, C.c_void_p)
+REDUCE_U8 = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_uint8), C.c_int64, C.c_void_p)
+
+
+class ReduceOpsC(C.Structure):
+    _fields_ = [("user", C.c_void_p), ("host_buffers", C.c_int32), ("min_u64", REDUCE_U64),
+                ("max_u8", REDUCE_U8)]
 
 
 DBG_DTYPES = {
@@ -110,7 +122,7 @@ EXPORTED_SYMBOLS = [
     "spray_gpu_set_scene", "spray_gpu_set_camera", "spray_gpu_trace", "spray_gpu_trace_device",
     "spray_scene_load", "spray_scene_free", "spray_scene_counts", "spray_scene_domains",
     "spray_scene_lights", "spray_write_ply", "spray_generate_wavelet", "spray_gpu_debug_count",
-    "spray_gpu_debug_copy", "spray_gpu_schedule_static",
+    "spray_gpu_debug_copy", "spray_gpu_schedule_static", "spray_gpu_set_insitu", "spray_gpu_insitu_partition",
 ]
 
 
@@ -146,6 +158,8 @@ def lib() -> C.CDLL:
         L.spray_gpu_trace_views.argtypes = [P, C.POINTER(ViewC), C.c_int32, P, C.POINTER(StatsC)]
         L.spray_gpu_trace_views_device.argtypes = [P, C.POINTER(ViewC), C.c_int32, P, C.POINTER(StatsC)]
         L.spray_scene_prepare.argtypes = [C.POINTER(DomainC), C.c_int32, C.c_char_p]
+        L.spray_gpu_set_insitu.argtypes = [P, C.c_int32, C.c_int32, C.POINTER(ReduceOpsC)]
+        L.spray_gpu_insitu_partition.argtypes = [P, C.c_int32, C.c_int32, P]
         L.spray_gpu_set_scene_prepared.argtypes = [P, C.c_char_p, C.c_int32, C.POINTER(LightC), C.c_int32]
         F4 = C.POINTER(C.c_float)
         L.spray_mlp_param_count.restype = C.c_int32
@@ -310,6 +324,36 @@ class Tracer:
         _check(lib().spray_gpu_set_scene_prepared(self._h, str(directory).encode(), num_domains, lts,
                                                   len(lights)))
 
+    def set_insitu(self, num_ranks: int, rank: int, min_u64=None, max_u8=None, host_buffers: bool = True) -> None:
+        """Domain-parallel tracing (spray_gpu_set_insitu), before set_scene.
+
+        min_u64(array) and max_u8(array) reduce a numpy array in place across
+        all ranks (element-wise unsigned minimum of uint64, maximum of uint8)
+        when host_buffers is true; otherwise they receive (device pointer, n,
+        stream) and must order their work on that stream."""
+        ops = ReduceOpsC()
+        ops.host_buffers = 1 if host_buffers else 0
+        if num_ranks > 1:
+            def wrap(fn, dtype):
+                def call(user, ptr, n, stream):
+                    try:
+                        if host_buffers:
+                            addr = C.cast(ptr, C.c_void_p).value
+                            buf = (C.c_char * (n * np.dtype(dtype).itemsize)).from_address(addr)
+                            fn(np.frombuffer(buf, dtype=dtype, count=n))
+                        else:
+                            fn(C.cast(ptr, C.c_void_p).value, n, stream)
+                        return 0
+                    except Exception:  # no exception may cross the C boundary
+                        import traceback
+                        traceback.print_exc()
+                        return 1
+                return call
+            ops.min_u64 = REDUCE_U64(wrap(min_u64, np.uint64))
+            ops.max_u8 = REDUCE_U8(wrap(max_u8, np.uint8))
+        self._reduce_ops = ops  # the callbacks must outlive the tracer's use of them
+        _check(lib().spray_gpu_set_insitu(self._h, num_ranks, rank, C.byref(ops)))
+
     def set_camera(self, pos, lookat, up=(0, 1, 0), vfov=None) -> None:
         f3 = lambda x: (C.c_float * 3)(*[float(v) for v in x])
         fov = self.config["fov"] if vfov is None else vfov
@@ -390,6 +434,15 @@ def schedule_static(domain_bounds_ptr: int, num_domains: int, org_ptr: int, dir_
                                            C.c_void_p(domain_start_ptr), C.byref(n),
                                            C.c_void_p(stream) if stream else None))
     return n.value
+
+
+def insitu_partition(bounds, num_ranks: int) -> np.ndarray:
+    """Rank of each domain under SpRay's in-situ partition (host only)."""
+    b = np.ascontiguousarray(bounds, np.float32).reshape(-1, 6)
+    out = np.zeros(len(b), np.int32)
+    _check(lib().spray_gpu_insitu_partition(b.ctypes.data_as(C.c_void_p), len(b), num_ranks,
+                                            out.ctypes.data_as(C.c_void_p)))
+    return out
 
 
 def prepare_scene(scene: "Scene", directory) -> None:

@@ -32,18 +32,6 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-struct CudaError : std::runtime_error {
-  using std::runtime_error::runtime_error;
-};
-
-#define CK(x)                                                                               \
-  do {                                                                                      \
-    cudaError_t e_ = (x);                                                                   \
-    if (e_ != cudaSuccess)                                                                  \
-      throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_) + " at " + __FILE__ + \
-                      ":" + std::to_string(__LINE__));                                      \
-  } while (0)
-
 template <class T>
 static void devAlloc(T** p, size_t n) {
   *p = nullptr;
@@ -360,6 +348,7 @@ Tracer::~Tracer() {
   if (ev_stop) cudaEventDestroy(ev_stop);
   if (stream) cudaStreamDestroy(stream);
   if (cstream) cudaStreamDestroy(cstream);
+  if (h_reduce) cudaFreeHost(h_reduce);
 }
 
 void Tracer::freeScene() {
@@ -490,10 +479,28 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   if (slots() > kMaxSlots) throw std::invalid_argument("too many shadow rays per hit (max 64)");
   std::vector<DomainPack> packs(nd);
   std::vector<std::string> errors(nd);
+  if (situ()) {
+    std::vector<float> b(6 * (size_t)nd);
+    for (int d = 0; d < nd; ++d)
+      for (int c = 0; c < 6; ++c) b[6 * d + c] = doms[d].world_bounds[c];
+    owner = insituPartition(b.data(), nd, insitu_ranks);
+  } else {
+    owner.assign(nd, 0);
+  }
 #pragma omp parallel for schedule(dynamic, 1)
   for (int d = 0; d < nd; ++d) {
     try {
-      buildPack(doms[d], d, packs[d]);
+      if (owner[d] == insitu_rank) {
+        buildPack(doms[d], d, packs[d]);
+      } else {
+        // another rank's domain: its box, material and triangle count only
+        DomainPack& p = packs[d];
+        if (doms[d].num_faces <= 0) throw std::invalid_argument("domain " + std::to_string(d) + " has no geometry");
+        for (int c = 0; c < 6; ++c) p.bounds[c] = doms[d].world_bounds[c];
+        p.bsdf = doms[d].bsdf_type;
+        for (int c = 0; c < 3; ++c) p.bsdf_p[c] = doms[d].bsdf_params[c];
+        p.prim_count = doms[d].num_faces;
+      }
     } catch (const std::exception& e) {
       errors[d] = e.what();
     }
@@ -521,6 +528,26 @@ void Tracer::setScenePrepared(const std::string& dir, int nd, const spray_gpu_li
   }
   for (int d = 0; d < nd; ++d)
     if (!errors[d].empty()) throw IoError(errors[d]);
+  if (situ()) {
+    std::vector<float> b(6 * (size_t)nd);
+    for (int d = 0; d < nd; ++d)
+      for (int c = 0; c < 6; ++c) b[6 * d + c] = packs[d].bounds[c];
+    owner = insituPartition(b.data(), nd, insitu_ranks);
+    for (int d = 0; d < nd; ++d)
+      if (owner[d] != insitu_rank) {
+        DomainPack& p = packs[d];
+        p.prim_count = p.nf;
+        p.nv = p.nf = 0;
+        p.nodes.clear();
+        p.tris.clear();
+        p.faces.clear();
+        p.colors.clear();
+        p.normals.clear();
+        p.bvh_depth = 0;
+      }
+  } else {
+    owner.assign(nd, 0);
+  }
   installScene(packs, ls, nl);
 }
 
@@ -554,7 +581,7 @@ void Tracer::installScene(std::vector<DomainPack>& packs, const spray_gpu_light*
     nn += packs[d].nodes.size();
     nt += (size_t)packs[d].nf;
     nvv += (size_t)packs[d].nv;
-    gp += (uint64_t)packs[d].nf;
+    gp += (uint64_t)(packs[d].prim_count >= 0 ? packs[d].prim_count : packs[d].nf);
     max_bvh_depth = std::max(max_bvh_depth, packs[d].bvh_depth);
     if (gp >= 0xffffffffull || nt >= (1ull << 31) || nn >= (1ull << 31))
       throw std::invalid_argument("scene too large for 32-bit triangle numbering");
@@ -574,6 +601,7 @@ void Tracer::installScene(std::vector<DomainPack>& packs, const spray_gpu_light*
   if (cfg.cache_bytes > 0) capacity = (int)std::max<int64_t>(1, std::min<int64_t>(nd, cfg.cache_bytes / (int64_t)slot_bytes));
   else if (cfg.cache_size > 0 && cfg.cache_size < nd) capacity = cfg.cache_size;
   ooc = capacity < nd;
+  if (ooc && situ()) throw std::invalid_argument("domain-parallel tracing keeps each rank's domains in core");
   if (ooc) {
     setupOutOfCore(packs, capacity, max_nodes, max_tris, max_verts, slot_bytes);
     packs.clear();
@@ -628,6 +656,7 @@ void Tracer::installScene(std::vector<DomainPack>& packs, const spray_gpu_light*
   }
   devAlloc(&d_lights, lf.size());
   CK(cudaMemcpy(d_lights, lf.data(), lf.size() * 4, cudaMemcpyHostToDevice));
+  if (situ()) devAlloc(&d_segs, 2 * (size_t)D + 2);  // one segment table over the owned domains
   freeBuffers();  // sizes depend on the domain count and slots
   if (learned()) setupProposal();
   has_scene = true;
@@ -1162,7 +1191,8 @@ void Tracer::traceWave(const Wave& w, bool capture) {
   // non-speculative (policy 4): one pass per list position, so radiance
   // queues are keyed by depth bucket out of core as well
   const bool nonspec = ooc && cfg.schedule_policy == 4;
-  const int order_by_depth = (cfg.cull && (!ooc || nonspec)) ? 1 : 0;
+  // domain-parallel: radiance keys are domains, each rank traces its own in one launch
+  const int order_by_depth = (cfg.cull && (!ooc || nonspec) && !situ()) ? 1 : 0;
   const int nblk = num_sms * kStreamBlocksPerSm;
   for (int b = 0; b < nb_total; ++b) {
     if (capture) captureRays(b);
@@ -1193,6 +1223,12 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       // pending rays first
       const int rb = order_by_depth ? kDepthBuckets : 1;
       for (int k = 0; k < rb; ++k) oocPass(true, false, S, rb, k, 1, true);
+    } else if (situ()) {
+      // this rank's domains, then the t-buffer composite: every rank's
+      // closest hit per ray, the minimum of the packed keys
+      traceOwned(false, S);
+      reduceCall(true, d_ray_key, w.samples, sizeof(uint64_t));
+      CK(cudaMemsetAsync(d_hit_ns, 0, (size_t)w.samples * sizeof(float4), stream));
     } else if (ooc) {
       order = scoreOrder();
       if (cfg.schedule_policy == 1) {
@@ -1220,6 +1256,9 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     launchResolve(stream, ta, d_hit_ns, nblk);
     launches += 1;
+    // the winning entry's rank published the hit's normal and colour, the
+    // other ranks left zeros: the bytewise maximum is the winner's record
+    if (situ()) reduceCall(false, d_hit_ns, w.samples * (int64_t)sizeof(float4), 1);
     if (learned() && !proposal_trained) collectPairs();
     if (capture) captureHits(b);
     // shade
@@ -1237,11 +1276,15 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     // In core the shadow entries are sorted by list position (the ray's own
     // domain first): the occlusion walk takes them in that order, so an
     // occluder found near the ray culls its entries in farther domains.
-    const int sorder = (!ooc && !nonspec) ? 1 : 0;
+    const int sorder = (!ooc && !nonspec && !situ()) ? 1 : 0;
     schedule(true, sorder, d_shadow_count, d_shadow_list, S, false, nonspec);
     if (capture) captureQueues(SPRAY_DBG_SQUEUES, b, sorder);
     if (nonspec) {
       oocPass(false, true, S, 1, 0, 0, true);
+    } else if (situ()) {
+      // occlusion in this rank's domains, then the occlusion composite
+      traceOwned(true, S);
+      reduceCall(false, sh.occluded, w.samples * (int64_t)S, 1);
     } else if (ooc && cfg.schedule_policy == 0) {
       traceOutOfCore(true, order, S);
     } else if (ooc) {
@@ -1961,6 +2004,7 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     d2h_bytes = 0;
     domain_loads = 0;
     inplace_domains = 0;
+    reduce_bytes = 0;
     ev_used = 0;
     sched_events.clear();
     trace_events.clear();
@@ -1974,7 +2018,7 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     CK(cudaMemcpyAsync(d_tiles, wave_tiles.data(), wave_tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice,
                        stream));
     h2d_bytes += hviews.size() * sizeof(ViewDev) + wave_tiles.size() * sizeof(TileDev);
-    const bool graphed = cfg.graphs && !ooc && !cfg.debug_capture && !learned();
+    const bool graphed = cfg.graphs && !ooc && !cfg.debug_capture && !learned() && !situ();
     if (graphed) {
       if (!graph_exec || graph_gen != buf_gen) captureFrame();
       CK(cudaGraphLaunch(graph_exec, stream));
@@ -2070,6 +2114,7 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->learn_eval_pairs = learn_eval_pairs;
       st->learn_top1 = learn_top1;
       st->learn_top1_nearest = learn_top1_nearest;
+      st->exchange_bytes = reduce_bytes;
     }
     return;
   }
@@ -2342,6 +2387,25 @@ int spray_gpu_set_camera(spray_gpu_tracer* t, const float pos[3], const float lo
   if (!t || !pos || !lookat || !up) return fail(SPRAY_GPU_EINVAL, "null argument");
   API_GUARD({
     t->impl->setCamera(pos, lookat, up, vfov);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_set_insitu(spray_gpu_tracer* t, int32_t num_ranks, int32_t rank,
+                         const spray_gpu_reduce_ops* ops) {
+  if (!t) return fail(SPRAY_GPU_EINVAL, "null tracer");
+  API_GUARD({
+    t->impl->setInsitu(num_ranks, rank, ops);
+    return SPRAY_GPU_OK;
+  })
+}
+
+int spray_gpu_insitu_partition(const float* domain_bounds, int32_t num_domains, int32_t num_ranks,
+                               int32_t* owner) {
+  if (!domain_bounds || !owner) return fail(SPRAY_GPU_EINVAL, "null argument");
+  API_GUARD({
+    std::vector<int> o = spray::insituPartition(domain_bounds, num_domains, num_ranks);
+    for (int d = 0; d < num_domains; ++d) owner[d] = o[d];
     return SPRAY_GPU_OK;
   })
 }

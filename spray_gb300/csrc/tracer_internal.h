@@ -25,8 +25,21 @@ struct OverflowError : std::runtime_error {
 struct IoError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define CK(x)                                                                               \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_) + " at " + __FILE__ + \
+                      ":" + std::to_string(__LINE__));                                      \
+  } while (0)
 
 int fail(int code, const std::string& msg);
+// Domain -> rank of SpRay's in-situ partition (insitu.cu).
+std::vector<int> insituPartition(const float* bounds, int nd, int num_ranks);
 
 struct HostTile {
   int x, y, w, h;
@@ -61,6 +74,10 @@ struct DomainPack {
   std::vector<uint32_t> colors;
   std::vector<float> normals;
   int bvh_depth = 0;
+  // triangles this domain numbers in the scene-wide triangle count (the hit
+  // keys' primitive ids); -1: nf.  A domain another rank owns keeps its count
+  // but no geometry, so every rank numbers triangles the same way.
+  int64_t prim_count = -1;
 };
 
 // Device slots of the out-of-core domain cache, least recently used first.
@@ -101,6 +118,8 @@ class Tracer {
   void traceViews(const spray_gpu_view* views, int n, float* out, bool out_is_device, spray_gpu_stats* st);
   int64_t debugCount(int what, int bounce) const;
   const std::vector<char>* debugData(int what, int bounce) const;
+  // domain-parallel (in-situ) execution, before setScene (insitu.cu)
+  void setInsitu(int num_ranks, int rank, const spray_gpu_reduce_ops* ops);
 
  private:
   int slots() const;
@@ -141,6 +160,17 @@ class Tracer {
                       size_t max_verts, size_t slot_bytes);
   void loadDomain(int d, int slot, cudaStream_t s);
   void traceOutOfCore(bool shadow, const std::vector<int>& order, int S);
+  // domain-parallel (in-situ) execution (insitu.cu)
+  bool situ() const { return insitu_ranks > 1; }
+  void traceOwned(bool shadow, int S);
+  void reduceCall(bool keys, void* dev, int64_t n, size_t elem);
+  char* reduceStage(size_t bytes);
+  int insitu_ranks = 1, insitu_rank = 0;
+  spray_gpu_reduce_ops reduce{};
+  std::vector<int> owner;      // domain -> rank of the partition
+  char* h_reduce = nullptr;    // pinned staging of the reductions
+  size_t h_reduce_cap = 0;
+  int64_t reduce_bytes = 0;    // bytes passed to the reductions during the frame
   // One pass over the domains for the radiance queues (buckets [rb_first,
   // rb_first + rb_count) of rbuckets) and/or the shadow queues; by_live orders
   // the domains by live entries, most first, instead of resident-first.
