@@ -289,6 +289,9 @@ int spray_generate_wavelet(int32_t samples, double iso, const double phase[3], f
 #define SPRAY_DBG_SHADOWS 3     /* spray_gpu_dbg_shadow, shadow rays and their occlusion */
 #define SPRAY_DBG_SQUEUES 4     /* spray_gpu_dbg_entry, shadow queue entries */
 #define SPRAY_DBG_SCORES 5      /* spray_gpu_dbg_score, domain scores and schedule order */
+#define SPRAY_DBG_LOADS 6       /* spray_gpu_dbg_load, out of core: every domain the frame asked the
+                                   cache for, in order (kept for every frame, bounce 0, no
+                                   debug_capture needed; empty in core) */
 
 typedef struct spray_gpu_dbg_ray {
   uint32_t sample;   /* index of the sample in the wavefront */
@@ -331,6 +334,14 @@ typedef struct spray_gpu_dbg_shadow {
   float tmax;
   int32_t occluded;
 } spray_gpu_dbg_shadow;
+
+typedef struct spray_gpu_dbg_load {
+  int32_t domain;
+  int32_t outcome;   /* 1 cache hit (already resident), 0 miss (copied into a slot), 2 traced
+                        in place from host memory (the cache is not asked) */
+  int32_t evicted;   /* domain whose slot a miss took, -1 none */
+  int32_t pass;      /* pass over the domains that made the request (0, 1, ... in the frame) */
+} spray_gpu_dbg_load;
 
 typedef struct spray_gpu_dbg_score {
   int32_t domain;

@@ -1075,6 +1075,7 @@ struct LruCache {  // lru_cache.cc:41-171
   std::list<std::pair<int, int>> blocks;  // (block, domain), front = LRU
   std::map<int, std::list<std::pair<int, int>>::iterator> id_to_block;
   std::vector<int> hit;
+  int last_evicted = -1;  // domain the last miss displaced, -1 when a block was free
   void init(int ndomains, int cache_size) {
     nd = ndomains;
     capacity = (cache_size < 0 || cache_size >= ndomains) ? ndomains : cache_size;
@@ -1093,6 +1094,7 @@ struct LruCache {  // lru_cache.cc:41-171
       return true;
     }
     hit[domid] = 1;
+    last_evicted = -1;
     if (size < capacity) {
       blocks.push_back({size, domid});
       id_to_block[domid] = std::prev(blocks.end());
@@ -1102,6 +1104,7 @@ struct LruCache {  // lru_cache.cc:41-171
       blocks.pop_front();
       id_to_block.erase(old.second);
       hit[old.second] = 0;
+      last_evicted = old.second;
       blocks.push_back({old.first, domid});
       id_to_block[domid] = std::prev(blocks.end());
     }
@@ -1903,10 +1906,15 @@ int orc_vbuf_trace(int32_t nsamples, int32_t H, int64_t n, const uint8_t* op, co
   return 0;
 }
 
-int orc_lru_trace(int32_t nd, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits) {
+int orc_lru_trace(int32_t nd, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits,
+                  int32_t* evicted) {
   orc::LruCache c;
   c.init(nd, cache_size);
-  for (int64_t i = 0; i < n; ++i) hits[i] = c.load(ids[i]) ? 1 : 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const bool h = c.load(ids[i]);
+    hits[i] = h ? 1 : 0;
+    if (evicted) evicted[i] = h ? -1 : c.last_evicted;
+  }
   return 0;
 }
 

@@ -114,8 +114,10 @@ int orc_slab(const float bounds[6], const float org[3], const float dir[3], floa
              float* tmin, float* tmax);
 int orc_triangle(const float org[3], const float dir[3], const float v[9], float tnear, float tfar,
                  float* t, float* u, float* v_out);
-/* replays domain loads through LruCache; hits[i] = 1 on a cache hit */
-int orc_lru_trace(int32_t num_domains, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits);
+/* replays domain loads through LruCache; hits[i] = 1 on a cache hit;
+ * evicted[i] (may be NULL) = the domain a miss displaced, -1 otherwise */
+int orc_lru_trace(int32_t num_domains, int32_t cache_size, int64_t n, const int32_t* ids, uint8_t* hits,
+                  int32_t* evicted);
 
 /* Per-function hooks, n cases each, for the comparison with the reference's
  * own code (oracle/build_ref.sh).  Vectors are packed float triples.

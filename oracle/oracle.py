@@ -89,7 +89,7 @@ def lib() -> C.CDLL:
         L.orc_sincos.argtypes = [C.c_int64, P, P, P]
         L.orc_slab.argtypes = [P, P, P, C.c_float, C.c_float, P, P]
         L.orc_triangle.argtypes = [P, P, P, C.c_float, C.c_float, P, P, P]
-        L.orc_lru_trace.argtypes = [C.c_int32, C.c_int32, C.c_int64, P, P]
+        L.orc_lru_trace.argtypes = [C.c_int32, C.c_int32, C.c_int64, P, P, P]
         L.orc_camera_rays.argtypes = [P, P, P, C.c_float, C.c_int32, C.c_int32, C.c_int64, P, P]
         for name in ("disk", "unpack_color", "blinn_phong"):
             getattr(L, "orc_" + name).argtypes = [C.c_int64, P, P]
@@ -149,11 +149,14 @@ def triangle(org, dir, verts, tnear=0.001, tfar=np.inf):
     return bool(hit), float(t[0]), float(u[0]), float(v[0])
 
 
-def lru_trace(num_domains: int, cache_size: int, ids) -> np.ndarray:
+def lru_trace(num_domains: int, cache_size: int, ids, with_evicted: bool = False):
+    """Replays loads through LruCache: hits (1 = hit), and with_evicted also
+    the domain each miss displaced (-1: none)."""
     ids = _i32(ids)
     hits = np.zeros(len(ids), np.uint8)
-    lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits))
-    return hits
+    ev = np.zeros(len(ids), np.int32)
+    lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits), _p(ev))
+    return (hits, ev) if with_evicted else hits
 
 
 def camera_rays(pos, lookat, up, vfov, image_w, image_h, xy) -> np.ndarray:

@@ -19,7 +19,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libspray_gpu.so"
 
 OK, EINVAL, ECUDA, EIO, ESTATE, EOVERFLOW, ENOMEM, ETIMEOUT = range(8)
-DBG_RAYS, DBG_RQUEUES, DBG_HITS, DBG_SHADOWS, DBG_SQUEUES, DBG_SCORES = range(6)
+DBG_RAYS, DBG_RQUEUES, DBG_HITS, DBG_SHADOWS, DBG_SQUEUES, DBG_SCORES, DBG_LOADS = range(7)
 
 
 class SprayError(RuntimeError):
@@ -113,6 +113,7 @@ DBG_DTYPES = {
                            ("origin", "<i4")]),
     DBG_SCORES: np.dtype([("domain", "<i4"), ("pad", "<i4"), ("score", "<i8"), ("order", "<i4"),
                           ("pad2", "<i4")]),
+    DBG_LOADS: np.dtype([("domain", "<i4"), ("outcome", "<i4"), ("evicted", "<i4"), ("pass", "<i4")]),
 }
 
 _lib_handle = None

@@ -787,7 +787,16 @@ void Tracer::loadDomain(int d, int slot, cudaStream_t s) {
 // entries are made resident in batches of at most the cache capacity (so a
 // batch never evicts its own domains), and each batch is traced in one launch
 // over its entry segments.
+// Request log of the frame (SPRAY_DBG_LOADS): domain, outcome, evicted, pass.
+void Tracer::logLoad(int d, int outcome, int evicted) {
+  const spray_gpu_dbg_load r{d, outcome, evicted, load_pass};
+  std::vector<char>& v = dbg[{SPRAY_DBG_LOADS, 0}];
+  const char* b = reinterpret_cast<const char*>(&r);
+  v.insert(v.end(), b, b + sizeof(r));
+}
+
 void Tracer::traceOutOfCore(bool shadow, const std::vector<int>& order, int S) {
+  ++load_pass;
   std::vector<uint32_t> ks(D + 1);
   CK(cudaMemcpyAsync(ks.data(), d_key_start, (D + 1) * 4, cudaMemcpyDeviceToHost, stream));
   CK(cudaStreamSynchronize(stream));
@@ -799,7 +808,9 @@ void Tracer::traceOutOfCore(bool shadow, const std::vector<int>& order, int S) {
     size_t j = std::min(todo.size(), i + (size_t)cache_capacity);
     for (size_t k = i; k < j; ++k) {
       int slot, evicted;
-      if (!lru.load(todo[k], &slot, &evicted)) {
+      const bool hit = lru.load(todo[k], &slot, &evicted);
+      logLoad(todo[k], hit ? 1 : 0, hit ? -1 : evicted);
+      if (!hit) {
         if (evicted >= 0) hdoms[evicted].resident = 0;
         loadDomain(todo[k], slot, stream);
       }
@@ -1339,6 +1350,7 @@ std::vector<int> Tracer::residentFirst(const std::vector<int>& order) const {
 // Dropping changes neither hit nor occlusion: a culled entry cannot beat its
 // ray's hit, and an occluded shadow ray stays occluded.
 void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int rb_count, bool by_live) {
+  ++load_pass;
   if (rb_count < 0) rb_count = rb - rb_first;
   const int rb_end = rb_first + rb_count;
   const int nrk = rb * D;  // radiance keys: bucket * D + domain
@@ -1462,10 +1474,13 @@ void Tracer::oocPass(bool with_r, bool with_s, int S, int rb, int rb_first, int 
       if (inPlace(d)) {
         hdoms[d].resident = 2;
         inplace.push_back(d);
+        logLoad(d, 2, -1);
         continue;
       }
       int slot, evicted;
-      if (!lru.load(d, &slot, &evicted)) {
+      const bool hit = lru.load(d, &slot, &evicted);
+      logLoad(d, hit ? 1 : 0, hit ? -1 : evicted);
+      if (!hit) {
         if (evicted >= 0) hdoms[evicted].resident = 0;
         loadDomain(d, slot, cstream);
       }
@@ -2011,6 +2026,8 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     occl_events.clear();
     copy_events.clear();
     dbg.clear();
+    dbg[{SPRAY_DBG_LOADS, 0}];  // the request log exists for every frame (empty in core)
+    load_pass = 0;
     use_pred_order = false;
     CK(cudaEventRecord(ev_start, stream));
     if (use_bins && fviews.size() == 1) buildScreenBins();
@@ -2269,7 +2286,8 @@ int64_t Tracer::debugCount(int what, int bounce) const {
   if (it == dbg.end()) return -1;
   static const size_t sizes[] = {sizeof(spray_gpu_dbg_ray), sizeof(spray_gpu_dbg_entry),
                                  sizeof(spray_gpu_dbg_hit), sizeof(spray_gpu_dbg_shadow),
-                                 sizeof(spray_gpu_dbg_entry), sizeof(spray_gpu_dbg_score)};
+                                 sizeof(spray_gpu_dbg_entry), sizeof(spray_gpu_dbg_score),
+                                 sizeof(spray_gpu_dbg_load)};
   return (int64_t)(it->second.size() / sizes[what]);
 }
 
@@ -2446,7 +2464,7 @@ int spray_gpu_trace_views_device(spray_gpu_tracer* t, const spray_gpu_view* view
 
 int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int64_t* count) {
   if (!t || !count) return fail(SPRAY_GPU_EINVAL, "null argument");
-  if (what < 0 || what > SPRAY_DBG_SCORES) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
+  if (what < 0 || what > SPRAY_DBG_LOADS) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
   int64_t n = t->impl->debugCount(what, bounce);
   if (n < 0) return fail(SPRAY_GPU_ESTATE, "no captured buffer (set debug_capture and trace)");
   *count = n;
@@ -2455,7 +2473,7 @@ int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int
 
 int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void* out, int64_t capacity) {
   if (!t || !out) return fail(SPRAY_GPU_EINVAL, "null argument");
-  if (what < 0 || what > SPRAY_DBG_SCORES) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
+  if (what < 0 || what > SPRAY_DBG_LOADS) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
   const std::vector<char>* d = t->impl->debugData(what, bounce);
   if (!d) return fail(SPRAY_GPU_ESTATE, "no captured buffer (set debug_capture and trace)");
   if ((int64_t)d->size() > capacity) return fail(SPRAY_GPU_EINVAL, "output buffer too small");

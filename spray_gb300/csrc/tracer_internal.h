@@ -329,6 +329,8 @@ class Tracer {
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   int64_t inplace_domains = 0;  // (domain, batch) pairs traced in place this frame
   std::map<std::pair<int, int>, std::vector<char>> dbg;
+  int load_pass = 0;  // passes over the domains in this frame (the request log's pass numbers)
+  void logLoad(int d, int outcome, int evicted);
 };
 
 }  // namespace spray
