@@ -113,6 +113,8 @@ typedef struct spray_gpu_config {
                                    predicted one first (in core and inside an out-of-core batch);
                                    0 = the prediction only orders the out-of-core domain loads,
                                    every ray keeps its front-to-back order (0) */
+  int32_t bvh_device;           /* 1: set_scene builds the domains' BVHs on the GPU (binned SAH,
+                                   4-wide nodes); 0: on the host cores (1) */
 } spray_gpu_config;
 
 /* One domain: a triangle mesh in world space (transform already applied, as

@@ -43,7 +43,7 @@ class ConfigC(C.Structure):
         ("learn_epochs", C.c_int32), ("learn_lr", C.c_float), ("learn_seed", C.c_int32),
         ("learn_frames", C.c_int32), ("graphs", C.c_int32), ("ooc_inplace", C.c_int32),
         ("trace_blocks_per_sm", C.c_int32), ("sched_chunks_per_warp", C.c_int32),
-        ("bucket_launches", C.c_int32), ("learn_buckets", C.c_int32),
+        ("bucket_launches", C.c_int32), ("learn_buckets", C.c_int32), ("bvh_device", C.c_int32),
     ]
 
 

@@ -123,7 +123,7 @@ CameraDev makeCamera(const float p[3], const float l[3], const float up[3], floa
 }
 
 // ---------------------------------------------------------------- domain preparation
-void buildPack(const spray_gpu_domain& src, int d, DomainPack& p) {
+void buildPack(const spray_gpu_domain& src, int d, DomainPack& p, bool bvh) {
   if (src.num_faces <= 0 || src.num_vertices <= 0 || !src.vertices || !src.faces)
     throw std::invalid_argument("domain " + std::to_string(d) + " has no geometry");
   if (src.num_faces >= (1ll << 28)) throw std::invalid_argument("domain too large");
@@ -134,19 +134,21 @@ void buildPack(const spray_gpu_domain& src, int d, DomainPack& p) {
   p.nf = src.num_faces;
   p.normals.resize(3 * (size_t)p.nv);
   computeVertexNormals(src.vertices, p.nv, src.faces, p.nf, p.normals.data());
-  BvhBuildResult bvh;
-  buildBvh4(src.vertices, src.faces, (uint32_t)p.nf, &bvh);
-  p.nodes = std::move(bvh.nodes);
-  p.bvh_depth = bvh.depth;
-  p.tris.resize(3 * (size_t)p.nf);
-  for (size_t k = 0; k < bvh.tri_order.size(); ++k) {
-    uint32_t prim = bvh.tri_order[k];
-    const uint32_t* fi = src.faces + 3 * (size_t)prim;
-    for (int c = 0; c < 3; ++c) {
-      const float* vp = src.vertices + 3 * (size_t)fi[c];
-      float w = 0.f;
-      if (c == 0) std::memcpy(&w, &prim, 4);
-      p.tris[3 * k + c] = make_float4(vp[0], vp[1], vp[2], w);
+  if (bvh) {
+    BvhBuildResult b;
+    buildBvh4(src.vertices, src.faces, (uint32_t)p.nf, &b);
+    p.nodes = std::move(b.nodes);
+    p.bvh_depth = b.depth;
+    p.tris.resize(3 * (size_t)p.nf);
+    for (size_t k = 0; k < b.tri_order.size(); ++k) {
+      uint32_t prim = b.tri_order[k];
+      const uint32_t* fi = src.faces + 3 * (size_t)prim;
+      for (int c = 0; c < 3; ++c) {
+        const float* vp = src.vertices + 3 * (size_t)fi[c];
+        float w = 0.f;
+        if (c == 0) std::memcpy(&w, &prim, 4);
+        p.tris[3 * k + c] = make_float4(vp[0], vp[1], vp[2], w);
+      }
     }
   }
   p.faces.assign(src.faces, src.faces + 3 * p.nf);
@@ -487,11 +489,12 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   } else {
     owner.assign(nd, 0);
   }
+  const bool dev_bvh = cfg.bvh_device != 0;
 #pragma omp parallel for schedule(dynamic, 1)
   for (int d = 0; d < nd; ++d) {
     try {
       if (owner[d] == insitu_rank) {
-        buildPack(doms[d], d, packs[d]);
+        buildPack(doms[d], d, packs[d], !dev_bvh);
       } else {
         // another rank's domain: its box, material and triangle count only
         DomainPack& p = packs[d];
@@ -507,6 +510,13 @@ void Tracer::setScene(const spray_gpu_domain* doms, int nd, const spray_gpu_ligh
   }
   for (int d = 0; d < nd; ++d)
     if (!errors[d].empty()) throw std::invalid_argument(errors[d]);
+  if (dev_bvh) {
+    std::vector<int> mine;
+    for (int d = 0; d < nd; ++d)
+      if (owner[d] == insitu_rank) mine.push_back(d);
+    // batches of at most 16 M triangles bound the build's device memory (~5 GB)
+    buildBvhsOnDevice(doms, mine, packs, stream, 16ull << 20);
+  }
   installScene(packs, ls, nl);
 }
 
@@ -2352,6 +2362,7 @@ void spray_gpu_config_defaults(spray_gpu_config* c) {
   c->learn_frames = 4;
   c->graphs = 1;
   c->ooc_inplace = 16384;
+  c->bvh_device = 1;
 }
 
 const char* spray_gpu_last_error(void) { return spray::g_last_error.c_str(); }

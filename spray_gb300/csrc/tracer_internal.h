@@ -93,7 +93,14 @@ struct LruSlots {
 
 // Normals, BVH and leaf-ordered triangles of one domain (TriMeshBuffer::load
 // and its Embree build, src/render/trimesh_buffer.cc:117-326).
-void buildPack(const spray_gpu_domain& src, int d, DomainPack& p);
+// Host preparation of one domain: checks, vertex normals, faces, colours and,
+// with `bvh`, the BVH and leaf-ordered triangles (otherwise left empty for
+// buildBvhsOnDevice).
+void buildPack(const spray_gpu_domain& src, int d, DomainPack& p, bool bvh = true);
+// The BVHs (nodes, leaf-ordered triangles, depth) of the domains `which` of
+// `src`, built on the current device (bvh_build.cu).
+void buildBvhsOnDevice(const spray_gpu_domain* src, const std::vector<int>& which, std::vector<DomainPack>& packs,
+                       cudaStream_t stream, uint64_t batch_tris);
 // Prepared-domain blobs: one file per domain holding everything buildPack
 // makes, so that a scene is prepared once and loaded without rebuilding.
 std::string domainBlobPath(const std::string& dir, int d);

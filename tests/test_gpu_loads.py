@@ -43,7 +43,7 @@ def test_domain_requests_replay_through_the_reference_lru(lib_built, oracle_mod,
     t = sg.Tracer(cfg)
     t.set_scene(grid)
     t.set_camera(*scenes.orbit_camera(grid))
-    reqs, loads = [], 0
+    reqs, loads, inplace = [], 0, 0
     for frame in range(3):
         _, st = t.trace()
         log = t.debug(sg.DBG_LOADS, 0)
@@ -52,8 +52,15 @@ def test_domain_requests_replay_through_the_reference_lru(lib_built, oracle_mod,
         assert st["inplace_domains"] == int(np.sum(log["outcome"] == 2))
         reqs.append(cached)
         loads += st["domain_loads"]
+        inplace += st["inplace_domains"]
     allr = np.concatenate(reqs)
-    assert len(allr) > 0 and loads > 0
+    if extra.get("ooc_inplace", 1) != 0 and policy in (2, 3):
+        # with in-place tracing this small frame may never ask the cache
+        assert len(allr) + inplace > 0
+        if len(allr) == 0:
+            return
+    else:
+        assert len(allr) > 0 and loads > 0 and inplace == 0
     hits, evicted = oracle_mod.lru_trace(len(grid.domains), cache, allr["domain"], with_evicted=True)
     assert np.array_equal(hits.astype(np.int32), allr["outcome"])
     assert np.array_equal(evicted, allr["evicted"])
