@@ -2,14 +2,16 @@
 # TEST INFRASTRUCTURE ONLY.  Builds, from the reference's own sources where
 # they lie (read-only), the two libraries the oracle is checked against:
 #   oracle/_ref/libref_rng.so   deps/embree/random_sampler.h (ref_rng.cpp)
-#   oracle/_ref/libref_path.so  render/{sampler,lru_cache,tile}.cc,
+#   oracle/_ref/libref_path.so  render/{sampler,lru_cache,tile,trimesh_buffer}.cc,
 #                               ooc/{ooc_domain_stats,ooc_vbuf}.cc,
 #                               io/{scene_loader,ply_loader}.cc,
 #                               deps/pbrt/memory.cpp and the inline code of
 #                               render/{aabb,camera,light,reflection}.h,
-#                               display/image.h and utils/util.h (ref_path.cpp)
+#                               display/image.h, utils/util.h and render/rays.h
+#                               (ref_path.cpp)
 # oracle/ref_shim stands in for glm, glog, mpi.h, the CMake-generated config
-# header and the MPI profiler header, none of which exist here.  Nothing of the
+# header, the MPI profiler header and the Embree 2 declarations, none of which
+# exist here.  Nothing of the
 # reference is copied.  Exits 0 without building when the reference tree is
 # absent.
 set -e
@@ -28,6 +30,7 @@ g++ $FLAGS -std=gnu++11 -fpermissive -DPBRT_HAVE_CONSTEXPR -DPBRT_CONSTEXPR=cons
     -DPBRT_HAVE_ALIGNAS -DPBRT_HAVE_ALIGNOF -DPBRT_HAVE_POSIX_MEMALIGN \
     -I "$HERE/ref_shim" -I "$REF/src" -I "$REF/deps" \
     "$HERE/ref_path.cpp" "$REF/src/render/sampler.cc" "$REF/src/render/lru_cache.cc" "$REF/src/render/tile.cc" \
+    "$REF/src/render/trimesh_buffer.cc" \
     "$REF/src/ooc/ooc_domain_stats.cc" "$REF/src/io/scene_loader.cc" "$REF/src/io/ply_loader.cc" \
     "$REF/src/ooc/ooc_vbuf.cc" "$REF/deps/pbrt/memory.cpp" \
     -o "$HERE/_ref/libref_path.so"

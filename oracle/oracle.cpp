@@ -377,6 +377,8 @@ struct Hit {
   uint32_t prim;
 };
 
+void sortDomainList(std::vector<std::pair<float, int>>* l);
+
 // Closest hit in a domain, tnear = 1e-3, tfar = inf (Scene::intersect,
 // src/render/scene.inl:189-199).  Ties keep the lowest primitive id.
 bool closestInDomain(const Domain& d, F3 org, F3 dir, Hit* h) {
@@ -617,9 +619,7 @@ struct Oracle {
       float tmin, tmx;
       if (intersectAabb(doms[i].lo, doms[i].hi, o, d, kEps, tmax, &tmin, &tmx)) out->push_back({tmin, i});
     }
-    std::sort(out->begin(), out->end(), [](const std::pair<float, int>& a, const std::pair<float, int>& b) {
-      return (a.first < b.first) || ((a.first == b.first) && (a.second < b.second));
-    });
+    sortDomainList(out);
   }
 
   int slots() const {
@@ -1539,31 +1539,81 @@ int orc_set_lights(void* ov, int32_t nl, const float* L) {
   return 0;
 }
 
+extern "C++" {
+namespace orc {
+// TriMeshBuffer::computeNormals (src/render/trimesh_buffer.cc:267-326):
+// unnormalised face normals (u x v) summed into each vertex in face order.
+void computeNormals(Domain& D) {
+  size_t nv = D.v.size() / 3, nf = D.f.size() / 3;
+  D.normals.assign(3 * nv, 0.0f);
+  for (size_t i = 0; i < nf; ++i) {
+    size_t vid[3] = {D.f[3 * i] * 3ull, D.f[3 * i + 1] * 3ull, D.f[3 * i + 2] * 3ull};
+    F3 v0 = f3(D.v[vid[0]], D.v[vid[0] + 1], D.v[vid[0] + 2]);
+    F3 v1 = f3(D.v[vid[1]], D.v[vid[1] + 1], D.v[vid[1] + 2]);
+    F3 v2 = f3(D.v[vid[2]], D.v[vid[2] + 1], D.v[vid[2] + 2]);
+    F3 u = sub(v1, v0), v = sub(v2, v0);
+    F3 n;
+    n.x = u.y * v.z - u.z * v.y;
+    n.y = u.z * v.x - u.x * v.z;
+    n.z = u.x * v.y - u.y * v.x;
+    for (int k = 0; k < 3; ++k) {
+      D.normals[vid[k]] += n.x;
+      D.normals[vid[k] + 1] += n.y;
+      D.normals[vid[k] + 2] += n.z;
+    }
+  }
+}
+
+// DomainList::sort (src/render/rays.h:71-79): by entry distance, ties by id.
+void sortDomainList(std::vector<std::pair<float, int>>* l) {
+  std::sort(l->begin(), l->end(), [](const std::pair<float, int>& a, const std::pair<float, int>& b) {
+    return (a.first < b.first) || ((a.first == b.first) && (a.second < b.second));
+  });
+}
+}  // namespace orc
+}  // extern "C++"
+
 int orc_build(void* ov) {
   Oracle* o = (Oracle*)ov;
 #pragma omp parallel for schedule(dynamic, 1)
   for (int d = 0; d < o->D(); ++d) {
     orc::Domain& D = o->doms[d];
-    // TriMeshBuffer::computeNormals (src/render/trimesh_buffer.cc:267-326)
-    size_t nv = D.v.size() / 3, nf = D.f.size() / 3;
-    D.normals.assign(3 * nv, 0.0f);
-    for (size_t i = 0; i < nf; ++i) {
-      size_t vid[3] = {D.f[3 * i] * 3ull, D.f[3 * i + 1] * 3ull, D.f[3 * i + 2] * 3ull};
-      F3 v0 = f3(D.v[vid[0]], D.v[vid[0] + 1], D.v[vid[0] + 2]);
-      F3 v1 = f3(D.v[vid[1]], D.v[vid[1] + 1], D.v[vid[1] + 2]);
-      F3 v2 = f3(D.v[vid[2]], D.v[vid[2] + 1], D.v[vid[2] + 2]);
-      F3 u = orc::sub(v1, v0), v = orc::sub(v2, v0);
-      F3 n;
-      n.x = u.y * v.z - u.z * v.y;
-      n.y = u.z * v.x - u.x * v.z;
-      n.z = u.x * v.y - u.y * v.x;
-      for (int k = 0; k < 3; ++k) {
-        D.normals[vid[k]] += n.x;
-        D.normals[vid[k] + 1] += n.y;
-        D.normals[vid[k] + 2] += n.z;
-      }
-    }
+    orc::computeNormals(D);
     orc::buildBvh(D.v, D.f, &D.bvh);
+  }
+  return 0;
+}
+
+int orc_domain_list_sort(int32_t n, const int32_t* ids, const float* ts, int32_t* ids_out, float* ts_out) {
+  std::vector<std::pair<float, int>> l;
+  for (int32_t i = 0; i < n; ++i) l.push_back({ts[i], ids[i]});
+  orc::sortDomainList(&l);
+  for (int32_t i = 0; i < n; ++i) {
+    ids_out[i] = l[i].second;
+    ts_out[i] = l[i].first;
+  }
+  return 0;
+}
+
+int orc_mesh_attributes(const float* vertices, int64_t nv, const uint32_t* faces, int64_t nf,
+                        const uint32_t* colors, int64_t n, const uint32_t* prim, const float* u, const float* v,
+                        uint32_t* color, float* ns, float* normals) {
+  orc::Domain D;
+  D.v.assign(vertices, vertices + 3 * nv);
+  D.f.assign(faces, faces + 3 * nf);
+  D.colors.assign(colors, colors + nv);
+  orc::computeNormals(D);
+  if (normals) std::memcpy(normals, D.normals.data(), D.normals.size() * 4);
+  for (int64_t i = 0; i < n; ++i) {
+    orc::Hit h;
+    h.prim = prim[i];
+    h.u = u[i];
+    h.v = v[i];
+    F3 nn;
+    orc::shadingAttributes(D, h, &color[i], &nn);
+    ns[3 * i] = nn.x;
+    ns[3 * i + 1] = nn.y;
+    ns[3 * i + 2] = nn.z;
   }
   return 0;
 }

@@ -146,6 +146,14 @@ int orc_refract(int64_t n, const float* args, uint8_t* ok, float* wt);
  * is the returned flag, hist the ray's history afterwards */
 int orc_vbuf_trace(int32_t nsamples, int32_t H, int64_t n, const uint8_t* op, const int32_t* samid,
                    const int32_t* depth, float* hist, const float* t, uint8_t* result);
+/* DomainList::sort (rays.h:71-79) of n (id, tnear) pairs in push order */
+int orc_domain_list_sort(int32_t n, const int32_t* ids, const float* ts, int32_t* ids_out, float* ts_out);
+/* TriMeshBuffer::computeNormals + updateIntersection (trimesh_buffer.cc:267-360)
+ * on a mesh: n (triangle, u, v) queries -> interpolated colour and shading
+ * normal; normals (may be NULL) receives the 3 * nv vertex normals */
+int orc_mesh_attributes(const float* vertices, int64_t nv, const uint32_t* faces, int64_t nf,
+                        const uint32_t* colors, int64_t n, const uint32_t* prim, const float* u, const float* v,
+                        uint32_t* color, float* ns, float* normals);
 /* HdrImage::add in order: rgba[4 * pixid[i] + c] += scale * rgb[3 * i + c] */
 int orc_hdr_add(int64_t n, const int32_t* pixid, const float* rgb, double scale, float* rgba);
 

@@ -98,6 +98,8 @@ def lib() -> C.CDLL:
         L.orc_cosine_sample.argtypes = [C.c_int64, P, P, P, P]
         L.orc_hdr_add.argtypes = [C.c_int64, P, P, C.c_double, P]
         L.orc_vbuf_trace.argtypes = [C.c_int32, C.c_int32, C.c_int64, P, P, P, P, P, P]
+        L.orc_domain_list_sort.argtypes = [C.c_int32, P, P, P, P]
+        L.orc_mesh_attributes.argtypes = [P, C.c_int64, P, C.c_int64, P, C.c_int64, P, P, P, P, P, P]
         L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
         L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
         _lib = L
@@ -157,6 +159,28 @@ def lru_trace(num_domains: int, cache_size: int, ids, with_evicted: bool = False
     ev = np.zeros(len(ids), np.int32)
     lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits), _p(ev))
     return (hits, ev) if with_evicted else hits
+
+
+def domain_list_sort(ids, ts) -> tuple[np.ndarray, np.ndarray]:
+    """DomainList::sort of (id, tnear) pairs pushed in the given order."""
+    ids, ts = _i32(ids), _f32(ts)
+    oi, ot = np.zeros_like(ids), np.zeros_like(ts)
+    lib().orc_domain_list_sort(len(ids), _p(ids), _p(ts), _p(oi), _p(ot))
+    return oi, ot
+
+
+def mesh_attributes(vertices, faces, colors, prim, u, v):
+    """Vertex normals and (colour, shading normal) at n (triangle, u, v)."""
+    vv = _f32(vertices).reshape(-1, 3)
+    ff = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+    cc = np.ascontiguousarray(colors, np.uint32)
+    pr = np.ascontiguousarray(prim, np.uint32)
+    col = np.zeros(len(pr), np.uint32)
+    ns = np.zeros((len(pr), 3), np.float32)
+    nrm = np.zeros((len(vv), 3), np.float32)
+    lib().orc_mesh_attributes(_p(vv), len(vv), _p(ff), len(ff), _p(cc), len(pr), _p(pr), _p(_f32(u)), _p(_f32(v)),
+                              _p(col), _p(ns), _p(nrm))
+    return nrm, col, ns
 
 
 def camera_rays(pos, lookat, up, vfov, image_w, image_h, xy) -> np.ndarray:

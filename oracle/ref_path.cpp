@@ -11,6 +11,10 @@
 // includes OpenGL); the slab test reads only Aabb::bounds, so the default
 // constructor it would provide is defined empty below.
 //
+// render/rays.h and render/trimesh_buffer.cc name Embree 2's ray, scene and
+// mesh declarations; oracle/ref_shim/embree2 declares them, with set-up calls
+// that do nothing (the pinned functions trace no rays).
+//
 // Include order follows src/apps/spray_ooc.cc: the shader headers (light.h,
 // reflection.h, hence sampler.h and <math.h>) come before camera.h, so the
 // unqualified tan() in Camera::init resolves as it does in that program.
@@ -30,6 +34,8 @@
 #include "ooc/ooc_vbuf.h"
 #include "utils/comm.h"
 #include "utils/util.h"
+#include "render/rays.h"
+#include "render/trimesh_buffer.h"
 
 namespace spray {
 Aabb::Aabb() {}
@@ -348,6 +354,43 @@ int ref_write_ppm(int32_t w, int32_t h, const float* rgba, const char* filename)
   img.resize(w, h);
   std::memcpy(img.buf, rgba, sizeof(float) * 4 * (size_t)w * h);
   img.writePpm(filename);
+  return 0;
+}
+
+// DomainList::push then DomainList::sort (render/rays.h:57-93) of n (id,
+// tnear) pairs, pushed in the given order; the sorted pairs come back.
+int ref_domain_list_sort(int32_t n, const int32_t* ids, const float* ts, int32_t* ids_out, float* ts_out) {
+  DomainList l;
+  l.resize((std::size_t)n);
+  l.reset();
+  for (int32_t i = 0; i < n; ++i) l.push(ids[i], ts[i]);
+  l.sort();
+  for (int32_t i = 0; i < n; ++i) {
+    ids_out[i] = l.getId((std::size_t)i);
+    ts_out[i] = l.getTnear((std::size_t)i);
+  }
+  return 0;
+}
+
+// TriMeshBuffer::load of a PLY file (no transform; vertex normals by
+// computeNormals, render/trimesh_buffer.cc:117-169,288-326), then
+// updateIntersection (trimesh_buffer.cc:328-360) for n (triangle, u, v):
+// interpolated colour and shading normal.
+int ref_mesh_attributes(const char* ply, int64_t max_nv, int64_t max_nf, int64_t n, const uint32_t* prim,
+                        const float* u, const float* v, uint32_t* color, float* ns) {
+  TriMeshBuffer mesh;
+  mesh.init(1, (std::size_t)max_nv, (std::size_t)max_nf, true);
+  mesh.load(ply, 0, glm::mat4(1.0f), false);
+  for (int64_t i = 0; i < n; ++i) {
+    RTCRayIntersection isect;
+    std::memset(&isect, 0, sizeof(isect));
+    isect.primID = prim[i];
+    isect.u = u[i];
+    isect.v = v[i];
+    mesh.updateIntersection(0, &isect);
+    color[i] = isect.color;
+    for (int k = 0; k < 3; ++k) ns[3 * i + k] = isect.Ns[k];
+  }
   return 0;
 }
 

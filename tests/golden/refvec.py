@@ -35,6 +35,9 @@ domain_order   DomainStats::schedule, ooc/ooc_domain_stats.cc:60-111 ties
 vbuf           VBuf::update/correct, ooc/ooc_vbuf.cc:41-112          exact
 hdr_add        HdrImage::add (double scale), display/image.h:99-109 bit-exact
 ppm            HdrImage::writePpm, display/image.h:183-204         bytes (*)
+domain_list    DomainList::push/sort, render/rays.h:57-93           exact
+mesh           TriMeshBuffer::computeNormals/updateIntersection,    bit-exact
+               render/trimesh_buffer.cc:267-360
 ============== ==================================================== =========
 
 (*) ppm holds the product's writer (spray_gb300.image), not the oracle, to the
@@ -79,7 +82,7 @@ BLINN_REL = 1e-5
 
 GROUPS = ["rng", "slab", "camera", "disk", "local_to_world", "cosine", "diffuse_light", "point_light",
           "blinn_phong", "reflect", "fr_dielectric", "refract", "unpack", "lru", "tiles", "domain_order",
-          "vbuf", "hdr_add", "ppm"]
+          "vbuf", "hdr_add", "ppm", "domain_list", "mesh"]
 VBUF_SAMPLES, HISTORY = 8, 4  # SPRAY_SPECU_HISTORY_SIZE in the reference's CMake defaults
 HDR_W, HDR_H = 13, 7
 
@@ -256,6 +259,39 @@ def make_cases(seed: int = 2024, scale: int = 1) -> dict:
                            np.inf, -np.inf, np.nan, 1e-30, 0.99999994]]).astype(f32)
     img.reshape(-1)[:len(edge)] = edge
     c["ppm"] = {"rgba": img}
+
+    # domain lists of up to 22 hits (the C3 list size) pushed in any order:
+    # distances quantised so that ties are common, negative entries (origin
+    # inside a box), +0 and -0; ids unique per list
+    nl = 120 * scale
+    sizes = rng.integers(1, 23, nl)
+    ids, ts = [], []
+    for n in sizes:
+        ids.append(rng.permutation(512)[:n].astype(np.int32))
+        t = np.round(rng.uniform(-2, 6, n) * 4) / 4
+        t[rng.random(n) < 0.1] = 0.0
+        t = t.astype(f32)
+        t[rng.random(n) < 0.05] = f32(-0.0)
+        ts.append(t)
+    c["domain_list"] = {"size": sizes.astype(np.int32), "ids": np.concatenate(ids), "ts": np.concatenate(ts)}
+
+    # a mesh with per-vertex colours (every byte value occurs), queried at
+    # its triangles' corners, edges and random barycentrics
+    mv, mf = _sphere(14, 24)
+    ncol = len(mv)
+    col = rng.integers(0, 256, (ncol, 3)).astype(np.uint32)
+    col[:3] = [[0, 0, 0], [255, 255, 255], [255, 0, 128]]
+    nq = 1000 * scale
+    prim = rng.integers(0, len(mf), nq).astype(np.uint32)
+    uu = rng.random(nq).astype(f32)
+    vv = (rng.random(nq) * (1 - uu)).astype(f32)
+    corners = np.array([[0, 0], [1, 0], [0, 1], [0.5, 0.5]], f32)
+    k = len(corners) * len(mf)
+    prim = np.concatenate([np.repeat(np.arange(len(mf), dtype=np.uint32), len(corners)), prim])
+    uu = np.concatenate([np.tile(corners[:, 0], len(mf)), uu])
+    vv = np.concatenate([np.tile(corners[:, 1], len(mf)), vv])
+    c["mesh"] = {"vertices": mv, "faces": mf, "colors": (col[:, 0] << 16) | (col[:, 1] << 8) | col[:, 2],
+                 "prim": prim, "u": uu, "v": vv, "corner_queries": np.array([k], np.int64)}
     return c
 
 
@@ -419,6 +455,26 @@ def reference_outputs(cases: dict, libs) -> dict:
         path = Path(tmp) / "ref.ppm"
         R.ref_write_ppm(img.shape[1], img.shape[0], _p(img), str(path).encode())
         out["ppm"] = {"bytes": np.frombuffer(path.read_bytes(), np.uint8).copy()}
+
+    R.ref_domain_list_sort.argtypes = [C.c_int32, P, P, P, P]
+    dl = cases["domain_list"]
+    oi, ot = np.zeros_like(dl["ids"]), np.zeros_like(dl["ts"])
+    off = 0
+    for n in dl["size"]:
+        R.ref_domain_list_sort(int(n), _p(dl["ids"][off:]), _p(dl["ts"][off:]), _p(oi[off:]), _p(ot[off:]))
+        off += int(n)
+    out["domain_list"] = {"ids": oi, "ts": ot}
+
+    R.ref_mesh_attributes.argtypes = [C.c_char_p, I64, I64, I64, P, P, P, P, P]
+    ms = cases["mesh"]
+    col = np.zeros(len(ms["prim"]), np.uint32)
+    ns = np.zeros((len(ms["prim"]), 3), f32)
+    with tempfile.TemporaryDirectory() as tmp:
+        ply = Path(tmp) / "mesh.ply"
+        ply.write_bytes(_ply_binary(ms["vertices"], ms["faces"], ms["colors"]))
+        R.ref_mesh_attributes(str(ply).encode(), len(ms["vertices"]), len(ms["faces"]), len(ms["prim"]),
+                              _p(ms["prim"]), _p(ms["u"]), _p(ms["v"]), _p(col), _p(ns))
+    out["mesh"] = {"color": col, "ns": ns}
     return out
 
 
@@ -500,6 +556,17 @@ def oracle_outputs(cases: dict) -> dict:
                                                   float(sc_)) for sc_ in hd["scale"]])}
     from spray_gb300 import image
     out["ppm"] = {"bytes": np.frombuffer(image.ppm_bytes(cases["ppm"]["rgba"]), np.uint8).copy()}
+    dl = cases["domain_list"]
+    ids, ts, off = [], [], 0
+    for n in dl["size"]:
+        a, b = O.domain_list_sort(dl["ids"][off:off + n], dl["ts"][off:off + n])
+        ids.append(a)
+        ts.append(b)
+        off += int(n)
+    out["domain_list"] = {"ids": np.concatenate(ids), "ts": np.concatenate(ts)}
+    ms = cases["mesh"]
+    nrm, col, ns = O.mesh_attributes(ms["vertices"], ms["faces"], ms["colors"], ms["prim"], ms["u"], ms["v"])
+    out["mesh"] = {"color": col, "ns": ns, "normals": nrm}
     return out
 
 
@@ -557,6 +624,21 @@ def compare(group: str, cases: dict, ref: dict, orc: dict) -> None:
         assert np.array_equal(r["ok"], o["ok"]) and _same(r["wt"], o["wt"])
     elif group == "lru":
         assert np.array_equal(r["hits"], o["hits"])
+    elif group == "domain_list":
+        assert np.array_equal(r["ids"], o["ids"]) and _same(r["ts"], o["ts"])
+    elif group == "mesh":
+        assert np.array_equal(r["color"], o["color"]), int(np.sum(r["color"] != o["color"]))
+        assert _same(r["ns"], o["ns"]), int(np.sum(np.any(_bits(r["ns"]) != _bits(o["ns"]), 1)))
+        # the reference's vertex normals, read at the triangles' corners
+        # (w, u, v = 1, 0, 0 / 0, 1, 0 / 0, 0, 1), equal the oracle's
+        ms = cases["mesh"]
+        k = int(ms["corner_queries"][0])
+        nc = 4
+        f = ms["faces"]
+        for corner, vi in ((0, 0), (1, 1), (2, 2)):
+            got = r["ns"][:k].reshape(-1, nc, 3)[:, corner]
+            want = o["normals"][f[:, vi]]
+            assert np.array_equal(got, want)  # values (+0 and -0 equal)
     elif group == "tiles":
         assert np.array_equal(r["count"], o["count"]) and np.array_equal(r["tiles"], o["tiles"])
     elif group == "domain_order":
