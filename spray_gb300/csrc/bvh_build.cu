@@ -10,9 +10,11 @@
 //              box, centroid box) in warp-private shared-memory bins, the SAH
 //              sweep, then a stable partition (block scan) from one index
 //              buffer into the other; the children's boxes and centroid
-//              boxes come from the bins.  Smaller tasks are built by single
-//              warps, depth first, continuing with the smaller child so a
-//              warp's stack stays within log2(kSmallTask) + 1 entries.
+//              boxes come from the bins.
+//   kBuildSmall the tasks of at most kSmallTask triangles, one warp each,
+//              warps of every SM pulling from one counter: depth first,
+//              continuing with the smaller child so a warp's stack stays
+//              within log2(kSmallTask) + 1 entries.
 //   kCollapse  4-wide nodes: each node takes its binary node's children and
 //              opens the inner child with the largest box until it holds
 //              four (the host builder's rule), one warp per domain
@@ -46,6 +48,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kSmallTask = 256;        // tasks of at most this many triangles go to a warp
 constexpr int kWarpStack = 12;         // >= log2(kSmallTask) + 2
 constexpr int kBigStack = 64;          // CTA task stack (depth first, smaller child first)
+constexpr int kMaxBatchDomains = 4096; // domains built together (kBuildSmall's shared prefix)
 constexpr float kTraversalCost = 1.0f;  // relative to one triangle test, as the host builder
 
 enum : int { kErrStack = 1, kErrSmallList = 2, kErrNodes = 4, kErrQueue = 8, kErrLeaf = 16, kErrPartition = 32 };
@@ -368,8 +371,10 @@ __device__ void rangeBounds(const Batch& B, const Dom& d, uint32_t parity, uint3
   else __syncwarp();
 }
 
-// Builds the subtree of a small task with one warp, depth first.
-__device__ void buildSmall(const Batch& B, const Dom& d, Shared& S, Task root, int warp, int lane) {
+// Builds the subtree of a small task with one warp, depth first; binary node
+// ids come from the domain's counter in global memory.
+__device__ void buildSmall(const Batch& B, const Dom& d, Shared& S, Task root, int warp, int lane,
+                           uint32_t* node_counter) {
   Bins* bins = &S.bins[warp];
   Task* st = S.wstack[warp];
   int sp = 0;
@@ -471,7 +476,7 @@ __device__ void buildSmall(const Batch& B, const Dom& d, Shared& S, Task root, i
                     clo[1], chi[1], false);
       }
       int ids = 0;
-      if (lane == 0) ids = atomicAdd(&S.nnodes, 2);
+      if (lane == 0) ids = (int)atomicAdd(node_counter, 2u);
       ids = __shfl_sync(0xffffffffu, ids, 0);
       if ((uint32_t)ids + 2 > 2 * d.nf) {
         if (lane == 0) atomicOr(B.error, kErrNodes);
@@ -662,14 +667,54 @@ __global__ void __launch_bounds__(kThreads) kBuild(Batch B) {
     if (S.stop) break;
   }
   __syncthreads();
-  // the small tasks, one warp each
-  const int nsmall = S.nsmall;
-  for (int k = warp; k < nsmall; k += kWarps) {
-    const Task t = B.small[d.small_base + k];
-    buildSmall(B, d, S, t, warp, lane);
+  // the small tasks go to kBuildSmall, whose warps spread over every SM
+  if (tid == 0) {
+    B.nnodes[blockIdx.x] = (uint32_t)S.nnodes;
+    B.nsmall[blockIdx.x] = (uint32_t)S.nsmall;
+  }
+  (void)lane;
+  (void)warp;
+}
+
+// The small tasks of every domain of the batch, one warp per task, warps of
+// all CTAs pulling from one counter (`next`): a domain's subtrees are built
+// in parallel on every SM instead of by its one CTA.
+__global__ void __launch_bounds__(kThreads) kBuildSmall(Batch B, int nb, uint32_t* next) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Shared& S = *reinterpret_cast<Shared*>(smem);
+  uint32_t* prefix = reinterpret_cast<uint32_t*>(smem + sizeof(Shared));  // [nb + 1]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    uint32_t run = 0;
+    for (int d = 0; d < nb; ++d) {
+      prefix[d] = run;
+      run += B.nsmall[d];
+    }
+    prefix[nb] = run;
   }
   __syncthreads();
-  if (tid == 0) B.nnodes[blockIdx.x] = (uint32_t)S.nnodes;
+  const uint32_t total = prefix[nb];
+  while (true) {
+    uint32_t k = 0;
+    int stop = 0;
+    if (lane == 0) {
+      k = atomicAdd(next, 1u);
+      stop = *((volatile int*)B.error);
+    }
+    k = __shfl_sync(0xffffffffu, k, 0);
+    stop = __shfl_sync(0xffffffffu, stop, 0);
+    if (k >= total || stop) break;
+    // the domain of task k: last d with prefix[d] <= k
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (prefix[mid] <= k) lo = mid;
+      else hi = mid - 1;
+    }
+    const Dom d = B.doms[lo];
+    const Task t = B.small[d.small_base + (k - prefix[lo])];
+    buildSmall(B, d, S, t, warp, lane, &B.nnodes[lo]);
+  }
 }
 
 // 4-wide collapse, one warp per domain: a queue of (binary node, 4-wide
@@ -827,11 +872,19 @@ void buildBvhsOnDevice(const spray_gpu_domain* src, const std::vector<int>& whic
   size_t k = 0;
   const size_t smem = sharedBytes();
   CK(cudaFuncSetAttribute(kBuild, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int dev = 0, sms = 1;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int small_blocks = 4 * sms;
+  CK(cudaFuncSetAttribute(kBuildSmall, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)(smem + (kMaxBatchDomains + 1) * 4)));
   while (k < which.size()) {
     // the batch: consecutive domains up to batch_tris triangles (at least one)
     size_t j = k;
     uint64_t tris = 0, verts = 0;
-    while (j < which.size() && (j == k || tris + (uint64_t)src[which[j]].num_faces <= batch_tris)) {
+    // (at most kMaxBatchDomains domains: kBuildSmall keeps their prefix in shared memory)
+    while (j < which.size() && (j - k) < (size_t)kMaxBatchDomains &&
+           (j == k || tris + (uint64_t)src[which[j]].num_faces <= batch_tris)) {
       tris += (uint64_t)src[which[j]].num_faces;
       verts += (uint64_t)src[which[j]].num_vertices;
       ++j;
@@ -864,6 +917,8 @@ void buildBvhsOnDevice(const spray_gpu_domain* src, const std::vector<int>& whic
     CK(cudaMalloc(&B.depth, nb * 4));
     CK(cudaMalloc(&B.queue, (2 * tris + 4 * nb) * sizeof(int2)));
     CK(cudaMalloc(&B.error, 4));
+    uint32_t* small_next = nullptr;
+    CK(cudaMalloc(&small_next, 4));
     CK(cudaMalloc(&dtris, 3 * tris * sizeof(float4)));
     CK(cudaMemsetAsync(B.error, 0, 4, stream));
     uint64_t vo = 0, fo = 0, so = 0, oo = 0;
@@ -889,6 +944,8 @@ void buildBvhsOnDevice(const spray_gpu_domain* src, const std::vector<int>& whic
     const int gx = 64;
     kPrep<<<dim3(gx, nb), 256, 0, stream>>>(B, nb);
     kBuild<<<nb, kThreads, smem, stream>>>(B);
+    CK(cudaMemsetAsync(small_next, 0, 4, stream));
+    kBuildSmall<<<small_blocks, kThreads, smem + (nb + 1) * 4, stream>>>(B, nb, small_next);
     kCollapse<<<nb, 32, 0, stream>>>(B);
     kFinish<<<dim3(gx, nb), 256, 0, stream>>>(B);
     kTris<<<dim3(gx, nb), 256, 0, stream>>>(B, dtris);
@@ -916,7 +973,7 @@ void buildBvhsOnDevice(const spray_gpu_domain* src, const std::vector<int>& whic
     for (void* ptr : {(void*)dv, (void*)df, (void*)ddoms, (void*)B.tlo, (void*)B.thi, (void*)B.cen,
                       (void*)B.idx[0], (void*)B.idx[1], (void*)B.order, (void*)B.nodes, (void*)B.small,
                       (void*)B.nnodes, (void*)B.nsmall, (void*)B.out, (void*)B.nout, (void*)B.depth,
-                      (void*)B.queue, (void*)B.error, (void*)dtris})
+                      (void*)B.queue, (void*)B.error, (void*)dtris, (void*)small_next})
       cudaFree(ptr);
     if (err) throw std::runtime_error("device BVH build ran out of room (error flags " + std::to_string(err) + ")");
     k = j;
