@@ -182,6 +182,7 @@ struct SchedArgs {
   uint64_t* ray_key;          // radiance: reset to kNoHit per scheduled ray
   const BvhNode4* dnodes;     // 4-wide hierarchy over the domain boxes (null: test every domain)
   int dnode_count;
+  const float* dboxes;        // domain boxes, 6 floats each (null: staged from the domain table)
   // primary rays: candidate domains per screen bin (null: not primary rays)
   const uint32_t* bin_start;  // [bins_x * bins_y + 1]
   const uint16_t* bin_ids;

@@ -100,26 +100,35 @@ __device__ __forceinline__ bool fitsList(int cnt, int j) { return j < cnt; }
 // kMinBlocks 6 caps the kernel at 40 registers (a few spills) so that six
 // blocks fit an SM when shared memory allows; with larger domain tables
 // shared memory holds fewer blocks and the variant for five (46 registers,
-// no spills) runs instead.
-template <int kMinBlocks>
+// no spills) runs instead.  kSharedTables: the domain boxes and the domain
+// hierarchy are staged in shared memory (small tables); otherwise they are
+// read through the read-only cache, which leaves the shared memory to the
+// per-warp histograms (512 domains: 34 KB of tables per block would hold the
+// kernel at two blocks per SM).
+template <int kMinBlocks, bool kSharedTables>
 __global__ void __launch_bounds__(kSchedThreads, kMinBlocks) kSchedLists(SchedArgs a,
                                                              const DomainDev* __restrict__ doms,
                                                              int D, int nkeys, int nwarps) {
   extern __shared__ uint32_t smem[];
   const int NN = a.dnode_count;
-  float4* snode = reinterpret_cast<float4*>(smem);  // 8 float4 per hierarchy node (BvhNode4)
-  float* sbox = reinterpret_cast<float*>(smem + 32 * NN);
-  uint32_t* hist = smem + 32 * NN + 6 * D;  // per warp: nkeys 16-bit counters, packed in pairs
+  const int table_words = kSharedTables ? 32 * NN + 6 * D : 0;
+  float4* stage_node = reinterpret_cast<float4*>(smem);  // 8 float4 per hierarchy node (BvhNode4)
+  float* stage_box = reinterpret_cast<float*>(smem + 32 * NN);
+  const float4* snode = kSharedTables ? stage_node : reinterpret_cast<const float4*>(a.dnodes);
+  const float* sbox = kSharedTables ? stage_box : a.dboxes;
+  uint32_t* hist = smem + table_words;  // per warp: nkeys 16-bit counters, packed in pairs
   const int hwords = (nkeys + 1) >> 1;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int d = threadIdx.x; d < D; d += blockDim.x) {
-    for (int c = 0; c < 3; ++c) {
-      sbox[6 * d + c] = doms[d].bmin[c];
-      sbox[6 * d + 3 + c] = doms[d].bmax[c];
+  if (kSharedTables) {
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+      for (int c = 0; c < 3; ++c) {
+        stage_box[6 * d + c] = doms[d].bmin[c];
+        stage_box[6 * d + 3 + c] = doms[d].bmax[c];
+      }
     }
+    for (int k = threadIdx.x; k < 8 * NN; k += blockDim.x)
+      stage_node[k] = reinterpret_cast<const float4*>(a.dnodes)[k];
   }
-  for (int k = threadIdx.x; k < 8 * NN; k += blockDim.x)
-    snode[k] = reinterpret_cast<const float4*>(a.dnodes)[k];
   uint32_t* h = hist + (size_t)wib * hwords;
   __syncthreads();
   const uint32_t n = *a.count;
@@ -617,43 +626,66 @@ __global__ void __launch_bounds__(128) kSchedHist(SchedArgs a, int D, int nkeys,
   }
 }
 
-static size_t listsSmem(int D, int nkeys, int dnode_count) {
-  return (size_t)dnode_count * 128 + (size_t)6 * D * 4 + (size_t)(kSchedThreads / 32) * ((nkeys + 1) / 2) * 4;
+// Domain tables up to this size are staged in shared memory by kSchedLists.
+constexpr size_t kSharedTableBytes = 8192;
+
+static bool tablesShared(int D, int dnode_count) {
+  return (size_t)dnode_count * 128 + (size_t)6 * D * 4 <= kSharedTableBytes;
+}
+
+static size_t listsSmem(int D, int nkeys, int dnode_count, bool shared_tables) {
+  return (shared_tables ? (size_t)dnode_count * 128 + (size_t)6 * D * 4 : 0) +
+         (size_t)(kSchedThreads / 32) * ((nkeys + 1) / 2) * 4;
 }
 
 // Resident blocks per SM of a kSchedLists variant with this shared memory.
-template <int kMinBlocks>
+template <int kMinBlocks, bool kShared>
 static int listsOccupancy(size_t smem) {
-  cudaFuncSetAttribute(kSchedLists<kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(kSchedLists<kMinBlocks, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int bps = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kSchedLists<kMinBlocks>, kSchedThreads, smem) !=
-          cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kSchedLists<kMinBlocks, kShared>, kSchedThreads,
+                                                    smem) != cudaSuccess ||
       bps < 1)
     bps = 1;
   return bps;
 }
 
 // The register-capped variant when shared memory lets six blocks share an SM.
-static bool listsCapped(size_t smem) { return listsOccupancy<6>(smem) >= 6; }
+template <bool kShared>
+static bool listsCapped(size_t smem) { return listsOccupancy<6, kShared>(smem) >= 6; }
+
+template <bool kShared>
+static int blocksFor(size_t smem) {
+  return listsCapped<kShared>(smem) ? listsOccupancy<6, kShared>(smem) : listsOccupancy<5, kShared>(smem);
+}
 
 int schedBlocksPerSm(int D, int nkeys, int dnode_count) {
-  const size_t smem = listsSmem(D, nkeys, dnode_count);
-  return listsCapped(smem) ? listsOccupancy<6>(smem) : listsOccupancy<5>(smem);
+  const bool shared = tablesShared(D, dnode_count);
+  const size_t smem = listsSmem(D, nkeys, dnode_count, shared);
+  return shared ? blocksFor<true>(smem) : blocksFor<false>(smem);
+}
+
+template <bool kShared>
+static void launchLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
+                        int nblocks) {
+  const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
+  // the variant is chosen for the allocation's key count (4 D), as in schedBlocksPerSm
+  const bool capped = listsCapped<kShared>(listsSmem(D, kDepthBuckets * D, a.dnode_count, kShared));
+  const size_t smem1 = listsSmem(D, nkeys, a.dnode_count, kShared);
+  if (capped) {
+    cudaFuncSetAttribute(kSchedLists<6, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    kSchedLists<6, kShared><<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
+  } else {
+    cudaFuncSetAttribute(kSchedLists<5, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    kSchedLists<5, kShared><<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
+  }
 }
 
 void launchSchedLists(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,
                       int nblocks) {
-  const int nkeys = a.order_by_depth ? kDepthBuckets * D : D;
-  // the variant is chosen for the allocation's key count (4 D), as in schedBlocksPerSm
-  const bool capped = listsCapped(listsSmem(D, kDepthBuckets * D, a.dnode_count));
-  const size_t smem1 = listsSmem(D, nkeys, a.dnode_count);
-  if (capped) {
-    cudaFuncSetAttribute(kSchedLists<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-    kSchedLists<6><<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
-  } else {
-    cudaFuncSetAttribute(kSchedLists<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-    kSchedLists<5><<<nblocks, kSchedThreads, smem1, s>>>(a, domains, D, nkeys, nwarps);
-  }
+  // without a box array (the allocation-free entry point) the tables are staged
+  if (!a.dboxes || tablesShared(D, a.dnode_count)) launchLists<true>(s, a, domains, D, nwarps, nblocks);
+  else launchLists<false>(s, a, domains, D, nwarps, nblocks);
 }
 
 void launchSchedule(cudaStream_t s, const SchedArgs& a, const DomainDev* domains, int D, int nwarps,

@@ -366,6 +366,7 @@ void Tracer::freeScene() {
   ooc = false;
   devFree(d_segs);
   devFree(d_dnodes);
+  devFree(d_dboxes);
   dnode_count = 0;
   devFree(d_bin_start);
   devFree(d_bin_ids);
@@ -640,13 +641,15 @@ void Tracer::installScene(std::vector<DomainPack>& packs, const spray_gpu_light*
   // hierarchy over the domain boxes for the scheduler (all domains are tested
   // directly when there are few)
   dnode_count = 0;
+  std::vector<float> boxes(6 * (size_t)nd);
+  for (int d = 0; d < nd; ++d)
+    for (int c = 0; c < 3; ++c) {
+      boxes[6 * d + c] = hdoms[d].bmin[c];
+      boxes[6 * d + 3 + c] = hdoms[d].bmax[c];
+    }
+  devAlloc(&d_dboxes, boxes.size());
+  CK(cudaMemcpy(d_dboxes, boxes.data(), boxes.size() * 4, cudaMemcpyHostToDevice));
   if (nd >= kDomainBvhMin) {
-    std::vector<float> boxes(6 * (size_t)nd);
-    for (int d = 0; d < nd; ++d)
-      for (int c = 0; c < 3; ++c) {
-        boxes[6 * d + c] = hdoms[d].bmin[c];
-        boxes[6 * d + 3 + c] = hdoms[d].bmax[c];
-      }
     std::vector<BvhNode4> dn;
     buildDomainBvh4(boxes.data(), nd, &dn);
     dnode_count = (int)dn.size();
@@ -1078,6 +1081,7 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.list_size = cfg.list_size;
   a.ray_key = d_ray_key;
   a.dnodes = d_dnodes;
+  a.dboxes = d_dboxes;
   a.dnode_count = dnode_count;
   if (primary && use_bins && fviews.size() == 1) {
     a.bin_start = d_bin_start;

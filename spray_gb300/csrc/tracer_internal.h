@@ -238,6 +238,7 @@ class Tracer {
   char* h_stage = nullptr;        // pinned staging of the domain and segment tables
   uint32_t* d_segs = nullptr;
   BvhNode4* d_dnodes = nullptr;  // 4-wide hierarchy over the domain boxes
+  float* d_dboxes = nullptr;     // domain boxes for the scheduler, 6 floats each
   int dnode_count = 0;
   // screen bins of candidate domains for the primary rays
   static constexpr int kBinShift = 4;
