@@ -84,8 +84,14 @@ typedef struct spray_gpu_config {
                                    more predicted hits go first; 4 non-speculative: the
                                    LoadAnyOnce baseline (src/baseline/baseline_schedulers.cc) --
                                    one pass per list position, a ray waits only in the queue of its
-                                   next domain, domains with the most pending rays first.  Images
-                                   are unchanged (0) */
+                                   next domain, domains with the most pending rays first;
+                                   5 non-speculative rounds: the reference's baseline image tracer
+                                   itself (src/baseline/baseline_image_tracer.inl:28-131), in core
+                                   or out of core -- each round runs the one domain holding the
+                                   most queued rays (LoadAnyOnceImageSched), a ray moves on to its
+                                   next domain only when no hit lies in front of it, the rays a
+                                   hit spawns run in that domain first; whole image on one rank,
+                                   one view.  Images are unchanged (0) */
   int32_t ooc_batch;            /* out-of-core, policy 2: domains made resident per traced batch,
                                    at most half the cache capacity so that the next batch's copies
                                    overlap this batch's traces; 0 = half the capacity (0) */
@@ -206,6 +212,8 @@ typedef struct spray_gpu_stats {
   double learn_top1_nearest;/* policy 3: share whose hit is in the nearest candidate (the
                                front-to-back order's guess) */
   int64_t exchange_bytes;   /* domain-parallel: bytes this rank passed to the reductions */
+  int64_t rounds;           /* policy 5: rounds (domains run, one per round) */
+  int64_t visits_shade;     /* policy 5: rays run in the domain of their hit for shading only */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

@@ -10,6 +10,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <deque>
 #include <limits>
 #include <list>
 #include <map>
@@ -933,6 +934,10 @@ struct Oracle {
 
   // ------------------------------------------------------------ mode A
   void renderSpeculative(int nthreads, float* rgba, orc_stats* st);
+
+  // ------------------------------------------------------------ mode C
+  void renderBaseline(float* rgba, orc_stats* st, std::vector<int>* schedule);
+  std::vector<int> baseline_schedule;  // the domains of the last mode C frame, one per round
 };
 
 // =================================================================== mode A
@@ -1486,6 +1491,248 @@ void Oracle::renderSpeculative(int T, float* rgba, orc_stats* out) {
   if (out) *out = s;
 }
 
+// =================================================================== mode C
+// The reference's non-speculative image tracer on one process:
+//   baseline::ImageTracer::trace (src/baseline/baseline_image_tracer.inl:28-131):
+//     all eye rays queued in their first domain, then rounds until every
+//     queue is empty; each round takes one domain from the scheduler, loads
+//     it, runs its shadow queue, its radiance queue and the rays its shaders
+//     spawned (temp_q), and adds the round's retired contributions;
+//   ImageTracer::schedule (baseline_image_tracer.inl:134-157): the count of a
+//     domain is its radiance plus shadow queue length;
+//   LoadAnyOnceSched::scheduleImage (baseline_schedulers.cc:43-62);
+//   InsituTracer::genEyeRays, isectEyeDomains, processRays, processShadow,
+//     processRay2 (baseline_insitu_tracer.inl:407-497, 545-766);
+//   DomainIntersector::intersect (baseline_isector.h:44-98);
+//   baseline::ShaderPt / ShaderAo (baseline_shader_pt.h:55-196,
+//     baseline_shader_ao.h:54-98): the light and bounce samples and their
+//     seeds are the speculative shaders', so Oracle::shade computes them; the
+//     shadow ray is tested in the shading domain when it is made.
+// One thread: what a round queues follows from each ray's own state, so the
+// per-domain counts that drive the schedule do not depend on the order in
+// which the round's rays run; only the order of the image additions does.
+
+// LoadAnyOnceSched::scheduleImage: the domain with the most queued rays;
+// equal counts stay in the order std::sort leaves them (ids ascending in).
+int loadAnyOnceSchedule(int nd, const int64_t* counts, bool* done) {
+  std::vector<std::pair<int, int64_t>> rc(nd);
+  for (int i = 0; i < nd; ++i) rc[i] = {i, counts[i]};
+  std::sort(rc.begin(), rc.end(),
+            [](const std::pair<int, int64_t>& a, const std::pair<int, int64_t>& b) { return a.second > b.second; });
+  *done = rc[0].second == 0;
+  return rc[0].first;
+}
+
+namespace {
+constexpr int kNone = std::numeric_limits<int>::max();  // INT_MAX in the reference's DRay
+
+struct BRay {  // baseline::DRay (baseline_ray.h) with the hit it carries
+  F3 org, dir, w;
+  int pixid, samid, depth;
+  float t;           // closest hit so far
+  int domid;         // its domain, kNone without one
+  Hit hit;
+  bool shade_only;   // DRAY_FLAG_SHADE: queued back to domid for shading
+  int domain_pos;    // position in the ray's domain list, kNone when not traversing
+  float next_tdom;   // entry distance of the domain after domain_pos
+  float tmax;        // occlusion range of shadow rays (infinite in the reference)
+};
+
+struct Commit {  // CommitB (baseline_commit_buffer.h)
+  int pixid;
+  F3 rgb;
+};
+}  // namespace
+
+void Oracle::renderBaseline(float* rgba, orc_stats* out, std::vector<int>* schedule) {
+  if (cfg.num_ranks != 1) throw std::invalid_argument("the baseline loop runs on one process");
+  const int W = cfg.image_w, H = cfg.image_h, spp = cfg.pixel_samples, nd = D();
+  std::fill(rgba, rgba + (size_t)W * H * 4, 0.0f);
+  orc_stats s{};
+  std::vector<BRay> rays;
+  std::vector<std::vector<int>> qs(nd), sqs(nd);
+  std::deque<int> temp_q;
+  std::vector<Commit> commits;
+  std::vector<std::pair<float, int>> list;
+
+  // DomainIntersector::intersect: advance the ray to the next domain of its
+  // list (a new ray starts past the current domain when that domain is the
+  // list's first) and queue it there; kNone when the list is exhausted
+  auto advance = [&](int current, int idx, std::vector<std::vector<int>>* q) {
+    BRay& r = rays[idx];
+    domainList(r.org, r.dir, r.tmax, &list);
+    const int n = (int)list.size();
+    if (r.domain_pos < kNone) r.domain_pos += 1;
+    else r.domain_pos = (n && list[0].second == current) ? 1 : 0;
+    if (r.domain_pos < n) {
+      r.next_tdom = r.domain_pos + 1 < n ? list[r.domain_pos + 1].first : kInf;
+      if (q) (*q)[list[r.domain_pos].second].push_back(idx);
+    } else {
+      r.domain_pos = kNone;
+      r.next_tdom = kInf;
+    }
+  };
+
+  // the shader of a hit in domain id: shadow rays tested here first, then
+  // queued in their next domain or retired; the bounce ray joins temp_q
+  auto shadeHit = [&](int id, int idx, const Hit& h) {
+    const BRay r = rays[idx];
+    uint32_t color;
+    F3 ns;
+    shadingAttributes(doms[id], h, &color, &ns);
+    std::vector<ShadowOut> sh;
+    BounceOut bo;
+    F3 pos;
+    shade(r.depth + 1, r.org, r.dir, r.w, r.pixid, r.samid, h.t, id, color, ns, &sh, &bo, &pos);
+    for (const ShadowOut& so : sh) {
+      if (!so.valid) continue;
+      ++s.rays_shadow;
+      ++s.visits_shadow;
+      if (occludedInDomain(doms[id], pos, so.dir, so.tmax)) continue;
+      BRay sr{};
+      sr.org = pos;
+      sr.dir = so.dir;
+      sr.w = so.w;
+      sr.pixid = r.pixid;
+      sr.samid = r.samid;
+      sr.depth = r.depth + 1;
+      sr.t = kInf;
+      sr.domid = kNone;
+      sr.domain_pos = kNone;
+      sr.next_tdom = kInf;
+      sr.tmax = so.tmax;
+      rays.push_back(sr);
+      const int si = (int)rays.size() - 1;
+      advance(id, si, &sqs);
+      if (rays[si].domain_pos == kNone) commits.push_back({r.pixid, so.w});
+    }
+    if (bo.valid) {
+      ++s.rays_bounce;
+      BRay br{};
+      br.org = pos;
+      br.dir = bo.dir;
+      br.w = bo.w;
+      br.pixid = r.pixid;
+      br.samid = r.samid;
+      br.depth = r.depth + 1;
+      br.t = kInf;
+      br.domid = kNone;
+      br.domain_pos = kNone;
+      br.next_tdom = kInf;
+      br.tmax = kInf;
+      rays.push_back(br);
+      temp_q.push_back((int)rays.size() - 1);
+    }
+  };
+
+  // processShadow: not occluded here -> next domain, or retired at the end
+  auto processShadow = [&](int id, int idx) {
+    ++s.visits_shadow;
+    const BRay& r = rays[idx];
+    if (occludedInDomain(doms[id], r.org, r.dir, r.tmax)) return;
+    advance(id, idx, &sqs);
+    if (rays[idx].domain_pos == kNone) commits.push_back({rays[idx].pixid, rays[idx].w});
+  };
+
+  // processRay2: shade a hit that is known to be the closest, move on, or
+  // send the ray back to the domain of its closest hit for shading
+  auto processRay = [&](int id, int idx) {
+    BRay& r = rays[idx];
+    if (r.shade_only) {
+      ++s.visits_shade;
+      shadeHit(id, idx, r.hit);
+      return;
+    }
+    ++s.visits_radiance;
+    Hit h;
+    if (closestInDomain(doms[id], r.org, r.dir, &h)) {
+      if (h.t < r.t) {
+        r.t = h.t;
+        r.domid = id;
+        r.hit = h;
+        if (std::isinf(r.next_tdom) || r.t < r.next_tdom) shadeHit(id, idx, h);
+        else advance(id, idx, &qs);
+      } else {
+        r.shade_only = true;
+        qs[r.domid].push_back(idx);
+      }
+    } else if (std::isinf(r.next_tdom)) {
+      if (r.domid < nd) {
+        r.shade_only = true;
+        qs[r.domid].push_back(idx);
+      }
+    } else {
+      advance(id, idx, &qs);
+    }
+  };
+
+  // genEyeRays + isectEyeDomains over the single tile of the image (ImgSchedNop)
+  rays.reserve((size_t)W * H * spp);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x)
+      for (int k = 0; k < spp; ++k) {
+        BRay r{};
+        const int pixid = y * W + x;
+        r.pixid = pixid;
+        r.org = cam_pos;
+        if (spp > 1) {
+          r.samid = spp * pixid + k;
+          RandomSampler rs;
+          samplerInit(rs, r.samid);
+          float fx = (float)x + samplerGet1D(rs);
+          float fy = (float)y + samplerGet1D(rs);
+          r.dir = generateRay(fx, fy);
+        } else {
+          r.samid = pixid;
+          r.dir = generateRay((float)x, (float)y);
+        }
+        r.w = f3(1.f, 1.f, 1.f);
+        r.t = kInf;
+        r.domid = kNone;
+        r.tmax = kInf;
+        r.next_tdom = kInf;
+        rays.push_back(r);
+        const int idx = (int)rays.size() - 1;
+        domainList(r.org, r.dir, kInf, &list);
+        if (!list.empty()) {
+          rays[idx].domain_pos = 0;
+          rays[idx].next_tdom = list.size() > 1 ? list[1].first : kInf;
+          qs[list[0].second].push_back(idx);
+        } else {
+          rays[idx].domain_pos = kNone;
+        }
+      }
+  s.rays_primary = (int64_t)rays.size();
+
+  LruCache cache;
+  cache.init(nd, cfg.cache_size);
+  std::vector<int64_t> counts(nd);
+  const double scale = 1.0 / (double)spp;
+  while (true) {
+    for (int i = 0; i < nd; ++i) counts[i] = (int64_t)qs[i].size() + (int64_t)sqs[i].size();
+    bool done;
+    const int id = loadAnyOnceSchedule(nd, counts.data(), &done);
+    if (done) break;
+    ++s.rounds;
+    if (schedule) schedule->push_back(id);
+    if (!cache.load(id)) ++s.domain_loads;
+    std::vector<int> shadows, radiance;
+    shadows.swap(sqs[id]);
+    radiance.swap(qs[id]);
+    for (int idx : shadows) processShadow(id, idx);
+    for (int idx : radiance) processRay(id, idx);
+    while (!temp_q.empty()) {
+      const int idx = temp_q.front();
+      temp_q.pop_front();
+      advance(kNone, idx, nullptr);  // list position only; the ray runs here first
+      processRay(id, idx);
+    }
+    for (const Commit& c : commits) hdrAdd(rgba + 4 * (size_t)c.pixid, c.rgb, scale);
+    commits.clear();
+  }
+  if (out) *out = s;
+}
+
 }  // namespace orc
 
 // =================================================================== C API
@@ -1975,6 +2222,31 @@ int orc_render_wavefront(void* ov, float* rgba, orc_stats* st) {
   } catch (const std::exception&) {
     return 1;
   }
+}
+
+int orc_render_baseline(void* ov, float* rgba, orc_stats* st) {
+  try {
+    Oracle* o = (Oracle*)ov;
+    o->baseline_schedule.clear();
+    o->renderBaseline(rgba, st, &o->baseline_schedule);
+    return 0;
+  } catch (const std::exception&) {
+    return 1;
+  }
+}
+
+int64_t orc_baseline_schedule(void* ov, int32_t* out, int64_t capacity) {
+  const std::vector<int>& s = ((Oracle*)ov)->baseline_schedule;
+  if (out) std::copy(s.begin(), s.begin() + std::min<int64_t>(capacity, (int64_t)s.size()), out);
+  return (int64_t)s.size();
+}
+
+int orc_load_any_once(int32_t nd, const int64_t* counts, int32_t* id, uint8_t* done) {
+  if (nd <= 0 || !counts || !id || !done) return 1;
+  bool d;
+  *id = orc::loadAnyOnceSchedule(nd, counts, &d);
+  *done = d ? 1 : 0;
+  return 0;
 }
 
 int orc_render_speculative(void* ov, int32_t nthreads, float* rgba, orc_stats* st) {

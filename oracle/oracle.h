@@ -17,12 +17,16 @@
  * published watertight triangle test (Woop, Benthin, Wald, JCGT 2013) for
  * Embree.
  *
- * Two modes:
+ * Three modes:
  *   A  orc_render_speculative: the reference's loop itself -- per-thread
  *      queues, DomainStats score order, VBuf speculation history, pending
  *      queue, LRU/infinite domain cache, OpenMP threads with the same barriers.
  *   B  stage functions (eye rays, scheduling, closest hit, shading, occlusion)
  *      and orc_render_wavefront, which applies them bounce by bounce.
+ *   C  orc_render_baseline: the reference's non-speculative image tracer
+ *      (src/baseline/): one domain per round, the one with the most queued
+ *      rays (LoadAnyOnceImageSched), each ray moving on to its next domain
+ *      only when no hit lies in front of it.
  */
 #ifndef SPRAY_ORACLE_H_
 #define SPRAY_ORACLE_H_
@@ -55,6 +59,7 @@ typedef struct orc_stats {
   int64_t visits_radiance, visits_shadow;
   int64_t domain_loads;
   int64_t rounds;
+  int64_t visits_shade;  /* mode C: rays sent back to the domain of their hit for shading */
 } orc_stats;
 
 void* orc_create(const orc_config* cfg, int32_t num_domains);
@@ -160,6 +165,18 @@ int orc_hdr_add(int64_t n, const int32_t* pixid, const float* rgb, double scale,
 /* Full frames: W*H*4 floats. */
 int orc_render_wavefront(void* o, float* rgba, orc_stats* stats);
 int orc_render_speculative(void* o, int32_t nthreads, float* rgba, orc_stats* stats);
+/* Mode C (one process).  visits_radiance counts closest-hit tests in a
+ * domain, visits_shadow occlusion tests (including the one in the shading
+ * domain), visits_shade the shading-only visits; rounds is the number of
+ * scheduled domains; domain_loads the misses of an LRU of cache_size domains
+ * over that sequence, from an empty cache. */
+int orc_render_baseline(void* o, float* rgba, orc_stats* stats);
+/* the domain of every round of the last orc_render_baseline frame: copies
+ * min(capacity, rounds) ids, returns rounds */
+int64_t orc_baseline_schedule(void* o, int32_t* out, int64_t capacity);
+/* LoadAnyOnceSched::scheduleImage on per-domain queue counts: the domain to
+ * process next and whether every count is zero */
+int orc_load_any_once(int32_t num_domains, const int64_t* counts, int32_t* id, uint8_t* done);
 
 #ifdef __cplusplus
 }

@@ -53,7 +53,7 @@ class OrcConfig(C.Structure):
 class OrcStats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("rays_primary", "rays_shadow", "rays_bounce",
                                          "visits_radiance", "visits_shadow", "domain_loads",
-                                         "rounds")]
+                                         "rounds", "visits_shade")]
 
     def asdict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -102,6 +102,10 @@ def lib() -> C.CDLL:
         L.orc_mesh_attributes.argtypes = [P, C.c_int64, P, C.c_int64, P, C.c_int64, P, P, P, P, P, P]
         L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
         L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
+        L.orc_render_baseline.argtypes = [P, P, C.POINTER(OrcStats)]
+        L.orc_baseline_schedule.argtypes = [P, P, C.c_int64]
+        L.orc_baseline_schedule.restype = C.c_int64
+        L.orc_load_any_once.argtypes = [C.c_int32, P, P, P]
         _lib = L
     return _lib
 
@@ -159,6 +163,16 @@ def lru_trace(num_domains: int, cache_size: int, ids, with_evicted: bool = False
     ev = np.zeros(len(ids), np.int32)
     lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits), _p(ev))
     return (hits, ev) if with_evicted else hits
+
+
+def load_any_once(counts) -> tuple[int, bool]:
+    """LoadAnyOnceSched::scheduleImage on per-domain queue counts: the domain
+    processed next, and whether every queue is empty."""
+    counts = np.ascontiguousarray(counts, np.int64)
+    i, d = C.c_int32(0), C.c_uint8(0)
+    if lib().orc_load_any_once(len(counts), _p(counts), C.byref(i), C.byref(d)) != 0:
+        raise ValueError("empty domain count array")
+    return int(i.value), bool(d.value)
 
 
 def domain_list_sort(ids, ts) -> tuple[np.ndarray, np.ndarray]:
@@ -425,6 +439,19 @@ class Oracle:
         if self.L.orc_render_wavefront(self.h, _p(img), C.byref(st)) != 0:
             raise RuntimeError("oracle wavefront render failed")
         return img, st.asdict()
+
+    def render_baseline(self):
+        """Mode C, the reference's non-speculative image tracer on one
+        process: the image, the stats and the domain scheduled in every
+        round."""
+        img = self._image()
+        st = OrcStats()
+        if self.L.orc_render_baseline(self.h, _p(img), C.byref(st)) != 0:
+            raise RuntimeError("oracle baseline render failed")
+        n = self.L.orc_baseline_schedule(self.h, None, 0)
+        sched = np.zeros(n, np.int32)
+        self.L.orc_baseline_schedule(self.h, _p(sched), n)
+        return img, st.asdict(), sched
 
     def render_speculative(self, nthreads=1):
         img = self._image()

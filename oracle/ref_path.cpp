@@ -36,6 +36,9 @@
 #include "utils/util.h"
 #include "render/rays.h"
 #include "render/trimesh_buffer.h"
+#include "render/data_partition.h"
+#include "baseline/baseline_qstats.h"
+#include "baseline/baseline_schedulers.h"
 
 namespace spray {
 Aabb::Aabb() {}
@@ -43,6 +46,10 @@ Aabb::Aabb() {}
 // programs): one process, rank 0.
 MpiComm global_mpi_comm;
 }  // namespace spray
+
+// LoadAnyOnceSched::scheduleMulti (baseline_schedulers.cc) sums counts over
+// processes; with one process it is never called.
+extern "C" int MPI_Allreduce(const void*, void*, int, MPI_Datatype, MPI_Op, MPI_Comm) { return 1; }
 
 using namespace spray;
 
@@ -208,6 +215,25 @@ int32_t ref_tiles(int64_t image_w, int64_t image_h, int64_t spp, int64_t num_ran
     }
   }
   return n;
+}
+
+// LoadAnyOnceImageSched::init + schedule (baseline/baseline_schedulers.cc:31-62)
+// on one round's per-domain queue counts: the domain processed next and
+// whether the frame is done.
+int ref_load_any_once(int32_t num_domains, const int64_t* counts, int32_t* id, uint8_t* done) {
+  global_mpi_comm.size = 1;
+  global_mpi_comm.rank = 0;
+  baseline::QStats stats;
+  stats.init(num_domains);
+  for (int32_t d = 0; d < num_domains; ++d) stats.set(d, counts[d]);
+  InsituPartition partition;
+  baseline::LoadAnyOnceImageSched sched;
+  sched.init(num_domains, partition);
+  sched.schedule(stats);
+  int out = -1;
+  *done = sched.getSchedule(&out) ? 1 : 0;
+  *id = out;
+  return 0;
 }
 
 // DomainStats::resize + increment + schedule (ooc/ooc_domain_stats.cc:34-111)

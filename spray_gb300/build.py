@@ -21,7 +21,7 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["sched.cu", "trace.cu", "shade.cu", "tracer.cu", "insitu.cu", "bvh_build.cu", "noalloc.cu",
-              "mlp.cu", "mlp_api.cu"]
+              "rounds.cu", "mlp.cu", "mlp_api.cu"]
 CPP_SOURCES = ["bvh.cpp", "host_scene.cpp", "host_api.cpp"]
 
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall",

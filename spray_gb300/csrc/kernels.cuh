@@ -63,6 +63,7 @@ struct DomainDev {
 constexpr unsigned long long kErrGlassBothLobes = 1ull;  // glass hit needing two rays
 constexpr unsigned long long kErrBadNode = 2ull;         // node or leaf index out of range
 constexpr unsigned long long kErrTraversalBound = 4ull;  // traversal exceeded its step bound
+constexpr unsigned long long kErrRetireContention = 8ull;  // an image addition lost its race too often
 
 struct SceneDev {
   const DomainDev* domains;

@@ -32,18 +32,6 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-template <class T>
-static void devAlloc(T** p, size_t n) {
-  *p = nullptr;
-  if (n == 0) n = 1;
-  CK(cudaMalloc((void**)p, n * sizeof(T)));
-}
-template <class T>
-static void devFree(T*& p) {
-  if (p) cudaFree(p);
-  p = nullptr;
-}
-
 // ---------------------------------------------------------------- tiles
 // ImageScheduleTileList::init (src/render/tile.cc:317-391) on the vertical
 // stripe of this rank (makeVerticalStripe, tile.cc:214-235).
@@ -309,8 +297,10 @@ Tracer::Tracer(const spray_gpu_config& c) : cfg(c) {
   if (cfg.max_samples_per_rank <= 0) throw std::invalid_argument("max_samples_per_rank must be positive");
   if (cfg.num_ranks <= 0 || cfg.rank < 0 || cfg.rank >= cfg.num_ranks)
     throw std::invalid_argument("rank must be in [0, num_ranks)");
-  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 4)
-    throw std::invalid_argument("schedule_policy must be 0, 1, 2, 3 or 4");
+  if (cfg.schedule_policy < 0 || cfg.schedule_policy > 5)
+    throw std::invalid_argument("schedule_policy must be 0, 1, 2, 3, 4 or 5");
+  if (cfg.schedule_policy == 5 && cfg.num_ranks != 1)
+    throw std::invalid_argument("schedule_policy 5 traces the whole image on one rank");
   if (cfg.schedule_policy == 3 &&
       (cfg.learn_samples < 0 || cfg.learn_batch <= 0 || cfg.learn_epochs < 0 || !(cfg.learn_lr > 0.0f) ||
        cfg.learn_frames < 1))
@@ -367,6 +357,7 @@ void Tracer::freeScene() {
   devFree(d_segs);
   devFree(d_dnodes);
   devFree(d_dboxes);
+  freeRounds();  // sized by the domain count
   dnode_count = 0;
   devFree(d_bin_start);
   devFree(d_bin_ids);
@@ -2042,6 +2033,8 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     dbg.clear();
     dbg[{SPRAY_DBG_LOADS, 0}];  // the request log exists for every frame (empty in core)
     load_pass = 0;
+    rounds = 0;
+    visits_shade = 0;
     use_pred_order = false;
     CK(cudaEventRecord(ev_start, stream));
     if (use_bins && fviews.size() == 1) buildScreenBins();
@@ -2049,7 +2042,7 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     CK(cudaMemcpyAsync(d_tiles, wave_tiles.data(), wave_tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice,
                        stream));
     h2d_bytes += hviews.size() * sizeof(ViewDev) + wave_tiles.size() * sizeof(TileDev);
-    const bool graphed = cfg.graphs && !ooc && !cfg.debug_capture && !learned() && !situ();
+    const bool graphed = cfg.graphs && !ooc && !cfg.debug_capture && !learned() && !situ() && !rounded();
     if (graphed) {
       if (!graph_exec || graph_gen != buf_gen) captureFrame();
       CK(cudaGraphLaunch(graph_exec, stream));
@@ -2060,11 +2053,15 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     } else {
       CK(cudaMemsetAsync(d_ctr, 0, sizeof(Counters), stream));
       CK(cudaMemsetAsync(d_image, 0, (size_t)frame_pixels * sizeof(float4), stream));
-      for (size_t k = 0; k < waves.size(); ++k) {
-        const bool capture = cfg.debug_capture && k == 0;
-        if (ooc && (cfg.schedule_policy == 2 || cfg.schedule_policy == 3) && !capture)
-        traceWaveBatched(waves[k]);
-        else traceWave(waves[k], capture);
+      if (rounded()) {
+        traceRounds();
+      } else {
+        for (size_t k = 0; k < waves.size(); ++k) {
+          const bool capture = cfg.debug_capture && k == 0;
+          if (ooc && (cfg.schedule_policy == 2 || cfg.schedule_policy == 3) && !capture)
+            traceWaveBatched(waves[k]);
+          else traceWave(waves[k], capture);
+        }
       }
     }
     CK(cudaEventRecord(ev_stop, stream));
@@ -2146,6 +2143,8 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->learn_top1 = learn_top1;
       st->learn_top1_nearest = learn_top1_nearest;
       st->exchange_bytes = reduce_bytes;
+      st->rounds = rounds;
+      st->visits_shade = visits_shade;
     }
     return;
   }

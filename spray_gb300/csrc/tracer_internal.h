@@ -81,6 +81,32 @@ struct DomainPack {
 };
 
 // Device slots of the out-of-core domain cache, least recently used first.
+// Device arrays of n elements (at least one), freed and nulled by devFree.
+template <class T>
+inline void devAlloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  CK(cudaMalloc((void**)p, n * sizeof(T)));
+}
+template <class T>
+inline void devFree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// Ray pool of the non-speculative round loop (rounds.cu), one entry per ray.
+struct RoundRays {
+  float4* org;  // xyz; w = occlusion range of a shadow ray (infinite for radiance)
+  float4* dir;  // xyz; w = entry distance of the domain after the current one
+  float4* wgt;  // rgb; w = t of the nearest hit so far
+  int4* meta;   // pixel, sample, depth | flags << 8, list position
+  int4* hit;    // domain of the nearest hit, its triangle (domain-local), u, v bits
+};
+
+// LoadAnyOnceSched::scheduleImage on per-domain queue counts (rounds.cu):
+// the domain to run next, -1 when every count is zero.
+int loadAnyOnceNext(const std::vector<int64_t>& counts);
+
 struct LruSlots {
   int capacity = 0;
   std::list<std::pair<int, int>> blocks;  // (slot, domain)
@@ -146,6 +172,8 @@ class Tracer {
                 bool primary = false, bool into_shadow_queues = false, bool predicted = false);
   // learned domain-order proposal (schedule_policy 3)
   bool learned() const { return cfg.schedule_policy == 3; }
+  // the non-speculative round loop (schedule_policy 5)
+  bool rounded() const { return cfg.schedule_policy == 5; }
   void setupProposal();
   void freeProposal();
   mlp::ArenaSource arenaSource() const;
@@ -185,6 +213,20 @@ class Tracer {
                int rb_count = -1, bool by_live = false);
   std::vector<int> residentFirst(const std::vector<int>& order) const;
   std::vector<int> scoreOrder();
+  // non-speculative round loop (schedule_policy 5, rounds.cu)
+  void traceRounds();
+  void ensureRounds(uint64_t pool, uint64_t arena, uint64_t segs);
+  void freeRounds();
+  RoundRays rr{};
+  unsigned long long* d_rr_pool = nullptr;  // [0]: ray count | round queue count << 32, [1]: shading-only visits
+  uint32_t* d_rr_arena = nullptr;           // queue entries (ray ids), grouped by domain per round
+  uint2* d_rr_out = nullptr;                // the round's queued rays: (domain, ray)
+  uint32_t* d_rr_hist = nullptr;            // per-domain counts of the round, total last
+  uint32_t* d_rr_cursor = nullptr;
+  uint32_t* d_rr_seg = nullptr;             // segment table of the round's domain
+  uint32_t* h_rr = nullptr;                 // pinned: segment table, then the round's counts
+  uint64_t rr_pool_cap = 0, rr_arena_cap = 0, rr_seg_cap = 0;
+  int64_t rounds = 0, visits_shade = 0;
 
   spray_gpu_config cfg;
   int num_sms = 0;

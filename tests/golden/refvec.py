@@ -38,6 +38,8 @@ ppm            HdrImage::writePpm, display/image.h:183-204         bytes (*)
 domain_list    DomainList::push/sort, render/rays.h:57-93           exact
 mesh           TriMeshBuffer::computeNormals/updateIntersection,    bit-exact
                render/trimesh_buffer.cc:267-360
+load_any_once  LoadAnyOnceSched::scheduleImage,                     exact
+               baseline/baseline_schedulers.cc:43-62
 ============== ==================================================== =========
 
 (*) ppm holds the product's writer (spray_gb300.image), not the oracle, to the
@@ -82,7 +84,7 @@ BLINN_REL = 1e-5
 
 GROUPS = ["rng", "slab", "camera", "disk", "local_to_world", "cosine", "diffuse_light", "point_light",
           "blinn_phong", "reflect", "fr_dielectric", "refract", "unpack", "lru", "tiles", "domain_order",
-          "vbuf", "hdr_add", "ppm", "domain_list", "mesh"]
+          "vbuf", "hdr_add", "ppm", "domain_list", "mesh", "load_any_once"]
 VBUF_SAMPLES, HISTORY = 8, 4  # SPRAY_SPECU_HISTORY_SIZE in the reference's CMake defaults
 HDR_W, HDR_H = 13, 7
 
@@ -292,6 +294,21 @@ def make_cases(seed: int = 2024, scale: int = 1) -> dict:
     vv = np.concatenate([np.tile(corners[:, 1], len(mf)), vv])
     c["mesh"] = {"vertices": mv, "faces": mf, "colors": (col[:, 0] << 16) | (col[:, 1] << 8) | col[:, 2],
                  "prim": prim, "u": uu, "v": vv, "corner_queries": np.array([k], np.int64)}
+
+    # one round's per-domain queue counts: 1 to 600 domains (std::sort's
+    # insertion-sort and introsort ranges), few distinct values so that the
+    # largest count is usually tied, and all-zero rounds (the frame is done)
+    nr = 300 * scale
+    nds = rng.integers(1, 601, nr)
+    nds[:4] = [1, 16, 17, 512]
+    counts = []
+    for k, n in enumerate(nds):
+        hi = int(rng.integers(1, 5)) if k % 3 else int(rng.integers(1, 10_000))
+        cnt = rng.integers(0, hi, n).astype(np.int64)
+        if k % 17 == 5:
+            cnt[:] = 0
+        counts.append(cnt)
+    c["load_any_once"] = {"ndomains": nds.astype(np.int32), "counts": np.concatenate(counts)}
     return c
 
 
@@ -465,6 +482,16 @@ def reference_outputs(cases: dict, libs) -> dict:
         off += int(n)
     out["domain_list"] = {"ids": oi, "ts": ot}
 
+    R.ref_load_any_once.argtypes = [C.c_int32, P, P, P]
+    la = cases["load_any_once"]
+    ids = np.zeros(len(la["ndomains"]), np.int32)
+    done = np.zeros(len(la["ndomains"]), np.uint8)
+    off = 0
+    for k, n in enumerate(la["ndomains"]):
+        R.ref_load_any_once(int(n), _p(la["counts"][off:]), _p(ids[k:]), _p(done[k:]))
+        off += int(n)
+    out["load_any_once"] = {"id": ids, "done": done}
+
     R.ref_mesh_attributes.argtypes = [C.c_char_p, I64, I64, I64, P, P, P, P, P]
     ms = cases["mesh"]
     col = np.zeros(len(ms["prim"]), np.uint32)
@@ -567,6 +594,14 @@ def oracle_outputs(cases: dict) -> dict:
     ms = cases["mesh"]
     nrm, col, ns = O.mesh_attributes(ms["vertices"], ms["faces"], ms["colors"], ms["prim"], ms["u"], ms["v"])
     out["mesh"] = {"color": col, "ns": ns, "normals": nrm}
+    la = cases["load_any_once"]
+    ids, done, off = [], [], 0
+    for n in la["ndomains"]:
+        i, d = O.load_any_once(la["counts"][off:off + n])
+        ids.append(i)
+        done.append(d)
+        off += int(n)
+    out["load_any_once"] = {"id": np.array(ids, np.int32), "done": np.array(done, np.uint8)}
     return out
 
 
@@ -626,6 +661,11 @@ def compare(group: str, cases: dict, ref: dict, orc: dict) -> None:
         assert np.array_equal(r["hits"], o["hits"])
     elif group == "domain_list":
         assert np.array_equal(r["ids"], o["ids"]) and _same(r["ts"], o["ts"])
+    elif group == "load_any_once":
+        # the same domain on ties too: both sort with std::sort over ids
+        # ascending, by count descending
+        assert np.array_equal(r["id"], o["id"]) and np.array_equal(r["done"], o["done"])
+        assert 0 < r["done"].mean() < 1
     elif group == "mesh":
         assert np.array_equal(r["color"], o["color"]), int(np.sum(r["color"] != o["color"]))
         assert _same(r["ns"], o["ns"]), int(np.sum(np.any(_bits(r["ns"]) != _bits(o["ns"]), 1)))

@@ -60,7 +60,8 @@ def test_invalid_config_rejected(lib_built):
     assert e.value.code in (sg.EINVAL, sg.ECUDA)
 
 
-@pytest.mark.parametrize("kw", [dict(schedule_policy=5), dict(schedule_policy=-1), dict(ooc_batch=-1),
+@pytest.mark.parametrize("kw", [dict(schedule_policy=6), dict(schedule_policy=-1), dict(ooc_batch=-1),
+                                dict(schedule_policy=5, num_ranks=2, rank=0),
                                 dict(schedule_policy=3, learn_batch=0), dict(schedule_policy=3, learn_lr=0.0),
                                 dict(schedule_policy=3, learn_frames=0), dict(ooc_inplace=-1),
                                 dict(trace_blocks_per_sm=33), dict(sched_chunks_per_warp=-1),

@@ -1,0 +1,85 @@
+"""The non-speculative round loop on the GPU (schedule_policy 5) against the
+oracle's restatement of the same loop (mode C): the reference's baseline
+image tracer (src/baseline/baseline_image_tracer.inl:28-131) with
+LoadAnyOnceImageSched (baseline_schedulers.cc:43-62).
+
+The GPU runs each round's rays in parallel and the oracle one by one, but
+what a round queues depends only on each ray's own state, so the two must
+agree exactly on the sequence of rounds (the domain of every round, from the
+load log), the cache loads, the closest-hit, occlusion and shading-only
+visits and the rays spawned; the images agree up to the order of the
+additions per pixel."""
+import numpy as np
+import pytest
+
+import spray_gb300 as sg
+from spray_gb300 import scenes
+from conftest import small_config
+from oracle import accuracy as A
+
+pytestmark = pytest.mark.gpu
+
+ORDER_RMSE = 1e-6
+COUNTS = ("rays_primary", "rays_shadow", "rays_bounce", "visits_radiance", "visits_shadow", "visits_shade",
+          "rounds")
+
+
+def _compare(oracle_mod, sc, cfg, frames=1):
+    cam = scenes.orbit_camera(sc)
+    t = sg.Tracer(dict(cfg, schedule_policy=5))
+    t.set_scene(sc)
+    t.set_camera(*cam)
+    o = oracle_mod.Oracle(cfg, sc)
+    o.set_camera(*cam)
+    want, ws, sched = o.render_baseline()
+    for frame in range(frames):
+        img, st = t.trace()
+        log = t.debug(sg.DBG_LOADS, 0)
+        assert np.array_equal(log["domain"], sched), frame
+        assert np.array_equal(log["pass"], np.arange(1, len(sched) + 1))
+        for k in COUNTS:
+            assert st[k] == ws[k], (frame, k, st[k], ws[k])
+        assert A.image_rmse(img, want) <= ORDER_RMSE, (frame, A.image_rmse(img, want))
+        if cfg["cache_size"] > 0 and frame == 0:
+            # a cold cache: the loads of the oracle's LRU over the same rounds
+            assert st["domain_loads"] == ws["domain_loads"] == int(np.sum(log["outcome"] == 0))
+    t.close()
+    return st, ws
+
+
+@pytest.mark.parametrize("mode,spp,cache", [("pt", 1, -1), ("pt", 2, 8), ("ao", 1, 8), ("ao", 2, -1),
+                                            ("pt", 3, 5)])
+def test_rounds_match_the_oracle_loop(lib_built, oracle_mod, mode, spp, cache):
+    sc = scenes.wavelet_grid(3, 16, colors="albedo", light="point+diffuse" if mode == "pt" else "point")
+    cfg = small_config(image_w=48, image_h=36, ao_mode=int(mode == "ao"), ao_samples=2, pixel_samples=spp,
+                       bounces=1 if mode == "ao" else 3, cache_size=cache)
+    st, ws = _compare(oracle_mod, sc, cfg, frames=2)
+    assert st["rounds"] > len(sc.domains) // 2 and st["visits_radiance"] > 0
+
+
+def test_rounds_send_rays_back_to_shade(lib_built, oracle_mod):
+    # two copies of a grid, the second shifted by a quarter of the scene:
+    # overlapping domains, so rays move on past a hit and come back to shade
+    sc = scenes.wavelet_grid(2, 14, colors="albedo", light="point")
+    lo, hi = scenes.scene_box(sc)
+    shift = ((np.asarray(hi) - np.asarray(lo)) * 0.25).astype(np.float32)
+    doms = list(sc.domains) + [sg.Domain(d.vertices + shift, d.faces, d.colors) for d in sc.domains]
+    sc2 = sg.Scene(doms, sc.lights)
+    cfg = small_config(image_w=40, image_h=30, ao_mode=0, pixel_samples=1, bounces=2, cache_size=3)
+    st, ws = _compare(oracle_mod, sc2, cfg)
+    assert st["visits_shade"] > 0
+
+
+def test_rounds_on_the_out_of_core_workload(lib_built, oracle_mod):
+    # C3's 512 domains, list size 22, 8 spp, 4 bounces, the 256-domain cache
+    path, _ = scenes.benchmark_scene("c3")
+    sc = sg.Scene.load(path, path.parent)
+    _, c3 = scenes.workload_config("c3", sc)
+    cfg = dict(c3, image_w=48, image_h=48)
+    for k, v in dict(history_size=4, max_samples_per_rank=1 << 20, num_ranks=1, rank=0).items():
+        cfg.setdefault(k, v)
+    assert cfg["cache_size"] == 256 and len(sc.domains) == 512
+    st, ws = _compare(oracle_mod, sc, cfg)
+    assert st["domain_loads"] > 0 and st["rounds"] >= st["domain_loads"]
+    print(f"C3 48x48 rounds {st['rounds']}, loads {st['domain_loads']}, "
+          f"visits/ray {st['visits_radiance'] / max(1, st['rays_primary'] + st['rays_bounce']):.3f}")
