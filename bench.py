@@ -47,7 +47,9 @@ METRIC = "Mrays/s at <=1e-3 image RMSE, learned vs plain scheduler; domain loads
 POLICIES = {"plain": (0, "plain speculative"), "resident": (1, "resident domains first"),
             "batched": (2, "batched passes (shadow b + radiance b+1), culled domains not loaded"),
             "learned": (3, "learned domain-order proposal (online-trained MLP) + batched passes"),
-            "nonspec": (4, "non-speculative LoadAnyOnce: one pass per list position, most pending rays first")}
+            "nonspec": (4, "non-speculative LoadAnyOnce: one pass per list position, most pending rays first"),
+            "rounds": (5, "the reference's non-speculative image tracer: one domain per round, the one "
+                          "holding the most queued rays (LoadAnyOnceImageSched)")}
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 NODE_BYTES, TRI_BYTES, ENTRY_BYTES, RAY_BYTES, HIT_BYTES = 128, 48, 8, 32, 24
@@ -268,7 +270,7 @@ def north_star_block(args, device: int) -> dict:
     frames = max(args.steps, args.ns_frames)
     ref_img = None
     small = None
-    for name in ("plain", "batched", "learned", "nonspec"):
+    for name in ("plain", "batched", "learned", "nonspec", "rounds"):
         cfg = dict(cfg0)
         pol = POLICIES[name][0]
         cfg["schedule_policy"] = pol
@@ -281,8 +283,11 @@ def north_star_block(args, device: int) -> dict:
         tr.set_scene_prepared(prep, len(scene.domains), scene.lights)
         tr.set_camera(*cam)
         img = np.empty((cfg["image_h"], cfg["image_w"], 4), np.float32)
-        warm = [tr.trace(img)[1] for _ in range(max(args.warmup, 3))]
-        sts = [tr.trace(img)[1] for _ in range(frames)]
+        # the round loop runs thousands of rounds per frame: fewer frames (it
+        # is deterministic, so frames differ only in the cache's warmth)
+        nwarm, ntimed = (1, min(frames, 3)) if name == "rounds" else (max(args.warmup, 3), frames)
+        warm = [tr.trace(img)[1] for _ in range(nwarm)]
+        sts = [tr.trace(img)[1] for _ in range(ntimed)]
         if ref_img is None:
             ref_img = img.copy()
         ms = sum(s["frame_ms"] for s in sts)
@@ -301,6 +306,13 @@ def north_star_block(args, device: int) -> dict:
              "inplace_domains_per_frame": sum(s["inplace_domains"] for s in sts) / n,
              "image_equals_plain": bool(A.bit_exact(img, ref_img)),
              "tuned": t["params"] if t and t.get("policy") == pol else None}
+        if name == "rounds":
+            # the reference loop's own image: it loses the few bounce rays whose
+            # origin lies just outside the domain that spawned them
+            r["image_rmse_vs_plain"] = A.image_rmse(img, ref_img)
+            r["rounds_per_frame"] = sum(s["rounds"] for s in sts) / n
+            r["shading_only_visits_per_frame"] = sum(s["visits_shade"] for s in sts) / n
+            r["cold_cache_domain_loads"] = warm[0]["domain_loads"]
         if name == "learned":
             w0 = next((w for w in warm if w["learn_ms"] > 0), None)
             r["learn"] = {"trained_before_timing": bool(warm[-1]["learn_trained"]),
@@ -320,6 +332,11 @@ def north_star_block(args, device: int) -> dict:
         tr.close()
     p, b, l = (out["policies"][k] for k in ("plain", "batched", "learned"))
     out["nonspec_vs_plain"] = {"speedup": out["policies"]["nonspec"]["mrays_per_s"] / p["mrays_per_s"]}
+    rd = out["policies"]["rounds"]
+    out["learned_vs_reference_nonspeculative_loop"] = {
+        "speedup": l["mrays_per_s"] / rd["mrays_per_s"],
+        "domain_load_reduction": 1 - l["domain_loads_per_frame"] / max(rd["domain_loads_per_frame"], 1e-9),
+        "radiance_visits_ratio": l["radiance_visits_per_frame"] / max(rd["radiance_visits_per_frame"], 1e-9)}
     out["learned_vs_plain"] = {"speedup": l["mrays_per_s"] / p["mrays_per_s"],
                                "domain_load_reduction": 1 - l["domain_loads_per_frame"] / max(p["domain_loads_per_frame"], 1e-9),
                                "bytes_moved_reduction": 1 - (l["h2d_bytes_per_frame"] + l["inplace_bytes_per_frame"]) /

@@ -35,6 +35,7 @@
 #include <cstring>
 #include <utility>
 
+#include "domain_walk.cuh"
 #include "kernels.cuh"
 #include "shade.cuh"
 #include "spray_math.cuh"
@@ -57,6 +58,8 @@ struct RoundArgs {
   SceneDev scene;
   const float* boxes;  // 6 floats per domain
   int D;
+  const float4* dnodes;  // 4-wide hierarchy over the boxes (8 float4 per node), null: every box
+  int dnode_count;
   RoundRays rays;
   uint32_t* pool_count;
   uint32_t pool_cap;
@@ -103,11 +106,11 @@ __device__ int advanceRay(const RoundArgs& a, V3 org, V3 dir, float tmax, int cu
   float lt[kRoundList];
   int ld[kRoundList];
   int cnt = 0, n = 0;
-  for (int d = 0; d < a.D; ++d) {
+  auto consider = [&](int d) {
     float t;
-    if (!slabTest(&a.boxes[6 * d], &a.boxes[6 * d + 3], org, inv, kRayEpsilon, tmax, &t)) continue;
+    if (!slabTest(&a.boxes[6 * d], &a.boxes[6 * d + 3], org, inv, kRayEpsilon, tmax, &t)) return;
     ++n;
-    if (cnt == need && (lt[cnt - 1] < t || (lt[cnt - 1] == t && ld[cnt - 1] < d))) continue;
+    if (cnt == need && (lt[cnt - 1] < t || (lt[cnt - 1] == t && ld[cnt - 1] < d))) return;
     int j = cnt < need ? cnt++ : need - 1;
     while (j > 0 && (lt[j - 1] > t || (lt[j - 1] == t && ld[j - 1] > d))) {
       lt[j] = lt[j - 1];
@@ -116,7 +119,10 @@ __device__ int advanceRay(const RoundArgs& a, V3 org, V3 dir, float tmax, int cu
     }
     lt[j] = t;
     ld[j] = d;
-  }
+  };
+  if (a.dnode_count > 0) descendDomains(a.dnodes, a.dnode_count, org, inv, tmax, consider, a.ctr);
+  else
+    for (int d = 0; d < a.D; ++d) consider(d);
   int p;
   if (domain_pos == kRoundNone) p = (n > 0 && ld[0] == current) ? 1 : 0;
   else p = domain_pos + 1;
@@ -520,6 +526,8 @@ void Tracer::traceRounds() {
     a.scene = sceneDev();
     a.boxes = d_dboxes;
     a.D = D;
+    a.dnodes = reinterpret_cast<const float4*>(d_dnodes);
+    a.dnode_count = dnode_count;
     a.rays = rr;
     a.pool_count = reinterpret_cast<uint32_t*>(d_rr_pool);
     a.pool_cap = (uint32_t)rr_pool_cap;
