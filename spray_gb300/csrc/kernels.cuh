@@ -20,6 +20,7 @@
 #include <stdint.h>
 
 #include "bvh.h"
+#include "spray_math.cuh"
 
 namespace spray {
 
@@ -149,6 +150,18 @@ struct CameraDev {
   float hv[3];   // full-height vector
   float image_w, image_h;
 };
+
+// Camera::generateRay (src/render/camera.h:173-209): the unit direction
+// through image point (fx, fy), u = fx / W, v = fy / H.
+__device__ __forceinline__ V3 cameraRay(const CameraDev& cam, float fx, float fy) {
+  const float u = fx / cam.image_w;
+  const float v = fy / cam.image_h;
+  const V3 ll = v3(cam.ll[0], cam.ll[1], cam.ll[2]);
+  const V3 wv = v3(cam.wv[0], cam.wv[1], cam.wv[2]);
+  const V3 hv = v3(cam.hv[0], cam.hv[1], cam.hv[2]);
+  const V3 pos = v3(cam.pos[0], cam.pos[1], cam.pos[2]);
+  return normalize(((ll + u * wv) + v * hv) - pos);
+}
 
 struct TileDev {
   int32_t x, y, w, h;

@@ -367,12 +367,8 @@ __global__ void kRoundEyes(RoundArgs a, int64_t n) {
     fx = (float)x + rngNext(st);
     fy = (float)y + rngNext(st);
   }
-  const float u = fx / cam.image_w, v = fy / cam.image_h;
-  const V3 ll = v3(cam.ll[0], cam.ll[1], cam.ll[2]);
-  const V3 wv = v3(cam.wv[0], cam.wv[1], cam.wv[2]);
-  const V3 hv = v3(cam.hv[0], cam.hv[1], cam.hv[2]);
   const V3 pos = v3(cam.pos[0], cam.pos[1], cam.pos[2]);
-  const V3 d = normalize(((ll + u * wv) + v * hv) - pos);
+  const V3 d = cameraRay(cam, fx, fy);
   int dp = kRoundNone;
   float nt;
   const int first = advanceRay(a, pos, d, __int_as_float(0x7f800000), kRoundNone, dp, nt);
@@ -444,6 +440,19 @@ __global__ void kRoundScatter(const uint2* out, const uint32_t* out_count, uint3
 // the domain with the most queued rays; equal counts keep the order std::sort
 // leaves them in when given the ids ascending.  Returns -1 when every count is 0.
 int loadAnyOnceNext(const std::vector<int64_t>& counts) {
+  // a unique largest count is the answer whatever the sort does with ties
+  int64_t best = 0;
+  int at = -1, ties = 0;
+  for (size_t i = 0; i < counts.size(); ++i) {
+    if (counts[i] > best) {
+      best = counts[i];
+      at = (int)i;
+      ties = 1;
+    } else if (counts[i] == best && best > 0) {
+      ++ties;
+    }
+  }
+  if (at < 0 || ties == 1) return at;
   std::vector<std::pair<int, int64_t>> rc(counts.size());
   for (size_t i = 0; i < counts.size(); ++i) rc[i] = {(int)i, counts[i]};
   std::sort(rc.begin(), rc.end(),

@@ -63,14 +63,8 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
     fx = (float)x + rngNext(st);
     fy = (float)y + rngNext(st);
   }
-  float u = fx / cam.image_w;
-  float v = fy / cam.image_h;
-  V3 ll = v3(cam.ll[0], cam.ll[1], cam.ll[2]);
-  V3 wv = v3(cam.wv[0], cam.wv[1], cam.wv[2]);
-  V3 hv = v3(cam.hv[0], cam.hv[1], cam.hv[2]);
-  V3 pos = v3(cam.pos[0], cam.pos[1], cam.pos[2]);
-  V3 d = normalize(((ll + u * wv) + v * hv) - pos);
-  rays.org[i] = make_float4(pos.x, pos.y, pos.z, 0.f);
+  const V3 d = cameraRay(cam, fx, fy);
+  rays.org[i] = make_float4(cam.pos[0], cam.pos[1], cam.pos[2], 0.f);
   rays.dir[i] = make_float4(d.x, d.y, d.z, 0.f);
   rays.pixid[i] = y * vw.image_w + x;
   rays.samid[i] = bufid;
