@@ -239,7 +239,11 @@ def accuracy_report(scene, cfg, cam, mode_a_img, oracle_obj, device: int) -> dic
     t.set_scene(scene)
     t.set_camera(*cam)
     img, st = t.trace()
-    mode_b, _ = oracle_obj.render_wavefront()
+    # the oracle walks the same hierarchies the GPU built (front to back,
+    # culled by the hit so far) and counts that walk's nodes and triangles
+    for d in range(len(scene.domains)):
+        oracle_obj.set_bvh4(d, t.debug(sg.DBG_NODES, d), t.debug(sg.DBG_TRIS, d))
+    mode_b, ost = oracle_obj.render_wavefront()
     hits, shadows = {}, {}
     for b in range(cfg["bounces"]):
         rays = t.debug(sg.DBG_RAYS, b)
@@ -251,6 +255,15 @@ def accuracy_report(scene, cfg, cam, mode_a_img, oracle_obj, device: int) -> dic
     t.close()
     rep = A.frame_report(img, mode_a_img, mode_b, hits, shadows)
     rep["frame"] = [c["image_w"], c["image_h"]]
+    gpu_bytes = (st["visits_radiance"] * (RAY_BYTES + ENTRY_BYTES + HIT_BYTES)
+                 + st["nodes_radiance"] * NODE_BYTES + st["tris_radiance"] * TRI_BYTES)
+    orc_bytes = (ost["bvh4_visits"] * (RAY_BYTES + ENTRY_BYTES + HIT_BYTES)
+                 + ost["bvh4_nodes"] * NODE_BYTES + ost["bvh4_tris"] * TRI_BYTES)
+    rep["closest_hit_traversal"] = {
+        "gpu": {"visits": st["visits_radiance"], "nodes": st["nodes_radiance"], "tris": st["tris_radiance"]},
+        "oracle": {"visits": ost["bvh4_visits"], "nodes": ost["bvh4_nodes"], "tris": ost["bvh4_tris"],
+                   "hit_mismatches": ost["bvh4_mismatches"]},
+        "oracle_to_gpu_bytes": orc_bytes / gpu_bytes if gpu_bytes else None}
     return rep
 
 
@@ -642,6 +655,17 @@ def main():
             gcfg = dict(cfg)
             gcfg.update(image_w=c["image_w"], image_h=c["image_h"], graphs=0)
             out["accuracy"] = accuracy_report(scene, gcfg, cam, mode_a, o, local)
+            tr = out["accuracy"]["closest_hit_traversal"]
+            rl = out["roofline"]
+            if rl["kernel"] == "closest-hit traversal" and tr["oracle_to_gpu_bytes"]:
+                # the algorithmic bytes with node and triangle counts from the
+                # oracle's ordered walk of the same hierarchies (measured on the
+                # accuracy frame, scaled to this frame by the ratio of the walks)
+                ob = rl["algorithmic_bytes_per_frame"] * tr["oracle_to_gpu_bytes"]
+                ach = ob / (rl["kernel_ms_per_frame"] * 1e-3) / 1e9
+                rl["oracle_counted"] = {"algorithmic_bytes_per_frame": ob, "achieved": ach,
+                                        "frac": ach / rl["peak"], "ratio_to_kernel_counts": tr["oracle_to_gpu_bytes"],
+                                        "sample": f"{c['image_w']}x{c['image_h']} frame of the same workload"}
         o.close()
     if rank == 0 and world == 1 and args.north_star and args.config == "c2":
         out["north_star"] = north_star_block(args, local)

@@ -301,7 +301,15 @@ int spray_generate_wavelet(int32_t samples, double iso, const double phase[3], f
 #define SPRAY_DBG_SCORES 5      /* spray_gpu_dbg_score, domain scores and schedule order */
 #define SPRAY_DBG_LOADS 6       /* spray_gpu_dbg_load, out of core: every domain the frame asked the
                                    cache for, in order (kept for every frame, bounce 0, no
-                                   debug_capture needed; empty in core) */
+                                   debug_capture needed; empty in core, except under
+                                   schedule_policy 5, which logs every round's domain) */
+#define SPRAY_DBG_NODES 7       /* the BVH of domain `bounce` as set_scene built it: BvhNode4
+                                   records of 128 bytes (child boxes lo/hi x, y, z as 4 floats each,
+                                   4 child references, 4 pad; child >= 0 inner node, kEmptyChild
+                                   0x80000000 unused, else leaf ~((first << 3) | (count - 1))); needs
+                                   no debug_capture */
+#define SPRAY_DBG_TRIS 8        /* the leaf-ordered triangles of domain `bounce`: 3 x float4 (the
+                                   vertices; w of the first = the domain-local face index bits) */
 
 typedef struct spray_gpu_dbg_ray {
   uint32_t sample;   /* index of the sample in the wavefront */

@@ -357,6 +357,17 @@ inline bool boxHit(const BNode& n, F3 org, F3 inv, float tnear, float tfar, floa
 }
 
 // ---------------------------------------------------------------- scene
+// A 4-wide BVH in the product's layout (128-byte nodes: child boxes lo/hi x,
+// lo/hi y, lo/hi z as four floats each, then four child references: >= 0 an
+// inner node, 0x80000000 an empty slot, otherwise a leaf ~((first << 3) |
+// (count - 1)) into the leaf-ordered triangles, three float4 each, the first
+// vertex's w holding the domain-local face index bits), given to the oracle
+// only to count the work of an ordered traversal of that same hierarchy.
+struct Bvh4 {
+  std::vector<float> nodes;  // 32 floats per node (the references as int bits)
+  std::vector<float> tris;   // 12 floats per triangle
+};
+
 struct Domain {
   std::vector<float> v;
   std::vector<uint32_t> f;
@@ -366,6 +377,8 @@ struct Domain {
   int bsdf = 0;
   float params[3] = {1, 1, 1};
   MeshBvh bvh;
+  Bvh4 b4;
+  uint32_t prim_base = 0;  // faces of the domains before this one
 };
 
 struct Light {
@@ -530,6 +543,105 @@ bool refract(float cosThetaI, float etaI, float etaT, F3 wo, F3 normal_ff, F3* w
   float cosThetaT = std::sqrt(1.0f - sin2ThetaT);
   *wt = add(smul(eta, neg(wo)), muls(normal_ff, eta * cosThetaI - cosThetaT));
   return true;
+}
+
+// Closest hit in one domain through its Bvh4, counting inner nodes expanded
+// and triangles tested.  The walk is the product's ordered traversal: the
+// four child boxes tested with t1 widened by kBoxSlack, children ordered near
+// to far by their entry distance (its two low bits replaced by the slot), the
+// nearest one continued when it starts within the best hit, the others pushed
+// far to near, and stack entries beyond the best hit dropped on pop; a leaf's
+// triangles are tested with an infinite tfar and kept by the (t, global face)
+// key.  best_key enters as the key to beat.
+constexpr float kBoxSlack = 1.0000004f;
+constexpr int32_t kEmpty4 = (int32_t)0x80000000;
+
+bool closestBvh4(const Domain& d, F3 org, F3 dir, uint64_t* best_key, float* best_t, int64_t* nodes,
+                 int64_t* tris) {
+  const float* N = d.b4.nodes.data();
+  const int nn = (int)(d.b4.nodes.size() / 32);
+  const float* T = d.b4.tris.data();
+  const int nt = (int)(d.b4.tris.size() / 12);
+  Shear sh = makeShear(dir);
+  const float inv[3] = {1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z};
+  const float o[3] = {org.x, org.y, org.z};
+  const int s[3] = {inv[0] < 0.0f, inv[1] < 0.0f, inv[2] < 0.0f};
+  int32_t sref[128];
+  float st[128];
+  int sp = 0;
+  bool found = false;
+  auto pop = [&]() -> int32_t {
+    while (sp > 0) {
+      --sp;
+      if (st[sp] <= *best_t) return sref[sp];
+    }
+    return kEmpty4;
+  };
+  int32_t cur = 0;
+  while (cur != kEmpty4) {
+    while (cur >= 0) {
+      if (cur >= nn) throw std::runtime_error("bvh4: node index out of range");
+      ++*nodes;
+      const float* q = N + 32 * (size_t)cur;
+      int32_t ch[4];
+      std::memcpy(ch, q + 24, 16);
+      uint32_t k[4];
+      for (int c = 0; c < 4; ++c) {
+        float t0 = kEps, t1 = *best_t;
+        float a[3], b[3];
+        for (int x = 0; x < 3; ++x) {
+          const float nearp = q[8 * x + 4 * s[x] + c], farp = q[8 * x + 4 * (s[x] ^ 1) + c];
+          a[x] = (nearp - o[x]) * inv[x];
+          b[x] = (farp - o[x]) * inv[x];
+        }
+        t0 = std::fmax(std::fmax(a[0], a[1]), std::fmax(a[2], kEps));
+        t1 = std::fmin(std::fmin(b[0], b[1]), std::fmin(b[2], *best_t)) * kBoxSlack;
+        uint32_t bits;
+        std::memcpy(&bits, &t0, 4);
+        k[c] = (t0 <= t1 && ch[c] != kEmpty4) ? ((bits & ~3u) | (uint32_t)c) : 0xffffffffu;
+      }
+      std::sort(k, k + 4);
+      float k0t;
+      const uint32_t k0b = k[0] & ~3u;
+      std::memcpy(&k0t, &k0b, 4);
+      if (k[0] != 0xffffffffu && k0t <= *best_t) {
+        for (int j = 3; j >= 1; --j) {
+          if (k[j] == 0xffffffffu) continue;
+          if (sp == 128) throw std::runtime_error("bvh4: traversal stack overflow");
+          const uint32_t kb = k[j] & ~3u;
+          sref[sp] = ch[k[j] & 3u];
+          std::memcpy(&st[sp], &kb, 4);
+          ++sp;
+        }
+        cur = ch[k[0] & 3u];
+      } else {
+        cur = pop();
+      }
+    }
+    if (cur == kEmpty4) break;
+    const uint32_t v = ~(uint32_t)cur;
+    const uint32_t first = v >> 3, cnt = (v & 7u) + 1u;
+    if ((int)(first + cnt) > nt) throw std::runtime_error("bvh4: leaf out of range");
+    *tris += cnt;
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const float* t3 = T + 12 * (size_t)(first + j);
+      float t, u, vv;
+      if (triangleHit(sh, org, f3(t3[0], t3[1], t3[2]), f3(t3[4], t3[5], t3[6]), f3(t3[8], t3[9], t3[10]), kEps,
+                      kInf, &t, &u, &vv)) {
+        uint32_t prim, tb;
+        std::memcpy(&prim, &t3[3], 4);
+        std::memcpy(&tb, &t, 4);
+        const uint64_t key = ((uint64_t)tb << 32) | (uint64_t)(d.prim_base + prim);
+        if (key < *best_key) {
+          *best_key = key;
+          *best_t = t;
+          found = true;
+        }
+      }
+    }
+    cur = pop();
+  }
+  return found;
 }
 
 struct Tile {
@@ -847,6 +959,23 @@ struct Oracle {
     return found;
   }
 
+  // The work of the ordered front-to-back walk of a ray over the Bvh4s: its
+  // domains in (entry t, id) order, a domain skipped when its entry lies
+  // beyond the best hit so far, each walk starting from that hit.  Returns the
+  // key (t bits << 32 | global face) of the closest hit, ~0 for none.
+  uint64_t countBvh4(F3 org, F3 dir, int64_t* visits, int64_t* nodes, int64_t* tris) const {
+    std::vector<std::pair<float, int>> list;
+    domainList(org, dir, kInf, &list);
+    uint64_t key = ~0ull;
+    float best = kInf;
+    for (auto& e : list) {
+      if (key != ~0ull && e.first > best) continue;
+      ++*visits;
+      closestBvh4(doms[e.second], org, dir, &key, &best, nodes, tris);
+    }
+    return key;
+  }
+
   bool occluded(F3 org, F3 dir, float tmax, int origin, int64_t* visits) const {
     if (visits) ++*visits;
     if (occludedInDomain(doms[origin], org, dir, tmax)) return true;
@@ -883,14 +1012,23 @@ struct Oracle {
         std::vector<char> nalive(n, 0);
         // per-sample shadow contributions, added per pixel in sample order
         std::vector<std::vector<std::pair<F3, bool>>> contrib(n);
-        int64_t vis_r = 0, vis_s = 0, nsh = 0, nb = 0;
-#pragma omp parallel for schedule(dynamic, 256) reduction(+ : vis_r, vis_s, nsh, nb)
+        int64_t vis_r = 0, vis_s = 0, nsh = 0, nb = 0, v4 = 0, n4 = 0, t4 = 0, bad4 = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : vis_r, vis_s, nsh, nb, v4, n4, t4, bad4)
         for (int64_t i = 0; i < n; ++i) {
           if (!alive[i]) continue;
           const WRay& r = rays[i];
           Hit h;
           int dom;
-          if (!closest(r.org, r.dir, &h, &dom, &vis_r)) continue;
+          const bool hit = closest(r.org, r.dir, &h, &dom, &vis_r);
+          if (has_bvh4) {
+            // the same hit through the product's hierarchy, and its work
+            const uint64_t k4 = countBvh4(r.org, r.dir, &v4, &n4, &t4);
+            uint32_t tb;
+            std::memcpy(&tb, &h.t, 4);
+            const uint64_t want = hit ? (((uint64_t)tb << 32) | (uint64_t)(doms[dom].prim_base + h.prim)) : ~0ull;
+            if (k4 != want) ++bad4;
+          }
+          if (!hit) continue;
           uint32_t color;
           F3 ns;
           shadingAttributes(doms[dom], h, &color, &ns);
@@ -912,6 +1050,10 @@ struct Oracle {
         }
         s.visits_radiance += vis_r;
         s.visits_shadow += vis_s;
+        s.bvh4_visits += v4;
+        s.bvh4_nodes += n4;
+        s.bvh4_tris += t4;
+        s.bvh4_mismatches += bad4;
         s.rays_shadow += nsh;
         if (b + 1 < cfg.bounces) s.rays_bounce += nb;
         for (int64_t p = 0; p < n / spp; ++p) {
@@ -938,6 +1080,7 @@ struct Oracle {
   // ------------------------------------------------------------ mode C
   void renderBaseline(float* rgba, orc_stats* st, std::vector<int>* schedule);
   std::vector<int> baseline_schedule;  // the domains of the last mode C frame, one per round
+  bool has_bvh4 = false;               // every domain holds a Bvh4 (orc_set_bvh4)
 };
 
 // =================================================================== mode A
@@ -1820,8 +1963,27 @@ void sortDomainList(std::vector<std::pair<float, int>>* l) {
 }  // namespace orc
 }  // extern "C++"
 
+int orc_set_bvh4(void* ov, int32_t d, const float* nodes, int64_t num_nodes, const float* tris,
+                 int64_t num_tris) {
+  Oracle* o = (Oracle*)ov;
+  if (d < 0 || d >= o->D() || num_nodes <= 0 || num_tris < 0 || !nodes || (!tris && num_tris)) return 1;
+  orc::Domain& D = o->doms[d];
+  if ((uint64_t)num_tris != D.f.size() / 3) return 2;  // one leaf slot per face
+  D.b4.nodes.assign(nodes, nodes + 32 * num_nodes);
+  D.b4.tris.assign(tris, tris + 12 * num_tris);
+  bool all = true;
+  for (const auto& x : o->doms) all = all && !x.b4.nodes.empty();
+  o->has_bvh4 = all;
+  return 0;
+}
+
 int orc_build(void* ov) {
   Oracle* o = (Oracle*)ov;
+  uint32_t base = 0;
+  for (auto& x : o->doms) {
+    x.prim_base = base;
+    base += (uint32_t)(x.f.size() / 3);
+  }
 #pragma omp parallel for schedule(dynamic, 1)
   for (int d = 0; d < o->D(); ++d) {
     orc::Domain& D = o->doms[d];

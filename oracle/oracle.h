@@ -60,6 +60,11 @@ typedef struct orc_stats {
   int64_t domain_loads;
   int64_t rounds;
   int64_t visits_shade;  /* mode C: rays sent back to the domain of their hit for shading */
+  /* mode B with orc_set_bvh4 on every domain: the ordered front-to-back walk
+   * of the radiance rays over those hierarchies (domains visited after
+   * culling, inner nodes expanded, triangles tested) and the rays whose hit
+   * differed from the oracle's own (0 when the hierarchies are sound) */
+  int64_t bvh4_visits, bvh4_nodes, bvh4_tris, bvh4_mismatches;
 } orc_stats;
 
 void* orc_create(const orc_config* cfg, int32_t num_domains);
@@ -71,6 +76,10 @@ int orc_set_domain(void* o, int32_t d, const float* vertices, int64_t nv, const 
 /* lights: 13 floats each: type, position[3], radiance[3], edge1[3], edge2[3] */
 int orc_set_lights(void* o, int32_t nl, const float* lights);
 int orc_build(void* o);  /* vertex normals and per-domain BVHs */
+/* the product's 4-wide BVH of domain d (32 floats per node, 12 per
+ * leaf-ordered triangle, one per face), for counting the work of an ordered
+ * traversal of it in orc_render_wavefront; after orc_build */
+int orc_set_bvh4(void* o, int32_t d, const float* nodes, int64_t num_nodes, const float* tris, int64_t num_tris);
 int orc_set_camera(void* o, const float pos[3], const float lookat[3], const float up[3], float vfov);
 int orc_normals(void* o, int32_t d, float* out);  /* 3 * nv */
 

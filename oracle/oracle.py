@@ -53,7 +53,8 @@ class OrcConfig(C.Structure):
 class OrcStats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("rays_primary", "rays_shadow", "rays_bounce",
                                          "visits_radiance", "visits_shadow", "domain_loads",
-                                         "rounds", "visits_shade")]
+                                         "rounds", "visits_shade", "bvh4_visits", "bvh4_nodes",
+                                         "bvh4_tris", "bvh4_mismatches")]
 
     def asdict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -103,6 +104,7 @@ def lib() -> C.CDLL:
         L.orc_render_wavefront.argtypes = [P, P, C.POINTER(OrcStats)]
         L.orc_render_speculative.argtypes = [P, C.c_int32, P, C.POINTER(OrcStats)]
         L.orc_render_baseline.argtypes = [P, P, C.POINTER(OrcStats)]
+        L.orc_set_bvh4.argtypes = [P, C.c_int32, P, C.c_int64, P, C.c_int64]
         L.orc_baseline_schedule.argtypes = [P, P, C.c_int64]
         L.orc_baseline_schedule.restype = C.c_int64
         L.orc_load_any_once.argtypes = [C.c_int32, P, P, P]
@@ -163,6 +165,21 @@ def lru_trace(num_domains: int, cache_size: int, ids, with_evicted: bool = False
     ev = np.zeros(len(ids), np.int32)
     lib().orc_lru_trace(num_domains, cache_size, len(ids), _p(ids), _p(hits), _p(ev))
     return (hits, ev) if with_evicted else hits
+
+
+def read_blob_bvh(path) -> tuple[np.ndarray, np.ndarray]:
+    """The BVH nodes (32 float32 each) and leaf-ordered triangles (12 float32
+    each) of a prepared domain blob (`domain_NNNNN.sdom`: a 128-byte header --
+    magic SPRAYDOM, version, BSDF, bounds, BSDF parameters, BVH depth, vertex,
+    face and node counts, array offsets -- then 256-byte-aligned arrays)."""
+    raw = np.fromfile(path, np.uint8)
+    if raw[:8].tobytes() != b"SPRAYDOM":
+        raise ValueError(f"{path}: not a prepared domain")
+    nv, nf, nn = raw[56:80].view(np.int64)
+    off_nodes, off_tris = raw[80:96].view(np.uint64)
+    nodes = raw[int(off_nodes):int(off_nodes) + 128 * int(nn)].view(np.float32)
+    tris = raw[int(off_tris):int(off_tris) + 48 * int(nf)].view(np.float32)
+    return nodes, tris
 
 
 def load_any_once(counts) -> tuple[int, bool]:
@@ -439,6 +456,19 @@ class Oracle:
         if self.L.orc_render_wavefront(self.h, _p(img), C.byref(st)) != 0:
             raise RuntimeError("oracle wavefront render failed")
         return img, st.asdict()
+
+    def set_bvh4(self, d: int, nodes, tris):
+        """Domain d's 4-wide BVH in the product's layout (128-byte nodes and
+        leaf-ordered triangles of three float4, as spray_gpu_debug returns
+        them or a prepared blob holds them); once every domain has one,
+        render_wavefront also counts an ordered walk over them."""
+        nodes = np.ascontiguousarray(nodes).view(np.float32).reshape(-1)
+        tris = np.ascontiguousarray(tris).view(np.float32).reshape(-1)
+        if nodes.size % 32 or tris.size % 12:
+            raise ValueError("nodes must be 128-byte records, triangles 48-byte records")
+        rc = self.L.orc_set_bvh4(self.h, d, _p(nodes), nodes.size // 32, _p(tris), tris.size // 12)
+        if rc != 0:
+            raise ValueError(f"domain {d}: BVH rejected ({rc})")
 
     def render_baseline(self):
         """Mode C, the reference's non-speculative image tracer on one

@@ -19,7 +19,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libspray_gpu.so"
 
 OK, EINVAL, ECUDA, EIO, ESTATE, EOVERFLOW, ENOMEM, ETIMEOUT = range(8)
-DBG_RAYS, DBG_RQUEUES, DBG_HITS, DBG_SHADOWS, DBG_SQUEUES, DBG_SCORES, DBG_LOADS = range(7)
+DBG_RAYS, DBG_RQUEUES, DBG_HITS, DBG_SHADOWS, DBG_SQUEUES, DBG_SCORES, DBG_LOADS, DBG_NODES, DBG_TRIS = range(9)
 
 
 class SprayError(RuntimeError):
@@ -114,6 +114,10 @@ DBG_DTYPES = {
     DBG_SCORES: np.dtype([("domain", "<i4"), ("pad", "<i4"), ("score", "<i8"), ("order", "<i4"),
                           ("pad2", "<i4")]),
     DBG_LOADS: np.dtype([("domain", "<i4"), ("outcome", "<i4"), ("evicted", "<i4"), ("pass", "<i4")]),
+    # one BVH node (BvhNode4) and one leaf-ordered triangle of a domain (bounce = the domain)
+    # box rows: lo x, hi x, lo y, hi y, lo z, hi z of the four children
+    DBG_NODES: np.dtype([("box", "<f4", (6, 4)), ("child", "<i4", 4), ("pad", "<i4", 4)]),
+    DBG_TRIS: np.dtype([("v", "<f4", (3, 4))]),
 }
 
 _lib_handle = None

@@ -358,6 +358,7 @@ void Tracer::freeScene() {
   devFree(d_dnodes);
   devFree(d_dboxes);
   freeRounds();  // sized by the domain count
+  bvh_dump.clear();
   dnode_count = 0;
   devFree(d_bin_start);
   devFree(d_bin_ids);
@@ -2309,6 +2310,28 @@ const std::vector<char>* Tracer::debugData(int what, int bounce) const {
   return it == dbg.end() ? nullptr : &it->second;
 }
 
+// The BVH nodes (SPRAY_DBG_NODES) or the leaf-ordered triangles
+// (SPRAY_DBG_TRIS) of domain d as set_scene built them: from the device in
+// core, from the pinned host copy out of core.  Null for a domain this tracer
+// did not build (another rank's, in situ).
+const std::vector<char>* Tracer::domainBvh(int what, int d) {
+  if (!has_scene || d < 0 || d >= D) return nullptr;
+  const DomainDev& dd = hdoms[d];
+  if (dd.num_nodes <= 0) return nullptr;
+  const bool nodes = what == SPRAY_DBG_NODES;
+  const size_t nb = nodes ? (size_t)dd.num_nodes * sizeof(BvhNode4) : (size_t)dd.num_tris * 3 * sizeof(float4);
+  std::vector<char>& v = bvh_dump[{what, d}];
+  v.resize(nb);
+  if (ooc) {
+    const char* q = h_pinned + host_off[d] + (nodes ? 0 : (size_t)dd.num_nodes * sizeof(BvhNode4));
+    std::memcpy(v.data(), q, nb);
+  } else {
+    const void* src = nodes ? (const void*)(d_nodes + dd.node_base) : (const void*)(d_tris + 3 * (size_t)dd.tri_base);
+    CK(cudaMemcpy(v.data(), src, nb, cudaMemcpyDeviceToHost));
+  }
+  return &v;
+}
+
 }  // namespace spray
 
 // ====================================================================== C ABI
@@ -2478,6 +2501,14 @@ int spray_gpu_trace_views_device(spray_gpu_tracer* t, const spray_gpu_view* view
 
 int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int64_t* count) {
   if (!t || !count) return fail(SPRAY_GPU_EINVAL, "null argument");
+  if (what == SPRAY_DBG_NODES || what == SPRAY_DBG_TRIS) {
+    API_GUARD({
+      const std::vector<char>* d = t->impl->domainBvh(what, bounce);
+      if (!d) return fail(SPRAY_GPU_EINVAL, "no BVH for that domain here");
+      *count = (int64_t)(d->size() / (what == SPRAY_DBG_NODES ? sizeof(spray::BvhNode4) : 3 * sizeof(float4)));
+      return SPRAY_GPU_OK;
+    })
+  }
   if (what < 0 || what > SPRAY_DBG_LOADS) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
   int64_t n = t->impl->debugCount(what, bounce);
   if (n < 0) return fail(SPRAY_GPU_ESTATE, "no captured buffer (set debug_capture and trace)");
@@ -2487,8 +2518,15 @@ int spray_gpu_debug_count(spray_gpu_tracer* t, int32_t what, int32_t bounce, int
 
 int spray_gpu_debug_copy(spray_gpu_tracer* t, int32_t what, int32_t bounce, void* out, int64_t capacity) {
   if (!t || !out) return fail(SPRAY_GPU_EINVAL, "null argument");
-  if (what < 0 || what > SPRAY_DBG_LOADS) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
-  const std::vector<char>* d = t->impl->debugData(what, bounce);
+  const bool bvh = what == SPRAY_DBG_NODES || what == SPRAY_DBG_TRIS;
+  if (!bvh && (what < 0 || what > SPRAY_DBG_LOADS)) return fail(SPRAY_GPU_EINVAL, "unknown debug buffer");
+  const std::vector<char>* d = nullptr;
+  if (bvh) {
+    API_GUARD({ d = t->impl->domainBvh(what, bounce); })
+    if (!d) return fail(SPRAY_GPU_EINVAL, "no BVH for that domain here");
+  } else {
+    d = t->impl->debugData(what, bounce);
+  }
   if (!d) return fail(SPRAY_GPU_ESTATE, "no captured buffer (set debug_capture and trace)");
   if ((int64_t)d->size() > capacity) return fail(SPRAY_GPU_EINVAL, "output buffer too small");
   std::memcpy(out, d->data(), d->size());

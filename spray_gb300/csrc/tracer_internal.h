@@ -151,6 +151,7 @@ class Tracer {
   void traceViews(const spray_gpu_view* views, int n, float* out, bool out_is_device, spray_gpu_stats* st);
   int64_t debugCount(int what, int bounce) const;
   const std::vector<char>* debugData(int what, int bounce) const;
+  const std::vector<char>* domainBvh(int what, int domain);
   // domain-parallel (in-situ) execution, before setScene (insitu.cu)
   void setInsitu(int num_ranks, int rank, const spray_gpu_reduce_ops* ops);
 
@@ -379,6 +380,7 @@ class Tracer {
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
   int64_t inplace_domains = 0;  // (domain, batch) pairs traced in place this frame
   std::map<std::pair<int, int>, std::vector<char>> dbg;
+  std::map<std::pair<int, int>, std::vector<char>> bvh_dump;  // (what, domain): domainBvh copies
   int load_pass = 0;  // passes over the domains in this frame (the request log's pass numbers)
   void logLoad(int d, int outcome, int evicted);
 };

@@ -107,3 +107,36 @@ def test_device_bvh_on_the_out_of_core_workload(lib_built):
     print(f"C3 set_scene: host BVH {host_s:.2f} s, device BVH {dev_s:.2f} s; nodes visited "
           f"{sd['nodes_radiance']} vs {sh['nodes_radiance']}")
     assert dev_s < host_s
+
+
+@pytest.mark.parametrize("cache", [-1, 10])
+def test_oracle_walks_the_gpu_hierarchy(lib_built, oracle_mod, cache):
+    # the hierarchies set_scene built on the device, read back through the
+    # debug hook (from the device in core, from pinned host memory out of
+    # core), give every ray the oracle's own closest hit; the kernel's node
+    # and triangle counts are close to those of the oracle's ordered walk
+    # (front to back over the domains, culled by the hit so far)
+    sc = scenes.wavelet_grid(4, 24, colors="albedo", light="quad")
+    cfg = small_config(image_w=96, image_h=72, ao_mode=0, pixel_samples=2, bounces=3, cache_size=cache,
+                       bucket_launches=4)
+    t, img, st, _ = _trace(sc, cfg)
+    o = oracle_mod.Oracle(cfg, sc)
+    o.set_camera(*scenes.orbit_camera(sc))
+    for d in range(len(sc.domains)):
+        nodes, tris = t.debug(sg.DBG_NODES, d), t.debug(sg.DBG_TRIS, d)
+        assert len(tris) == len(sc.domains[d].faces) and len(nodes) >= 1
+        assert np.all(np.isin(np.sort(tris["v"][:, 0, 3].view(np.uint32)),
+                              np.arange(len(tris), dtype=np.uint32)))
+        o.set_bvh4(d, nodes, tris)
+    want, ost = o.render_wavefront()
+    assert np.array_equal(bits(img), bits(want))
+    assert ost["bvh4_mismatches"] == 0
+    # out of core the queues run domain by domain in score order, so fewer
+    # entries see a nearer hit before they start
+    hi = 1.25 if cache < 0 else 2.0
+    for k, g in (("bvh4_nodes", "nodes_radiance"), ("bvh4_tris", "tris_radiance"),
+                 ("bvh4_visits", "visits_radiance")):
+        r = st[g] / ost[k]
+        print(f"{g}: gpu {st[g]} oracle {ost[k]} ratio {r:.4f}")
+        assert 0.9 <= r <= hi, (g, st[g], ost[k])
+    t.close()
