@@ -53,6 +53,7 @@ constexpr uint32_t kRoundShade = 2u;    // DRAY_FLAG_SHADE: back in the domain o
 constexpr int kRoundList = kMaxList + 1;
 // Retries of a pixel's compare-and-swap before the error flag is raised.
 constexpr int kCasLimit = 1 << 20;
+constexpr uint32_t kNoRay = 0xffffffffu;  // no ray (pool exhausted, nothing spawned)
 
 struct RoundArgs {
   SceneDev scene;
@@ -79,9 +80,12 @@ struct RoundArgs {
   unsigned long long* visits_shade;
 };
 
-// Node and triangle counts of one thread's walks (closest hit, occlusion).
+// One thread's counts, added to the frame's counters when it ends: the nodes
+// and triangles of its walks (closest hit, occlusion), its visits and the
+// rays it spawned.
 struct WalkCounts {
   uint32_t rnodes, rtris, snodes, stris;
+  uint32_t vrad, vshadow, vshade, nshadow, nbounce;
 };
 
 __device__ __forceinline__ uint32_t depthOf(int4 m) { return (uint32_t)m.z & 0xffu; }
@@ -170,7 +174,7 @@ __device__ uint32_t newRay(const RoundArgs& a) {
   const uint32_t r = atomicAdd(a.pool_count, 1u);
   if (r >= a.pool_cap) {
     atomicAdd(&a.ctr->arena_overflows, 1ull);
-    return 0xffffffffu;
+    return kNoRay;
   }
   return r;
 }
@@ -199,19 +203,18 @@ __device__ uint32_t shadeHere(const RoundArgs& a, const DomainDev& dom, float4 o
   const V3 pos = v3(dir.x * t + org.x, dir.y * t + org.y, dir.z * t + org.z);
   const int pixid = meta.x, samid = meta.y;
   const uint32_t depth = depthOf(meta) + 1u;
-  uint32_t bounce = 0xffffffffu;
-  unsigned long long nshadow = 0, nvis = 0;
+  uint32_t bounce = kNoRay;
   shadeHit(
       a.env, a.view, dir, v3(w4.x, w4.y, w4.z), pos, ns, unpackRound(col), dom.bsdf, dom.bsdf_p, pixid, samid,
       (int)depth,
       [&](int, V3 wi, V3 w, float tmax, bool valid) {
         if (!valid) return;
-        ++nshadow;
-        ++nvis;
+        ++wc.nshadow;
+        ++wc.vshadow;
         const TravRay tr = makeTravRay(pos, wi);
         if (traverseAny(a.scene, dom, tr, tmax, a.ctr, wc.snodes, wc.stris)) return;
         const uint32_t s = newRay(a);
-        if (s == 0xffffffffu) return;
+        if (s == kNoRay) return;
         int dp = kRoundNone;
         float nt;
         const int nd = advanceRay(a, pos, wi, tmax, a.id, dp, nt);
@@ -225,17 +228,15 @@ __device__ uint32_t shadeHere(const RoundArgs& a, const DomainDev& dom, float4 o
       },
       [&](V3 wi, V3 w) {
         const uint32_t b = newRay(a);
-        if (b == 0xffffffffu) return;
+        if (b == kNoRay) return;
         a.rays.org[b] = make_float4(pos.x, pos.y, pos.z, __int_as_float(0x7f800000));
         a.rays.dir[b] = make_float4(wi.x, wi.y, wi.z, __int_as_float(0x7f800000));
         a.rays.wgt[b] = make_float4(w.x, w.y, w.z, __int_as_float(0x7f800000));
         a.rays.meta[b] = make_int4(pixid, samid, (int)depth, kRoundNone);
         a.rays.hit[b] = make_int4(kRoundNone, 0, 0, 0);
-        atomicAdd(&a.ctr->rays_bounce, 1ull);
+        ++wc.nbounce;
         bounce = b;
       });
-  if (nshadow) atomicAdd(&a.ctr->rays_shadow, nshadow);
-  if (nvis) atomicAdd(&a.ctr->visits_shadow, nvis);
   return bounce;
 }
 
@@ -247,10 +248,10 @@ __device__ uint32_t runRadiance(const RoundArgs& a, const DomainDev& dom, uint32
   int4 meta = a.rays.meta[ray];
   int4 hit = a.rays.hit[ray];
   if (flagsOf(meta) & kRoundShade) {
-    atomicAdd(a.visits_shade, 1ull);
+    ++wc.vshade;
     return shadeHere(a, dom, o4, d4, w4, meta, hit.y, __int_as_float(hit.z), __int_as_float(hit.w), wc);
   }
-  atomicAdd(&a.ctr->visits_radiance, 1ull);
+  ++wc.vrad;
   const V3 org = v3(o4.x, o4.y, o4.z), dir = v3(d4.x, d4.y, d4.z);
   const TravRay tr = makeTravRay(org, dir);
   uint64_t key = kNoHit;
@@ -289,12 +290,12 @@ __device__ uint32_t runRadiance(const RoundArgs& a, const DomainDev& dom, uint32
   } else {
     moveOn();
   }
-  return 0xffffffffu;
+  return kNoRay;
 }
 
 // processShadow: not occluded here -> the next domain, or retired
 __device__ void runShadow(const RoundArgs& a, const DomainDev& dom, uint32_t ray, WalkCounts& wc) {
-  atomicAdd(&a.ctr->visits_shadow, 1ull);
+  ++wc.vshadow;
   const float4 o4 = a.rays.org[ray], d4 = a.rays.dir[ray];
   const V3 org = v3(o4.x, o4.y, o4.z), dir = v3(d4.x, d4.y, d4.z);
   if (traverseAny(a.scene, dom, makeTravRay(org, dir), o4.w, a.ctr, wc.snodes, wc.stris)) return;
@@ -329,9 +330,9 @@ __global__ void __launch_bounds__(128) kRoundRays(RoundArgs a) {
       continue;
     }
     // each spawned ray is one depth deeper: the chain ends within `bounces`
-    for (int guard = 0; guard <= a.view.bounces && ray != 0xffffffffu; ++guard) {
+    for (int guard = 0; guard <= a.view.bounces && ray != kNoRay; ++guard) {
       ray = runRadiance(a, dom, ray, wc);
-      if (ray == 0xffffffffu) break;
+      if (ray == kNoRay) break;
       // a new ray: its list position only, then this domain first
       const float4 o4 = a.rays.org[ray], d4 = a.rays.dir[ray];
       int4 meta = a.rays.meta[ray];
@@ -347,6 +348,11 @@ __global__ void __launch_bounds__(128) kRoundRays(RoundArgs a) {
   if (wc.rtris) atomicAdd(&a.ctr->tris_radiance, (unsigned long long)wc.rtris);
   if (wc.snodes) atomicAdd(&a.ctr->nodes_shadow, (unsigned long long)wc.snodes);
   if (wc.stris) atomicAdd(&a.ctr->tris_shadow, (unsigned long long)wc.stris);
+  if (wc.vrad) atomicAdd(&a.ctr->visits_radiance, (unsigned long long)wc.vrad);
+  if (wc.vshadow) atomicAdd(&a.ctr->visits_shadow, (unsigned long long)wc.vshadow);
+  if (wc.vshade) atomicAdd(a.visits_shade, (unsigned long long)wc.vshade);
+  if (wc.nshadow) atomicAdd(&a.ctr->rays_shadow, (unsigned long long)wc.nshadow);
+  if (wc.nbounce) atomicAdd(&a.ctr->rays_bounce, (unsigned long long)wc.nbounce);
 }
 
 // genEyeRays + isectEyeDomains over the image as one tile (ImgSchedNop,
