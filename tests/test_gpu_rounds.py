@@ -126,3 +126,35 @@ def test_rounds_reject_several_views(lib_built):
         t.trace_views(views)
     assert e.value.code == sg.EINVAL
     t.close()
+
+
+def test_rounds_when_every_ray_misses(lib_built):
+    sc = scenes.wavelet_grid(2, 12, colors="albedo", light="point")
+    t = sg.Tracer(small_config(image_w=32, image_h=16, schedule_policy=5))
+    t.set_scene(sc)
+    t.set_camera((0, 0, 50), (0, 0, 100), (0, 1, 0))  # looking away from the grid
+    img, st = t.trace()
+    assert not img.any() and st["rounds"] == 0 and st["visits_radiance"] == 0
+    assert len(t.debug(sg.DBG_LOADS, 0)) == 0
+    t.close()
+
+
+def test_rounds_on_one_domain(lib_built, oracle_mod):
+    # one domain: every list holds it alone (no domain hierarchy), and a ray
+    # spawned on its surface may start outside its box
+    v = np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    f = np.array([[0, 1, 2], [0, 1, 3], [1, 2, 3], [2, 0, 3]], np.uint32)
+    sc = sg.Scene([sg.Domain(v, f, np.full(4, 0x80a0c0, np.uint32))], [sg.Light(0, (0, 0, 5))])
+    cfg = small_config(image_w=37, image_h=23, ao_mode=0, pixel_samples=3, bounces=3)
+    cam = ((0.1, 0.2, 3), (0, 0, 0), (0, 1, 0))
+    t = sg.Tracer(dict(cfg, schedule_policy=5))
+    t.set_scene(sc)
+    t.set_camera(*cam)
+    img, st = t.trace()
+    o = oracle_mod.Oracle(cfg, sc)
+    o.set_camera(*cam)
+    want, ws, sched = o.render_baseline()
+    for k in COUNTS:
+        assert st[k] == ws[k], (k, st[k], ws[k])
+    assert A.image_rmse(img, want) <= ORDER_RMSE and img[..., :3].max() > 0
+    t.close()
