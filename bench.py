@@ -14,7 +14,7 @@ albedo, one emissive quad light, seeded orbit camera.  Prints one JSON line.
                 RMSE against the reference loop restated on the CPU (oracle
                 mode A), bit equality with the wavefront restatement (mode B),
                 hit and occlusion agreement of every depth's rays
-  the benchmark spec    the 512-domain out-of-core workload (C3) under the plain
+  c3_schedulers the 512-domain out-of-core workload (C3) under the plain
                 speculative order, batched passes and the learned proposal:
                 Mrays/s by ray class, domain loads, bytes copied and bytes read
                 in place from host memory per frame
@@ -267,9 +267,10 @@ def accuracy_report(scene, cfg, cam, mode_a_img, oracle_obj, device: int) -> dic
     return rep
 
 
-def north_star_block(args, device: int) -> dict:
+def c3_schedulers_block(args, device: int) -> dict:
     """C3 (512 domains out of core) under the plain speculative order, the
-    batched passes and the learned proposal: the metric's comparison."""
+    batched passes, the learned proposal, the non-speculative passes and the
+    reference's non-speculative round loop: the metric's comparison."""
     import spray_gb300 as sg
     from spray_gb300 import autotune, scenes
     from oracle import accuracy as A
@@ -280,7 +281,7 @@ def north_star_block(args, device: int) -> dict:
     prep = Path(tempfile.gettempdir()) / f"spray_c3_prepared_{os.getpid()}"
     sg.prepare_scene(scene, prep)
     out = {"workload": describe("c3", spec, cfg0), "policies": {}}
-    frames = max(args.steps, args.ns_frames)
+    frames = max(args.steps, args.c3_frames)
     ref_img = None
     small = None
     for name in ("plain", "batched", "learned", "nonspec", "rounds"):
@@ -367,7 +368,7 @@ def north_star_block(args, device: int) -> dict:
         cfg["schedule_policy"] = POLICIES["learned"][0]
         cfg["learn_frames"] = 1
         threads = os.cpu_count() or 1
-        scale = max(1, cfg0["image_w"] // args.ns_accuracy_size)
+        scale = max(1, cfg0["image_w"] // args.c3_accuracy_size)
         _, _, c, _, mode_a, o = cpu_speculative(scene, cfg, threads, scale)
         tr = sg.Tracer(dict(c, schedule_policy=3, learn_frames=1), device=device)
         tr.set_scene_prepared(prep, len(scene.domains), scene.lights)
@@ -383,7 +384,7 @@ def north_star_block(args, device: int) -> dict:
         # the round loop against the oracle's restatement of the reference's
         # baseline tracer (mode C) on a small frame: the same rounds, loads
         # and visits from a cold cache; the image up to the order of additions
-        rc = dict(cfg0, image_w=args.ns_rounds_size, image_h=args.ns_rounds_size)
+        rc = dict(cfg0, image_w=args.c3_rounds_size, image_h=args.c3_rounds_size)
         oc = dict(rc)
         for k, v in dict(history_size=4, max_samples_per_rank=1 << 20, num_ranks=1, rank=0).items():
             oc.setdefault(k, v)
@@ -435,12 +436,13 @@ def main():
                     help="apply the committed autotuner result for the workload (spray_gb300/tuned)")
     ap.add_argument("--scale", type=int, default=1,
                     help="divide the image size (profiling captures on a small frame only)")
-    ap.add_argument("--north-star", type=int, default=1, choices=[0, 1],
-                    help="1: also run the C3 plain / batched / learned comparison (rank 0 of a single-GPU run)")
-    ap.add_argument("--ns-frames", type=int, default=15, help="timed C3 frames per scheduler")
-    ap.add_argument("--ns-rounds-size", type=int, default=64,
+    ap.add_argument("--c3-schedulers", type=int, default=1, choices=[0, 1],
+                    help="1: also run C3 under every scheduler (plain, batched, learned, non-speculative, "
+                         "the reference's round loop; rank 0 of a single-GPU run)")
+    ap.add_argument("--c3-frames", type=int, default=15, help="timed C3 frames per scheduler")
+    ap.add_argument("--c3-rounds-size", type=int, default=64,
                     help="image size of the round loop's comparison with the oracle")
-    ap.add_argument("--ns-accuracy-size", type=int, default=256, help="C3 accuracy frame width")
+    ap.add_argument("--c3-accuracy-size", type=int, default=256, help="C3 accuracy frame width")
     ap.add_argument("--accuracy", type=int, default=1, choices=[0, 1],
                     help="1: compare the GPU with the oracle on the CPU baseline's reduced frame")
     args = ap.parse_args()
@@ -667,8 +669,8 @@ def main():
                                         "frac": ach / rl["peak"], "ratio_to_kernel_counts": tr["oracle_to_gpu_bytes"],
                                         "sample": f"{c['image_w']}x{c['image_h']} frame of the same workload"}
         o.close()
-    if rank == 0 and world == 1 and args.north_star and args.config == "c2":
-        out["north_star"] = north_star_block(args, local)
+    if rank == 0 and world == 1 and args.c3_schedulers and args.config == "c2":
+        out["c3_schedulers"] = c3_schedulers_block(args, local)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
