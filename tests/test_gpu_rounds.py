@@ -51,7 +51,7 @@ def _compare(oracle_mod, sc, cfg, frames=1, rel=None):
 
 
 @pytest.mark.parametrize("mode,spp,cache", [("pt", 1, -1), ("pt", 2, 8), ("ao", 1, 8), ("ao", 2, -1),
-                                            ("pt", 3, 5)])
+                                            ("pt", 3, 5), ("pt", 1, 1)])
 def test_rounds_match_the_oracle_loop(lib_built, oracle_mod, mode, spp, cache):
     sc = scenes.wavelet_grid(3, 16, colors="albedo", light="point+diffuse" if mode == "pt" else "point")
     cfg = small_config(image_w=48, image_h=36, ao_mode=int(mode == "ao"), ao_samples=2, pixel_samples=spp,
