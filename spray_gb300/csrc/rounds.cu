@@ -78,7 +78,18 @@ struct RoundArgs {
   ShadeEnv env;
   Counters* ctr;
   unsigned long long* visits_shade;
+  uint32_t* hist;  // the round's partition: D counts, total, overflow flag, queued count
 };
+
+// Words after the D counts of the round's histogram.
+constexpr int kHistExtra = 3;
+
+// The kernel that starts a round (kRoundEyes, kRoundRays) zeroes the
+// histogram the partition after it fills (the host has read the last one).
+__device__ __forceinline__ void zeroHist(uint32_t* hist, int D) {
+  if (blockIdx.x == 0)
+    for (int d = threadIdx.x; d < D + kHistExtra; d += blockDim.x) hist[d] = 0u;
+}
 
 // One thread's counts, added to the frame's counters when it ends: the nodes
 // and triangles of its walks (closest hit, occlusion), its visits and the
@@ -313,6 +324,7 @@ __device__ void runShadow(const RoundArgs& a, const DomainDev& dom, uint32_t ray
 // One round: every ray queued in domain a.id, each with the bounce rays its
 // shading spawns in turn (InsituTracer::processRays' temp_q).
 __global__ void __launch_bounds__(128) kRoundRays(RoundArgs a) {
+  zeroHist(a.hist, a.D);
   const uint32_t n = a.seg[2 * a.nseg];
   const DomainDev dom = a.scene.domains[a.id];
   WalkCounts wc{};
@@ -359,6 +371,7 @@ __global__ void __launch_bounds__(128) kRoundRays(RoundArgs a) {
 // src/baseline/baseline_tilers.h:35-47): sample s of pixel p has id
 // spp * p + s, which seeds its jitter when spp > 1 (pixel corners at 1 spp).
 __global__ void kRoundEyes(RoundArgs a, int64_t n) {
+  zeroHist(a.hist, a.D);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const ViewDev& vw = a.view;
@@ -387,15 +400,18 @@ __global__ void kRoundEyes(RoundArgs a, int64_t n) {
 }
 
 // The round's queued rays into the arena, grouped by domain: counts, their
-// offsets (after `base`), then the entries.  hist[D] receives the total.
+// offsets (after `base`), then the entries.
 __global__ void kRoundCount(const uint2* out, const uint32_t* out_count, uint32_t out_cap, uint32_t* hist) {
   const uint32_t n = min(*out_count, out_cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     atomicAdd(&hist[out[i].x], 1u);
 }
 
-__global__ void __launch_bounds__(1024) kRoundOffsets(const uint32_t* hist, int D, uint32_t base,
-                                                      uint32_t* cursor, uint32_t* total) {
+// Also records the overflow flag and the queued count, and clears the queue
+// counter for the next round (the scatter reads the recorded count).
+__global__ void __launch_bounds__(1024) kRoundOffsets(uint32_t* hist, int D, uint32_t base, uint32_t* cursor,
+                                                      uint32_t* out_count, uint32_t out_cap, const Counters* ctr) {
+  uint32_t* total = hist + D;
   __shared__ uint32_t warp_sums[32];
   __shared__ uint32_t carry;
   if (threadIdx.x == 0) carry = base;
@@ -426,17 +442,26 @@ __global__ void __launch_bounds__(1024) kRoundOffsets(const uint32_t* hist, int 
     if (threadIdx.x == blockDim.x - 1) carry += warp_sums[(blockDim.x >> 5) - 1];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *total = carry - base;
+  if (threadIdx.x == 0) {
+    *total = carry - base;
+    if (ctr->arena_overflows) hist[D + 1] = 1u;
+    hist[D + 2] = min(*out_count, out_cap);
+    *out_count = 0u;
+  }
 }
 
-__global__ void kRoundScatter(const uint2* out, const uint32_t* out_count, uint32_t out_cap, uint32_t* cursor,
-                              uint32_t* arena, uint32_t arena_cap, Counters* ctr) {
-  const uint32_t n = min(*out_count, out_cap);
+__global__ void kRoundScatter(const uint2* out, uint32_t* hist, int D, uint32_t* cursor, uint32_t* arena,
+                              uint32_t arena_cap, Counters* ctr) {
+  const uint32_t n = hist[D + 2];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint2 e = out[i];
     const uint32_t k = atomicAdd(&cursor[e.x], 1u);
-    if (k < arena_cap) arena[k] = e.y;
-    else atomicAdd(&ctr->arena_overflows, 1ull);
+    if (k < arena_cap) {
+      arena[k] = e.y;
+    } else {
+      atomicAdd(&ctr->arena_overflows, 1ull);
+      hist[D + 1] = 1u;
+    }
   }
 }
 
@@ -508,7 +533,7 @@ void Tracer::ensureRounds(uint64_t pool, uint64_t arena, uint64_t segs) {
   }
   if (!d_rr_pool) devAlloc(&d_rr_pool, 2);
   if (!d_rr_hist) {
-    devAlloc(&d_rr_hist, (size_t)D + 1);
+    devAlloc(&d_rr_hist, (size_t)D + kHistExtra);
     devAlloc(&d_rr_cursor, (size_t)D);
   }
   if (segs > rr_seg_cap) {
@@ -517,7 +542,7 @@ void Tracer::ensureRounds(uint64_t pool, uint64_t arena, uint64_t segs) {
     h_rr = nullptr;
     devAlloc(&d_rr_seg, 2 * segs + 1);
     // pinned: the segment table going out, the round's counts coming back
-    CK(cudaMallocHost(&h_rr, (2 * segs + 1 + (size_t)D + 1) * sizeof(uint32_t)));
+    CK(cudaMallocHost(&h_rr, (2 * segs + 1 + (size_t)D + kHistExtra) * sizeof(uint32_t)));
     rr_seg_cap = segs;
   }
 }
@@ -557,6 +582,7 @@ void Tracer::traceRounds() {
     a.env = ShadeEnv{d_lights, (int)lights.size(), {cfg.ks[0], cfg.ks[1], cfg.ks[2]}, cfg.shininess, d_ctr};
     a.ctr = d_ctr;
     a.visits_shade = d_rr_pool + 1;
+    a.hist = d_rr_hist;
     // the pool counter and the round's queue counter share d_rr_pool[0];
     // visits_shade lives in d_rr_pool[1]
     CK(cudaMemcpyAsync(a.pool_count, &eyes, sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
@@ -571,20 +597,18 @@ void Tracer::traceRounds() {
     // the round's queued rays into the arena; counts back to the host
     auto partition = [&]() -> bool {
       const int blocks = num_sms * 4;
-      CK(cudaMemsetAsync(d_rr_hist, 0, ((size_t)D + 1) * sizeof(uint32_t), stream));
       kRoundCount<<<blocks, 256, 0, stream>>>(d_rr_out, a.out_count, a.out_cap, d_rr_hist);
-      kRoundOffsets<<<1, 1024, 0, stream>>>(d_rr_hist, D, (uint32_t)arena_fill, d_rr_cursor, d_rr_hist + D);
-      kRoundScatter<<<blocks, 256, 0, stream>>>(d_rr_out, a.out_count, a.out_cap, d_rr_cursor, d_rr_arena,
+      kRoundOffsets<<<1, 1024, 0, stream>>>(d_rr_hist, D, (uint32_t)arena_fill, d_rr_cursor, a.out_count,
+                                            a.out_cap, d_ctr);
+      kRoundScatter<<<blocks, 256, 0, stream>>>(d_rr_out, d_rr_hist, D, d_rr_cursor, d_rr_arena,
                                                 (uint32_t)rr_arena_cap, d_ctr);
       launches += 3;
       uint32_t* h_hist = h_rr + 2 * rr_seg_cap + 1;
-      unsigned long long ovf = 0;
-      CK(cudaMemcpyAsync(h_hist, d_rr_hist, ((size_t)D + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-      CK(cudaMemcpyAsync(&ovf, &d_ctr->arena_overflows, sizeof(ovf), cudaMemcpyDeviceToHost, stream));
-      CK(cudaMemsetAsync(a.out_count, 0, sizeof(uint32_t), stream));
+      CK(cudaMemcpyAsync(h_hist, d_rr_hist, ((size_t)D + kHistExtra) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                         stream));
       CK(cudaStreamSynchronize(stream));
-      d2h_bytes += ((size_t)D + 1) * sizeof(uint32_t) + sizeof(ovf);
-      if (ovf) return false;
+      d2h_bytes += ((size_t)D + kHistExtra) * sizeof(uint32_t);
+      if (h_hist[D + 1]) return false;
       uint64_t off = arena_fill;
       for (int d = 0; d < D; ++d) {
         if (!h_hist[d]) continue;
