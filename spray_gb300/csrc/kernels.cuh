@@ -342,7 +342,10 @@ void launchSchedPartition(cudaStream_t s, const SchedArgs& a, int ndomains, int 
 // Resident blocks per SM of the scheduling kernel for this shared-memory use.
 int schedBlocksPerSm(int D, int nkeys, int dnode_count);
 void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks);
-void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks);
+// The winners' colour and normal into hit_ns: interpolated from the records'
+// barycentrics after an in-core closest-hit launch (interpolate), copied from
+// the records after out-of-core and domain-parallel launches.
+void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks, bool interpolate);
 void launchTraceOccluded(cudaStream_t s, const TraceArgs& a, int nblocks);
 void launchShade(cudaStream_t s, const ShadeArgs& a, int nblocks);
 // Stable compaction of flag[i] != 0 for i < n (n from *n_dev or n_host when

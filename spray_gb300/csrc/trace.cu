@@ -248,7 +248,14 @@ __global__ void __launch_bounds__(256, SPRAY_TRACE_MIN_BLOCKS) kTraceClosest(Tra
       ipt += ntris - t0;
       iph += hit ? 1u : 0u;
     }
-    if (hit) {
+    if (hit && kPack) {
+      // in core the winner's colour and normal are interpolated by kResolve:
+      // the record keeps the barycentrics
+      atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
+      a.rec_key[e] = best_key;
+      a.rec_attr[e] = make_float4(u, v, 0.f, 0.f);
+    } else if (hit) {
+      // out of core the domain may leave the cache before resolve: interpolate now
       atomicMin((unsigned long long*)&a.ray_key[ray], (unsigned long long)best_key);
       const DomArrays g = domArrays(a.scene, dom);
       const uint32_t* f = g.faces + 3 * (size_t)prim;
@@ -297,8 +304,22 @@ void launchTraceClosest(cudaStream_t s, const TraceArgs& a, int nblocks) {
   else kTraceClosest<false><<<nblocks, 256, smem, s>>>(a);
 }
 
-// The entry that holds a ray's final key publishes its colour and normal.
+// Domains whose first global face resolve keeps in shared memory for the
+// winner's domain search (more domains search the device table).
+constexpr int kResolveSmemDomains = 4096;
+
+// The entry that holds a ray's final key publishes its colour and normal:
+// recorded by the trace out of core (kInterp false), interpolated here from
+// the recorded barycentrics in core (TriMeshBuffer::updateIntersection,
+// src/render/trimesh_buffer.cc:328-360).
+template <bool kInterp>
 __global__ void kResolve(TraceArgs a, float4* hit_ns) {
+  __shared__ uint32_t sprim[kInterp ? kResolveSmemDomains : 1];
+  const int D = a.scene.num_domains;
+  const bool stab = kInterp && D <= kResolveSmemDomains;
+  if (stab)
+    for (int k = threadIdx.x; k < D; k += blockDim.x) sprim[k] = a.scene.domains[k].gprim_base;
+  if (kInterp) __syncthreads();
   const uint32_t E = *a.num_entries;
   // four entries per thread per step, their loads in flight together
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -313,13 +334,40 @@ __global__ void kResolve(TraceArgs a, float4* hit_ns) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) ray[q] = k[q] != kNoHit ? a.entries[e0 + q * stride].x & kRayIdMask : 0u;
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (k[q] != kNoHit && a.ray_key[ray[q]] == k[q]) hit_ns[ray[q]] = a.rec_attr[e0 + q * stride];
+    for (int q = 0; q < 4; ++q) {
+      if (k[q] == kNoHit || a.ray_key[ray[q]] != k[q]) continue;
+      const float4 rec = a.rec_attr[e0 + q * stride];
+      if (!kInterp) {
+        hit_ns[ray[q]] = rec;
+        continue;
+      }
+      // the winner's domain: the last whose first global face is <= the hit's
+      const uint32_t gprim = (uint32_t)k[q];
+      int lo = 0, hi = D - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((stab ? sprim[mid] : a.scene.domains[mid].gprim_base) <= gprim) lo = mid;
+        else hi = mid - 1;
+      }
+      const DomainDev dom = a.scene.domains[lo];
+      const DomArrays g = domArrays(a.scene, dom);
+      const uint32_t* f = g.faces + 3 * (size_t)(gprim - dom.gprim_base);
+      const uint32_t i0 = f[0], i1 = f[1], i2 = f[2];
+      const float u = rec.x, v = rec.y;
+      const uint32_t col = interpolateColor(g.colors[i0], g.colors[i1], g.colors[i2], u, v);
+      const float* nb = g.normals;
+      const V3 ns = interpolateNormal(v3(nb[3 * (size_t)i0], nb[3 * (size_t)i0 + 1], nb[3 * (size_t)i0 + 2]),
+                                      v3(nb[3 * (size_t)i1], nb[3 * (size_t)i1 + 1], nb[3 * (size_t)i1 + 2]),
+                                      v3(nb[3 * (size_t)i2], nb[3 * (size_t)i2 + 1], nb[3 * (size_t)i2 + 2]),
+                                      u, v);
+      hit_ns[ray[q]] = make_float4(ns.x, ns.y, ns.z, __uint_as_float(col));
+    }
   }
 }
 
-void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks) {
-  kResolve<<<nblocks, 256, 0, s>>>(a, hit_ns);
+void launchResolve(cudaStream_t s, const TraceArgs& a, float4* hit_ns, int nblocks, bool interpolate) {
+  if (interpolate) kResolve<true><<<nblocks, 256, 0, s>>>(a, hit_ns);
+  else kResolve<false><<<nblocks, 256, 0, s>>>(a, hit_ns);
 }
 
 // Occlusion with persistent, refilling warps: each round, the lanes whose

@@ -1271,7 +1271,8 @@ void Tracer::traceWave(const Wave& w, bool capture) {
       }
       launches += nb;
     }
-    launchResolve(stream, ta, d_hit_ns, nblk);
+    // in core the closest-hit launch left barycentrics for resolve to interpolate
+    launchResolve(stream, ta, d_hit_ns, nblk, !ooc && !situ());
     launches += 1;
     // the winning entry's rank published the hit's normal and colour, the
     // other ranks left zeros: the bytewise maximum is the winner's record
@@ -1627,7 +1628,7 @@ void Tracer::traceWaveBatched(const Wave& w) {
   oocPass(true, false, S, rb);
   for (int b = 0; b < nb_total; ++b) {
     TraceArgs ta = traceArgs(0, S);
-    launchResolve(stream, ta, d_hit_ns, nblk);
+    launchResolve(stream, ta, d_hit_ns, nblk, false);
     if (learned() && !proposal_trained) collectPairs();
     CK(cudaMemsetAsync(d_next_flag, 0, (size_t)w.samples, stream));
     launchShade(stream, shadeArgs(b, S), nblk);
