@@ -124,3 +124,57 @@ def test_static_scratch_zero_rays(lib_built):
                                entries.data_ptr(), 4, starts.data_ptr())
         assert k == 0
         assert np.array_equal(starts.cpu().numpy(), np.zeros(D + 1, np.int32))
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_static_schedule_matches_the_oracle_on_degenerate_inputs(lib_built, oracle_mod, seed):
+    # boxes that overlap, touch, are flat in one or two axes or are points;
+    # rays with zero direction components (infinite inverse), starting inside
+    # boxes, on their faces and on shared faces: the slab tests, the (t, id)
+    # order and the queue positions must equal the oracle's bit for bit
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(seed)
+    D = 48
+    lo = np.round(rng.uniform(-4, 4, (D, 3)) * 2) / 2
+    ext = np.round(rng.uniform(0, 3, (D, 3)) * 2) / 2
+    ext[rng.random((D, 3)) < 0.15] = 0.0  # flat sides, some boxes points
+    lo[D // 2:D // 2 + 4] = lo[0]          # identical boxes
+    ext[D // 2:D // 2 + 4] = ext[0]
+    bounds = np.concatenate([lo, lo + ext], 1).astype(np.float32)
+    n = 20000
+    org = rng.uniform(-5, 5, (n, 3)).astype(np.float32)
+    pick = rng.integers(0, D, n)
+    face = rng.random(n) < 0.3               # start on a box's face or corner
+    org[face] = np.where(rng.random((face.sum(), 3)) < 0.5, bounds[pick[face], :3], bounds[pick[face], 3:])
+    inside = rng.random(n) < 0.2
+    org[inside] = (bounds[pick[inside], :3] + bounds[pick[inside], 3:]) * 0.5
+    dr = rng.normal(size=(n, 3)).astype(np.float32)
+    dr[rng.random((n, 3)) < 0.2] = 0.0       # axis-parallel rays
+    dr[np.all(dr == 0, 1)] = (1, 0, 0)
+    dr = (dr / np.linalg.norm(dr, axis=1, keepdims=True)).astype(np.float32)
+    # the oracle's queues: one Oracle with these boxes as its domains
+    doms = [sg.Domain(np.array([b[:3], b[3:], b[:3]], np.float32), np.array([[0, 1, 2]], np.uint32),
+                      bounds=b) for b in bounds]
+    o = oracle_mod.Oracle(small_config(), sg.Scene(doms, [sg.Light(0, (0, 0, 9))]))
+    want, _ = o.schedule(org, dr)
+    o.close()
+    order = np.lexsort((want["depth"], want["ray"], want["domain"]))  # queue order: domain, then ray
+    want = want[order]
+    dev = torch.device("cuda:0")
+    to4 = lambda a: torch.from_numpy(np.concatenate([a, np.zeros((len(a), 1), np.float32)], 1)).to(dev)
+    bnd = torch.from_numpy(bounds).to(dev)
+    cap = len(want) + 64
+    entries = torch.zeros((cap, 2), dtype=torch.int32, device=dev)
+    starts = torch.zeros(D + 1, dtype=torch.int32, device=dev)
+    o4, d4 = to4(org), to4(dr)  # kept alive: the call takes raw device pointers
+    torch.cuda.synchronize()
+    k = sg.schedule_static(bnd.data_ptr(), D, o4.data_ptr(), d4.data_ptr(), n, 16,
+                           entries.data_ptr(), cap, starts.data_ptr())
+    assert k == len(want) and k > n // 4
+    e = entries[:k].cpu().numpy().view(np.uint32)
+    ks = starts.cpu().numpy().astype(np.int64)
+    dom = np.repeat(np.arange(D), np.diff(ks))
+    assert np.array_equal(dom, want["domain"])
+    assert np.array_equal(e[:, 0] & ((1 << 26) - 1), want["ray"])
+    assert np.array_equal((e[:, 0] >> 26) & 31, want["depth"])
+    assert np.array_equal(e[:, 1], want["tdom"].view(np.uint32))
