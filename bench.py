@@ -104,10 +104,19 @@ def clock_sampler(out: Path):
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
     try:
         f = open(out, "w")
-        return subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                 "-lms", "100"], stdout=f, stderr=subprocess.DEVNULL), f
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                              "-lms", "50"], stdout=f, stderr=subprocess.DEVNULL)
     except Exception:
         return None, None
+    # the timed region starts once the sampler writes (its start-up takes
+    # longer than a few frames)
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < 3.0 and p.poll() is None:
+        f.flush()
+        if out.stat().st_size > 0:
+            break
+        time.sleep(0.01)
+    return p, f
 
 
 def smi_index(local: int) -> int:
