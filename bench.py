@@ -629,6 +629,9 @@ def main():
                                  for k in ("primary", "shadow", "bounce")},
         "visits_per_ray": (s0["visits_radiance"] + s0["visits_shadow"]) / max(nrays, 1),
         "visits_culled": s0["visits_culled"],
+        # primary rays (included in rays_per_frame) whose 16x16 screen bin no
+        # domain box's projection touches: misses, resolved at generation
+        "eyes_culled_per_frame": s0.get("eyes_culled", 0),
         "domain_loads_per_frame": s0["domain_loads"],
         "inplace_domains_per_frame": s0["inplace_domains"],
         "inplace_bytes_per_frame": s0["inplace_bytes"],

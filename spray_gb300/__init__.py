@@ -83,6 +83,7 @@ class StatsC(C.Structure):
         ("inplace_bytes", C.c_int64), ("cache_slots", C.c_int64), ("cache_slot_bytes", C.c_int64),
         ("learn_eval_pairs", C.c_int64), ("learn_top1", C.c_double), ("learn_top1_nearest", C.c_double),
         ("exchange_bytes", C.c_int64), ("rounds", C.c_int64), ("visits_shade", C.c_int64),
+        ("eyes_culled", C.c_int64),
     ]
 
     def asdict(self) -> dict:

@@ -123,6 +123,7 @@ struct Counters {
   unsigned long long nodes_inplace;
   unsigned long long tris_inplace;
   unsigned long long hits_inplace;    // closest hits whose faces, colours and normals were read there
+  unsigned long long eyes_culled;     // primary rays resolved as misses by the screen bins
 };
 
 // Radiance rays of a wave, indexed by sample.
@@ -323,9 +324,19 @@ struct ShadeArgs {
 // ---------------------------------------------------------------- launchers
 // Views (cameras) and tiles are read from device memory, so a captured frame
 // follows camera changes.
+// Screen bins of a single-view frame for eye culling: bin (bx, by) of pixel
+// (x >> bin_shift, y >> bin_shift) lists the domains bin_start[b] ..
+// bin_start[b + 1]; live (one byte per sample) receives 1 for the samples
+// whose bin lists a domain.  live == nullptr: no culling, every sample alive.
+struct EyeCull {
+  const uint32_t* bin_start = nullptr;
+  int bins_x = 0;
+  int bin_shift = 0;
+  uint8_t* live = nullptr;
+};
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles,
                       int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
-                      int32_t* alive_idx, Counters* ctr);
+                      int32_t* alive_idx, const EyeCull& cull, Counters* ctr);
 // scan_tmp holds scan_words words, at least scanTmpWords(nkeys, nchunks) for
 // the fastest scan (fewer give a scan over fewer chunk groups).  Launches 5
 // kernels.

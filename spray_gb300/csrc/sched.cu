@@ -33,12 +33,18 @@ __device__ __forceinline__ uint32_t warpExclusiveScan(uint32_t v, uint32_t* tota
 // (src/ooc/ooc_tracer.inl:84-172) with Camera::generateRay
 // (src/render/camera.h:173-209): u = x / W, v = y / H, jitter drawn from a
 // sampler seeded with the tile-local sample id when pixel_samples > 1.
+//
+// With eye culling (cull.live set), a sample whose pixel lies in a screen bin
+// that no domain box's projection touches is a miss without a domain list (the
+// exact slab test of every domain fails for it): its record is not written,
+// live[i] = 0, and a compaction of `live` makes the alive list.  It still
+// counts as a primary ray.
 __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __restrict__ tiles, int ntiles,
                             int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
-                            int32_t* alive_idx, Counters* ctr) {
+                            int32_t* alive_idx, EyeCull cull, Counters* ctr) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
-    *alive_count = (uint32_t)nsamples;
+    if (!cull.live) *alive_count = (uint32_t)nsamples;
     atomicAdd(&ctr->rays_primary, (unsigned long long)nsamples);
   }
   if (i >= nsamples) return;
@@ -57,6 +63,15 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
   int32_t lp = spp > 1 ? bufid / spp : bufid;
   int x = tl.x + lp % tl.w;
   int y = tl.y + lp / tl.w;
+  if (cull.live) {
+    const int bin = (y >> cull.bin_shift) * cull.bins_x + (x >> cull.bin_shift);
+    const bool live = cull.bin_start[bin] != cull.bin_start[bin + 1];
+    cull.live[i] = live;
+    const unsigned dead = __ballot_sync(__activemask(), !live);
+    if (dead && (threadIdx.x & 31) == __ffs(dead) - 1)
+      atomicAdd(&ctr->eyes_culled, (unsigned long long)__popc(dead));
+    if (!live) return;
+  }
   float fx = (float)x, fy = (float)y;
   if (spp > 1) {
     uint32_t st = rngSeed(bufid);
@@ -69,18 +84,20 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
   rays.pixid[i] = y * vw.image_w + x;
   rays.samid[i] = bufid;
   rays.view[i] = (uint16_t)tl.view;
-  alive_list[i] = (uint32_t)i;
-  alive_idx[i] = (int32_t)i;
+  if (!cull.live) {
+    alive_list[i] = (uint32_t)i;
+    alive_idx[i] = (int32_t)i;
+  }
 }
 
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles, int64_t nsamples,
                       RayBuf rays, uint32_t* alive_list, uint32_t* alive_count, int32_t* alive_idx,
-                      Counters* ctr) {
+                      const EyeCull& cull, Counters* ctr) {
   int threads = 256;
   int64_t blocks = (nsamples + threads - 1) / threads;
   if (blocks < 1) blocks = 1;
   kGenPrimary<<<(unsigned)blocks, threads, 0, s>>>(views, tiles, ntiles, nsamples, rays, alive_list, alive_count,
-                                                   alive_idx, ctr);
+                                                   alive_idx, cull, ctr);
 }
 
 // ---------------------------------------------------------------- schedule

@@ -1171,11 +1171,30 @@ cudaEvent_t Tracer::poolEvent() {
 }
 
 // Generates the wave's primary rays (tiles and camera are already on the device).
+//
+// A single-view frame culls its eye rays by the screen bins: the samples of
+// pixels in bins that no domain box's projection touches have an empty domain
+// list, so they stop here (no record, alive index -1) instead of passing
+// through the depth-0 scheduling, shading and compaction; a compaction of the
+// live flags makes the alive list in sample order.  The debug capture keeps
+// every sample alive (its ray and hit records cover every eye ray).
 void Tracer::beginWave(const Wave& w) {
   cur = 0;
+  EyeCull cull;
+  if (use_bins && fviews.size() == 1 && !cfg.debug_capture && d_bin_start) {
+    cull.bin_start = d_bin_start;
+    cull.bins_x = bins_x;
+    cull.bin_shift = kBinShift;
+    cull.live = d_next_flag;
+  }
   launchGenPrimary(stream, d_views, d_tiles + w.first_tile, w.num_tiles, w.samples, rays[0], d_alive_list,
-                   d_alive_count, d_alive_idx, d_ctr);
+                   d_alive_count, d_alive_idx, cull, d_ctr);
   launches += 1;
+  if (cull.live) {
+    launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count, d_alive_idx,
+                  d_block_tmp, compact_blocks);
+    launches += 3;
+  }
 }
 
 ShadeArgs Tracer::shadeArgs(int b, int S) {
@@ -2147,6 +2166,7 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
       st->exchange_bytes = reduce_bytes;
       st->rounds = rounds;
       st->visits_shade = visits_shade;
+      st->eyes_culled = (int64_t)ctr.eyes_culled;
     }
     return;
   }
