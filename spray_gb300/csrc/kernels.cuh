@@ -337,6 +337,8 @@ struct EyeCull {
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles,
                       int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
                       int32_t* alive_idx, const EyeCull& cull, Counters* ctr);
+// Adds nsamples - *alive_count to Counters::eyes_culled (after the live flags' compaction).
+void launchCountCulled(cudaStream_t s, const uint32_t* alive_count, int64_t nsamples, Counters* ctr);
 // scan_tmp holds scan_words words, at least scanTmpWords(nkeys, nchunks) for
 // the fastest scan (fewer give a scan over fewer chunk groups).  Launches 5
 // kernels.

@@ -67,9 +67,6 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
     const int bin = (y >> cull.bin_shift) * cull.bins_x + (x >> cull.bin_shift);
     const bool live = cull.bin_start[bin] != cull.bin_start[bin + 1];
     cull.live[i] = live;
-    const unsigned dead = __ballot_sync(__activemask(), !live);
-    if (dead && (threadIdx.x & 31) == __ffs(dead) - 1)
-      atomicAdd(&ctr->eyes_culled, (unsigned long long)__popc(dead));
     if (!live) return;
   }
   float fx = (float)x, fy = (float)y;
@@ -88,6 +85,17 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
     alive_list[i] = (uint32_t)i;
     alive_idx[i] = (int32_t)i;
   }
+}
+
+// The culled eye rays of a wave: its samples less the live ones the
+// compaction kept (one thread; a counter per culled warp would serialise
+// hundreds of thousands of atomics on one address).
+__global__ void kCountCulled(const uint32_t* alive_count, int64_t nsamples, Counters* ctr) {
+  ctr->eyes_culled += (unsigned long long)(nsamples - (int64_t)*alive_count);
+}
+
+void launchCountCulled(cudaStream_t s, const uint32_t* alive_count, int64_t nsamples, Counters* ctr) {
+  kCountCulled<<<1, 1, 0, s>>>(alive_count, nsamples, ctr);
 }
 
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles, int64_t nsamples,

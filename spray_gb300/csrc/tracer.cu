@@ -1193,7 +1193,8 @@ void Tracer::beginWave(const Wave& w) {
   if (cull.live) {
     launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count, d_alive_idx,
                   d_block_tmp, compact_blocks);
-    launches += 3;
+    launchCountCulled(stream, d_alive_count, w.samples, d_ctr);
+    launches += 4;
   }
 }
 
