@@ -216,8 +216,8 @@ typedef struct spray_gpu_stats {
   int64_t visits_shade;     /* policy 5: rays run in the domain of their hit for shading only */
   int64_t eyes_culled;      /* primary rays (counted in rays_primary) resolved as misses at
                                generation: their pixel's 16x16 screen bin touches no domain
-                               box's projection, so every slab test fails for them; single-view
-                               frames without debug_capture */
+                               box's projection, so every slab test fails for them; frames
+                               without debug_capture */
 } spray_gpu_stats;
 
 /* ---------------------------------------------------------------- setup */

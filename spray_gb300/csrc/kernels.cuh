@@ -182,6 +182,8 @@ struct ViewDev {
   float ao_max_distance;
   int64_t pixel_base;   // first pixel of the view in the frame's image buffer
   double scale;         // retire weight scale, 1 / spp
+  int32_t bin_base;     // the view's first screen bin in the frame's bin table
+  int32_t bins_x;       // screen bins per image row
 };
 
 // Scheduling of one ray set into per-domain queues.
@@ -198,10 +200,12 @@ struct SchedArgs {
   const BvhNode4* dnodes;     // 4-wide hierarchy over the domain boxes (null: test every domain)
   int dnode_count;
   const float* dboxes;        // domain boxes, 6 floats each (null: staged from the domain table)
-  // primary rays: candidate domains per screen bin (null: not primary rays)
-  const uint32_t* bin_start;  // [bins_x * bins_y + 1]
+  // primary rays: candidate domains per screen bin (null: not primary rays);
+  // a ray's bins are those of its view (ViewDev::bin_base, bins_x)
+  const uint32_t* bin_start;  // [all views' bins + 1]
   const uint16_t* bin_ids;
-  int bins_x, bin_shift, image_w;
+  const ViewDev* views;
+  int bin_shift;
   // outputs
   uint2* arena;               // per-ray sorted (domain | depth << 16, tdom) lists
   unsigned long long* arena_top;
@@ -324,13 +328,13 @@ struct ShadeArgs {
 // ---------------------------------------------------------------- launchers
 // Views (cameras) and tiles are read from device memory, so a captured frame
 // follows camera changes.
-// Screen bins of a single-view frame for eye culling: bin (bx, by) of pixel
-// (x >> bin_shift, y >> bin_shift) lists the domains bin_start[b] ..
-// bin_start[b + 1]; live (one byte per sample) receives 1 for the samples
-// whose bin lists a domain.  live == nullptr: no culling, every sample alive.
+// Screen bins for eye culling: pixel (x, y) of a view lies in bin
+// view.bin_base + (y >> bin_shift) * view.bins_x + (x >> bin_shift), which
+// lists the domains bin_start[b] .. bin_start[b + 1]; live (one byte per
+// sample) receives 1 for the samples whose bin lists a domain.
+// live == nullptr: no culling, every sample alive.
 struct EyeCull {
   const uint32_t* bin_start = nullptr;
-  int bins_x = 0;
   int bin_shift = 0;
   uint8_t* live = nullptr;
 };

@@ -64,7 +64,7 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
   int x = tl.x + lp % tl.w;
   int y = tl.y + lp / tl.w;
   if (cull.live) {
-    const int bin = (y >> cull.bin_shift) * cull.bins_x + (x >> cull.bin_shift);
+    const int bin = vw.bin_base + (y >> cull.bin_shift) * vw.bins_x + (x >> cull.bin_shift);
     const bool live = cull.bin_start[bin] != cull.bin_start[bin + 1];
     cull.live[i] = live;
     if (!live) return;
@@ -217,8 +217,9 @@ __global__ void __launch_bounds__(kSchedThreads, kMinBlocks) kSchedLists(SchedAr
       if (a.bin_start) {
         // primary rays: the domains whose projected box covers this pixel's bin
         const int pid = a.rays.pixid[rid];
-        const int bx = (pid % a.image_w) >> a.bin_shift, by = (pid / a.image_w) >> a.bin_shift;
-        const int bin = by * a.bins_x + bx;
+        const ViewDev& vw = a.views[a.rays.view[rid]];
+        const int bx = (pid % vw.image_w) >> a.bin_shift, by = (pid / vw.image_w) >> a.bin_shift;
+        const int bin = vw.bin_base + by * vw.bins_x + bx;
         const uint32_t c0 = a.bin_start[bin], c1 = a.bin_start[bin + 1];
         for (uint32_t c = c0; c < c1; ++c) consider((int)a.bin_ids[c]);
       } else if (NN == 0) {

@@ -1075,12 +1075,11 @@ void Tracer::schedule(bool shadow, int order_by_depth, uint32_t* count, uint32_t
   a.dnodes = d_dnodes;
   a.dboxes = d_dboxes;
   a.dnode_count = dnode_count;
-  if (primary && use_bins && fviews.size() == 1) {
+  if (primary && use_bins) {
     a.bin_start = d_bin_start;
     a.bin_ids = d_bin_ids;
-    a.bins_x = bins_x;
+    a.views = d_views;
     a.bin_shift = kBinShift;
-    a.image_w = fviews[0].w;
   }
   a.arena = d_arena;
   a.arena_top = d_arena_top;
@@ -1172,18 +1171,17 @@ cudaEvent_t Tracer::poolEvent() {
 
 // Generates the wave's primary rays (tiles and camera are already on the device).
 //
-// A single-view frame culls its eye rays by the screen bins: the samples of
-// pixels in bins that no domain box's projection touches have an empty domain
-// list, so they stop here (no record, alive index -1) instead of passing
-// through the depth-0 scheduling, shading and compaction; a compaction of the
-// live flags makes the alive list in sample order.  The debug capture keeps
-// every sample alive (its ray and hit records cover every eye ray).
+// The eye rays are culled by the screen bins: the samples of pixels in bins
+// that no domain box's projection touches have an empty domain list, so they
+// stop here (no record, alive index -1) instead of passing through the
+// depth-0 scheduling, shading and compaction; a compaction of the live flags
+// makes the alive list in sample order.  The debug capture keeps every sample
+// alive (its ray and hit records cover every eye ray).
 void Tracer::beginWave(const Wave& w) {
   cur = 0;
   EyeCull cull;
-  if (use_bins && fviews.size() == 1 && !cfg.debug_capture && d_bin_start) {
+  if (use_bins && !cfg.debug_capture && d_bin_start) {
     cull.bin_start = d_bin_start;
-    cull.bins_x = bins_x;
     cull.bin_shift = kBinShift;
     cull.live = d_next_flag;
   }
@@ -1884,27 +1882,11 @@ void Tracer::captureFrame() {
   graph_occl = occl_events;
 }
 
-// Screen bins of the primary rays.  Each domain box is projected through the
-// camera onto the image plane; the pixel rectangle of its 8 corners, widened
-// by two pixels, lists the domain in every bin it touches.  A box with a
-// corner at or behind the camera plane is listed everywhere.  A ray can only
-// pass the exact slab test of a box whose projection contains its pixel, so
-// the per-bin lists are supersets of what the full test would find.
-void Tracer::buildScreenBins() {
-  const int W = fviews[0].w, H = fviews[0].h;
-  const CameraDev& cam = fviews[0].cam;
-  // the bins depend only on the camera, the image size and the domain boxes:
-  // unchanged since the last build, the device copy is still current
-  std::vector<unsigned char> key(sizeof(CameraDev) + 2 * sizeof(int));
-  std::memcpy(key.data(), &cam, sizeof(CameraDev));
-  std::memcpy(key.data() + sizeof(CameraDev), &W, sizeof(int));
-  std::memcpy(key.data() + sizeof(CameraDev) + sizeof(int), &H, sizeof(int));
-  if (key == bins_key && d_bin_start && d_bin_ids) return;
-  bins_key = key;
-  bins_x = (W + kBinSize - 1) / kBinSize;
-  bins_y = (H + kBinSize - 1) / kBinSize;
-  const int nb = bins_x * bins_y;
-  std::vector<std::vector<uint16_t>> lists(nb);
+// The bins of one view (bins_x per row) in lists[0 ..]: the domains whose
+// projected, widened box touches each bin, nearest box first.
+void Tracer::binView(const FrameView& f, std::vector<uint16_t>* lists, int bins_x) const {
+  const int W = f.w, H = f.h;
+  const CameraDev& cam = f.cam;
   // camera frame in double: P(u, v) = ll + u wv + v hv, viewing along -w
   double pos[3], ll[3], wv[3], hv[3], fw[3];
   for (int k = 0; k < 3; ++k) {
@@ -1962,6 +1944,44 @@ void Tracer::buildScreenBins() {
     for (int by = y0 / kBinSize; by <= y1 / kBinSize; ++by)
       for (int bx = x0 / kBinSize; bx <= x1 / kBinSize; ++bx) lists[by * bins_x + bx].push_back((uint16_t)d);
   }
+}
+
+// Screen bins of the primary rays, per view.  Each domain box is projected
+// through the view's camera onto its image plane; the pixel rectangle of its 8
+// corners, widened by two pixels, lists the domain in every bin it touches.  A
+// box with a corner at or behind the camera plane is listed everywhere.  A ray
+// can only pass the exact slab test of a box whose projection contains its
+// pixel, so the per-bin lists are supersets of what the full test would find.
+// The views' bins lie back to back in one table (ViewDev::bin_base, bins_x).
+void Tracer::buildScreenBins() {
+  // the bins depend only on the cameras, the image sizes and the domain boxes:
+  // unchanged since the last build, the device copy is still current
+  const size_t vk = sizeof(CameraDev) + 2 * sizeof(int);
+  std::vector<unsigned char> key(fviews.size() * vk);
+  for (size_t v = 0; v < fviews.size(); ++v) {
+    std::memcpy(key.data() + v * vk, &fviews[v].cam, sizeof(CameraDev));
+    std::memcpy(key.data() + v * vk + sizeof(CameraDev), &fviews[v].w, sizeof(int));
+    std::memcpy(key.data() + v * vk + sizeof(CameraDev) + sizeof(int), &fviews[v].h, sizeof(int));
+  }
+  const bool current = key == bins_key && d_bin_start && d_bin_ids;
+  if (!current) {
+    bins_key = key;
+    bin_view_base.assign(fviews.size(), 0);
+    bin_view_x.assign(fviews.size(), 0);
+  }
+  int nb = 0;
+  for (size_t v = 0; v < fviews.size(); ++v) {
+    if (!current) {
+      bin_view_base[v] = nb;
+      bin_view_x[v] = (fviews[v].w + kBinSize - 1) / kBinSize;
+    }
+    hviews[v].bin_base = bin_view_base[v];
+    hviews[v].bins_x = bin_view_x[v];
+    nb += bin_view_x[v] * ((fviews[v].h + kBinSize - 1) / kBinSize);
+  }
+  if (current) return;
+  std::vector<std::vector<uint16_t>> lists(nb);
+  for (size_t v = 0; v < fviews.size(); ++v) binView(fviews[v], lists.data() + bin_view_base[v], bin_view_x[v]);
   std::vector<uint32_t> start(nb + 1, 0);
   for (int b = 0; b < nb; ++b) start[b + 1] = start[b] + (uint32_t)lists[b].size();
   std::vector<uint16_t> ids(std::max<uint32_t>(start[nb], 1));
@@ -2059,7 +2079,7 @@ void Tracer::traceFrame(float* out, bool out_is_device, spray_gpu_stats* st) {
     visits_shade = 0;
     use_pred_order = false;
     CK(cudaEventRecord(ev_start, stream));
-    if (use_bins && fviews.size() == 1) buildScreenBins();
+    if (use_bins) buildScreenBins();
     CK(cudaMemcpyAsync(d_views, hviews.data(), hviews.size() * sizeof(ViewDev), cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_tiles, wave_tiles.data(), wave_tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice,
                        stream));

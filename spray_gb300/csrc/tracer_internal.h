@@ -183,6 +183,7 @@ class Tracer {
   void predictDomainCounts(bool run_predict);
   void trainProposal();
   void buildScreenBins();
+  void binView(const FrameView& f, std::vector<uint16_t>* lists, int bins_x) const;
   TraceArgs traceArgs(int order_by_depth, int S);
   SceneDev sceneDev() const;
   cudaEvent_t poolEvent();
@@ -288,7 +289,7 @@ class Tracer {
   static constexpr int kBinSize = 1 << kBinShift;
   bool use_bins = true;
   std::vector<unsigned char> bins_key;  // camera and image the current bins were built for
-  int bins_x = 0, bins_y = 0;
+  std::vector<int32_t> bin_view_base, bin_view_x;  // per view: first bin, bins per row
   uint32_t* d_bin_start = nullptr;
   uint16_t* d_bin_ids = nullptr;
   size_t bin_start_cap = 0, bin_ids_cap = 0;

@@ -1,9 +1,9 @@
-"""Eye culling by the screen bins: in a single-view frame, the samples of
-pixels whose 16x16 bin no domain box's projection touches stop at generation
+"""Eye culling by the screen bins: the samples of pixels whose 16x16 bin no domain box's projection touches stop at generation
 (no domain list is possible for them) and never enter the alive list.
 
 The debug capture keeps every sample alive, so the same frame traced with and
-without it must give the bit-identical image and the same ray counts; the
+without it must give the bit-identical image and the same ray counts, for one
+view and for a multi-view batch (each view has its own bins); the
 culled samples must be among those the capture shows without any queue entry;
 and the culled frame must equal the oracle's wavefront image bit for bit."""
 import numpy as np
@@ -63,15 +63,24 @@ def test_culled_eyes_keep_the_image_and_the_counts(lib_built, oracle_mod, mode, 
     o.close()
 
 
-def test_no_culling_with_several_views(lib_built):
-    # the bins belong to one camera: a multi-view batch keeps every sample
-    sc = scenes.wavelet_grid(2, 12, colors="albedo", light="point")
-    t = sg.Tracer(small_config(image_w=64, image_h=48))
-    t.set_scene(sc)
+def test_culled_eyes_in_a_multi_view_batch(lib_built):
+    # each view has its own bins; the batch equals the same views traced with
+    # every sample alive (debug capture), view by view and bit for bit
+    sc = scenes.wavelet_grid(3, 14, colors="albedo", light="point+diffuse")
     views = []
-    for k in range(2):
+    for k, (w, h, spp, ao) in enumerate([(96, 64, 2, 0), (64, 64, 1, 1), (128, 80, 3, 0)]):
         pos, look, up = scenes.orbit_camera(sc, frame=k)
-        views.append(dict(position=pos + 2.0 * (pos - look), lookat=look, up=up, vfov=60.0))
-    _, st = t.trace_views(views)
-    assert st["eyes_culled"] == 0 and st["rays_primary"] == 2 * 64 * 48
-    t.close()
+        views.append(dict(position=look + 1.5 * (pos - look), lookat=look, up=up, vfov=60.0, image_w=w,
+                          image_h=h, pixel_samples=spp, ao_mode=ao, bounces=1 if ao else 3, ao_samples=2))
+    out = []
+    for kw in ({}, dict(debug_capture=1)):
+        t = sg.Tracer(small_config(max_samples_per_rank=4096), **kw)
+        t.set_scene(sc)
+        out.append(t.trace_views(views))
+        t.close()
+    (imgs, st), (imgs_c, st_c) = out
+    assert st_c["eyes_culled"] == 0 and st["eyes_culled"] > 0
+    for a, b in zip(imgs, imgs_c):
+        assert np.array_equal(bits(a), bits(b))
+    for k in RAYS:
+        assert st[k] == st_c[k], k
