@@ -340,7 +340,7 @@ struct EyeCull {
 };
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles,
                       int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
-                      int32_t* alive_idx, const EyeCull& cull, Counters* ctr);
+                      const EyeCull& cull, Counters* ctr);
 // Adds nsamples - *alive_count to Counters::eyes_culled (after the live flags' compaction).
 void launchCountCulled(cudaStream_t s, const uint32_t* alive_count, int64_t nsamples, Counters* ctr);
 // scan_tmp holds scan_words words, at least scanTmpWords(nkeys, nchunks) for
@@ -384,9 +384,10 @@ void launchCompactList(cudaStream_t s, const uint32_t* src, const uint32_t* n_de
 void launchCompactCounted(cudaStream_t s, const uint8_t* flag, const uint32_t* n_dev, uint32_t n_mul,
                           uint32_t* list, uint32_t* count, int32_t* index_of, const uint32_t* src,
                           uint32_t* block_tmp, int nblocks);
-void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
-                      const ViewDev* views, const int32_t* alive_idx, const ShadowBuf sh,
-                      const uint8_t* flag, int slots, int nblocks);
+// Adds the unoccluded shadow rays of the alive list's samples (*count of them,
+// shadow slot k of entry j at j * slots + k) to their pixels.
+void launchRetire(cudaStream_t s, float4* image, const ViewDev* views, const uint32_t* list, const uint32_t* count,
+                  const RayBuf& rays, const ShadowBuf& sh, const uint8_t* flag, int slots, int nblocks);
 // Uploads the constant tables of the shader (once per device).
 void initShadeTables();
 void launchScores(cudaStream_t s, const long long* dstats, int ndomains, int list_size,

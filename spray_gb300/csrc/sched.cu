@@ -41,7 +41,7 @@ __device__ __forceinline__ uint32_t warpExclusiveScan(uint32_t v, uint32_t* tota
 // counts as a primary ray.
 __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __restrict__ tiles, int ntiles,
                             int64_t nsamples, RayBuf rays, uint32_t* alive_list, uint32_t* alive_count,
-                            int32_t* alive_idx, EyeCull cull, Counters* ctr) {
+                            EyeCull cull, Counters* ctr) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     if (!cull.live) *alive_count = (uint32_t)nsamples;
@@ -81,10 +81,7 @@ __global__ void kGenPrimary(const ViewDev* __restrict__ views, const TileDev* __
   rays.pixid[i] = y * vw.image_w + x;
   rays.samid[i] = bufid;
   rays.view[i] = (uint16_t)tl.view;
-  if (!cull.live) {
-    alive_list[i] = (uint32_t)i;
-    alive_idx[i] = (int32_t)i;
-  }
+  if (!cull.live) alive_list[i] = (uint32_t)i;
 }
 
 // The culled eye rays of a wave: its samples less the live ones the
@@ -99,13 +96,13 @@ void launchCountCulled(cudaStream_t s, const uint32_t* alive_count, int64_t nsam
 }
 
 void launchGenPrimary(cudaStream_t s, const ViewDev* views, const TileDev* tiles, int ntiles, int64_t nsamples,
-                      RayBuf rays, uint32_t* alive_list, uint32_t* alive_count, int32_t* alive_idx,
-                      const EyeCull& cull, Counters* ctr) {
+                      RayBuf rays, uint32_t* alive_list, uint32_t* alive_count, const EyeCull& cull,
+                      Counters* ctr) {
   int threads = 256;
   int64_t blocks = (nsamples + threads - 1) / threads;
   if (blocks < 1) blocks = 1;
   kGenPrimary<<<(unsigned)blocks, threads, 0, s>>>(views, tiles, ntiles, nsamples, rays, alive_list, alive_count,
-                                                   alive_idx, cull, ctr);
+                                                   cull, ctr);
 }
 
 // ---------------------------------------------------------------- schedule

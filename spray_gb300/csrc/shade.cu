@@ -156,100 +156,91 @@ void launchShade(cudaStream_t s, const ShadeArgs& a, int nblocks) {
   kShade<<<nblocks, 256, 0, s>>>(a);
 }
 
-// Per pixel of the wave: samples in order, slots in order, each unoccluded
-// shadow ray adds w * (1 / spp) with the double-precision scale of
-// HdrImage::add (src/display/image.h:99-109).
-// Per pixel of the wave: its tile (binary search on pix_base), its samples
-// (tile-local pixel lp holds samples lp * spp .. lp * spp + spp - 1), its view's
-// image slot and scale; samples and slots in order, the sum in double.
+// Retire (CommitBuffer::retire, src/ooc/ooc_tcontext.inl:123-135, with
+// HdrImage::add, src/display/image.h:99-109): per pixel, its samples in order,
+// each sample's slots in order, every unoccluded shadow ray adds w * (1 / spp)
+// in double precision.
 //
-// A block takes 256 consecutive pixels, whose samples are one contiguous
-// range: their alive indices are staged in shared memory with coalesced loads
-// (one pad word per 32, so that each thread's run of spp indices is read
-// without bank conflicts) when the range fits kRetireStage, else read directly.
-constexpr int kRetireStage = 4096;
+// Only the pixels with a sample alive at this depth can receive anything, so
+// the kernel walks the depth's alive list (samples in order; a pixel's samples
+// are consecutive sample ids s0 .. s0 + spp - 1, s0 = s - samid % spp).  A warp
+// takes the list 32 entries at a time and queues the entries that start a
+// pixel (the previous entry lies before s0) in a per-warp FIFO; once 32 wait
+// (or the list ends) every lane adds one pixel's contributions.  The alive
+// index of an entry is its position in the list, so shadow slot k of entry j
+// is j * S + k.
+__device__ __forceinline__ void retirePixel(float4* image, const ViewDev* __restrict__ views,
+                                            const uint32_t* __restrict__ list, uint32_t n, uint32_t j,
+                                            const RayBuf& rays, const ShadowBuf& sh,
+                                            const uint8_t* __restrict__ flag, int S) {
+  const uint32_t s = list[j];
+  const ViewDev& vw = views[rays.view[s]];
+  const uint32_t send = s - (uint32_t)(rays.samid[s] % vw.spp) + (uint32_t)vw.spp;
+  float4* px = image + vw.pixel_base + rays.pixid[s];
+  const double scale = vw.scale;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool touched = false;
+  for (uint32_t q = j; q < n; ++q) {
+    if (q > j && list[q] >= send) break;
+    for (int k = 0; k < S; ++k) {
+      const uint32_t sid = q * (uint32_t)S + (uint32_t)k;
+      if (!flag[sid] || sh.occluded[sid]) continue;
+      const float4 w = sh.wgt[sid];
+      if (!touched) acc = *px;
+      acc.x = (float)((double)acc.x + scale * (double)w.x);
+      acc.y = (float)((double)acc.y + scale * (double)w.y);
+      acc.z = (float)((double)acc.z + scale * (double)w.z);
+      touched = true;
+    }
+  }
+  if (touched) *px = acc;
+}
 
-__global__ void __launch_bounds__(256) kRetire(float4* image, const TileDev* __restrict__ tiles, int ntiles,
-                                               int64_t npix, const ViewDev* __restrict__ views,
-                                               const int32_t* __restrict__ alive_idx, ShadowBuf sh,
+__global__ void __launch_bounds__(256) kRetire(float4* image, const ViewDev* __restrict__ views,
+                                               const uint32_t* __restrict__ list,
+                                               const uint32_t* __restrict__ count, RayBuf rays, ShadowBuf sh,
                                                const uint8_t* __restrict__ flag, int S) {
-  __shared__ int32_t sidx[kRetireStage + kRetireStage / 32];
-  __shared__ int64_t range[2];
-  for (int64_t p0 = (int64_t)blockIdx.x * blockDim.x; p0 < npix; p0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = p0 + threadIdx.x;
-    const bool valid = p < npix;
-    int lo = 0;
-    if (valid) {
-      int hi = ntiles - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (tiles[mid].pix_base <= p) lo = mid;
-        else hi = mid - 1;
+  __shared__ uint32_t fifo[8][64];
+  uint32_t* q = fifo[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  uint32_t below;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(below));
+  const uint32_t n = *count;
+  const uint32_t nchunks = (n + 31u) >> 5;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  int nq = 0;
+  for (uint32_t c = warp;; c += nwarps) {
+    const bool more = c < nchunks;
+    if (more) {
+      const uint32_t j = (c << 5) + lane;
+      bool head = false;
+      if (j < n) {
+        const uint32_t s = list[j];
+        const uint32_t s0 = s - (uint32_t)(rays.samid[s] % views[rays.view[s]].spp);
+        head = j == 0 || list[j - 1] < s0;
       }
+      const uint32_t hm = __ballot_sync(0xffffffffu, head);
+      if (head) q[nq + __popc(hm & below)] = j;  // nq < 32 here, so at most 63 queued
+      nq += __popc(hm);
+      __syncwarp();
     }
-    const TileDev tl = tiles[lo];
-    const int spp = tl.spp;
-    const int64_t lp = p - tl.pix_base;
-    const int64_t s0 = tl.sample_base + lp * spp;
-    if (threadIdx.x == 0) range[0] = s0;
-    if (p == min(npix, p0 + (int64_t)blockDim.x) - 1) range[1] = s0 + spp;
-    __syncthreads();
-    const int64_t sbeg = range[0], nstage = range[1] - range[0];
-    const bool staged = nstage <= kRetireStage;
-    if (staged) {
-      // 8 loads in flight per thread before their shared-memory stores
-      for (int j0 = threadIdx.x; j0 < (int)nstage; j0 += 8 * blockDim.x) {
-        int32_t v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int j = j0 + u * (int)blockDim.x;
-          v[u] = j < (int)nstage ? alive_idx[sbeg + j] : 0;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int j = j0 + u * (int)blockDim.x;
-          if (j < (int)nstage) sidx[j + (j >> 5)] = v[u];
-        }
-      }
+    while (nq >= 32 || (!more && nq > 0)) {
+      const int take = min(nq, 32), rest = nq - take;
+      if (lane < take) retirePixel(image, views, list, n, q[lane], rays, sh, flag, S);
+      const uint32_t moved = lane < rest ? q[take + lane] : 0u;
+      __syncwarp();
+      if (lane < rest) q[lane] = moved;
+      __syncwarp();
+      nq = rest;
     }
-    __syncthreads();
-    if (valid) {
-      const ViewDev& vw = views[tl.view];
-      const double scale = vw.scale;
-      const int lpi = (int)lp;  // tile-local pixel (32-bit division)
-      const int x = tl.x + lpi % tl.w, y = tl.y + lpi / tl.w;
-      float4* px = image + vw.pixel_base + (int64_t)y * vw.image_w + x;
-      float4 acc = *px;
-      bool touched = false;
-      const int f0 = (int)(s0 - sbeg);
-      for (int s = 0; s < spp; ++s) {
-        const int f = f0 + s;
-        const int32_t ai = staged ? sidx[f + (f >> 5)] : alive_idx[s0 + s];
-        if (ai < 0) continue;
-        for (int k = 0; k < S; ++k) {
-          uint32_t sid = (uint32_t)ai * S + k;
-          if (!flag[sid] || sh.occluded[sid]) continue;
-          float4 w = sh.wgt[sid];
-          acc.x = (float)((double)acc.x + scale * (double)w.x);
-          acc.y = (float)((double)acc.y + scale * (double)w.y);
-          acc.z = (float)((double)acc.z + scale * (double)w.z);
-          touched = true;
-        }
-      }
-      if (touched) *px = acc;
-    }
-    __syncthreads();  // the next group restages sidx and range
+    if (!more) break;
   }
 }
 
-void launchRetireImpl(cudaStream_t s, float4* image, const TileDev* tiles, int ntiles, int64_t npix,
-                      const ViewDev* views, const int32_t* alive_idx, const ShadowBuf sh,
-                      const uint8_t* flag, int slots, int nblocks) {
-  // one 256-pixel group per block where the grid allows (the staged loads of
-  // many blocks overlap), at least nblocks
-  const int64_t groups = (npix + 255) / 256;
-  const int64_t blocks = std::max<int64_t>(nblocks, std::min<int64_t>(groups, 1 << 24));
-  kRetire<<<(unsigned)blocks, 256, 0, s>>>(image, tiles, ntiles, npix, views, alive_idx, sh, flag, slots);
+void launchRetire(cudaStream_t s, float4* image, const ViewDev* views, const uint32_t* list, const uint32_t* count,
+                  const RayBuf& rays, const ShadowBuf& sh, const uint8_t* flag, int slots, int nblocks) {
+  kRetire<<<nblocks, 256, 0, s>>>(image, views, list, count, rays, sh, flag, slots);
 }
 
 }  // namespace spray

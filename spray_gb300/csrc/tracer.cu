@@ -393,7 +393,6 @@ void Tracer::freeBuffers() {
   devFree(d_alive_list);
   devFree(d_alive_list2);
   devFree(d_alive_count2);
-  devFree(d_alive_idx);
   devFree(d_alive_count);
   devFree(d_next_flag);
   devFree(d_ray_key);
@@ -423,7 +422,6 @@ void Tracer::freeBuffers() {
   devFree(d_sentries);
   devFree(d_skey_start);
   devFree(d_snum_entries);
-  devFree(d_alive_idx_prev);
   devFree(d_rec_key);
   devFree(d_rec_attr);
   devFree(d_work);
@@ -1005,7 +1003,6 @@ void Tracer::ensureBuffers(int64_t nsamples) {
   devAlloc(&d_alive_list, N);
   devAlloc(&d_alive_list2, N);
   devAlloc(&d_alive_count2, 1);
-  devAlloc(&d_alive_idx, N);
   devAlloc(&d_alive_count, 1);
   devAlloc(&d_next_flag, N);
   devAlloc(&d_ray_key, N);
@@ -1038,7 +1035,6 @@ void Tracer::ensureBuffers(int64_t nsamples) {
     devAlloc(&d_sentries, E);
     devAlloc(&d_skey_start, nkeys + 1);
     devAlloc(&d_snum_entries, 1);
-    devAlloc(&d_alive_idx_prev, N);
   }
   devAlloc(&d_rec_key, E);
   devAlloc(&d_rec_attr, E);
@@ -1186,10 +1182,10 @@ void Tracer::beginWave(const Wave& w) {
     cull.live = d_next_flag;
   }
   launchGenPrimary(stream, d_views, d_tiles + w.first_tile, w.num_tiles, w.samples, rays[0], d_alive_list,
-                   d_alive_count, d_alive_idx, cull, d_ctr);
+                   d_alive_count, cull, d_ctr);
   launches += 1;
   if (cull.live) {
-    launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count, d_alive_idx,
+    launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count, nullptr,
                   d_block_tmp, compact_blocks);
     launchCountCulled(stream, d_alive_count, w.samples, d_ctr);
     launches += 4;
@@ -1337,14 +1333,12 @@ void Tracer::traceWave(const Wave& w, bool capture) {
     }
     if (capture) captureShadows(b, S);
     // retire
-    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, d_alive_idx, sh,
-                     d_shadow_flag, S, nblk);
+    launchRetire(stream, d_image, d_views, d_alive_list, d_alive_count, rays[cur], sh, d_shadow_flag, S, nblk);
     launches += 1;
     // next depth
     if (b + 1 < nb_total) {
-      // compact this depth's alive list (not every sample of the wave): samples
-      // that stop get index -1, the ones dead before keep theirs (-1)
-      launchCompactCounted(stream, d_next_flag, d_alive_count, 1, d_alive_list2, d_alive_count2, d_alive_idx,
+      // compact this depth's alive list (not every sample of the wave)
+      launchCompactCounted(stream, d_next_flag, d_alive_count, 1, d_alive_list2, d_alive_count2, nullptr,
                            d_alive_list, d_block_tmp2, compact_blocks);
       std::swap(d_alive_list, d_alive_list2);
       std::swap(d_alive_count, d_alive_count2);
@@ -1654,19 +1648,22 @@ void Tracer::traceWaveBatched(const Wave& w) {
                   nullptr, d_block_tmp, compact_blocks);
     launches += 5;
     schedule(true, 0, d_shadow_count, d_shadow_list, S, false, true);
-    const int32_t* retire_idx = d_alive_idx;
+    // this depth's alive list stays for the retire below (the next depth's
+    // list goes to the other buffer)
+    const uint32_t* retire_list = d_alive_list;
+    const uint32_t* retire_count = d_alive_count;
     const bool more = b + 1 < nb_total;
     if (more) {
-      std::swap(d_alive_idx, d_alive_idx_prev);
-      launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list, d_alive_count,
-                    d_alive_idx, d_block_tmp, compact_blocks);
+      launchCompact(stream, d_next_flag, nullptr, 1, (uint64_t)w.samples, d_alive_list2, d_alive_count2, nullptr,
+                    d_block_tmp, compact_blocks);
+      std::swap(d_alive_list, d_alive_list2);
+      std::swap(d_alive_count, d_alive_count2);
       launches += 3;
       cur ^= 1;
       scheduleRadiance(false);
     }
     oocPass(more, true, S, rb);
-    launchRetireImpl(stream, d_image, d_tiles + w.first_tile, w.num_tiles, w.pixels, d_views, retire_idx, sh,
-                     d_shadow_flag, S, nblk);
+    launchRetire(stream, d_image, d_views, retire_list, retire_count, rays[cur], sh, d_shadow_flag, S, nblk);
     launches += 1;
   }
 }

@@ -310,9 +310,8 @@ class Tracer {
   int32_t* d_samid = nullptr;
   uint16_t* d_view = nullptr;
   uint32_t* d_alive_list = nullptr;
-  uint32_t* d_alive_list2 = nullptr;   // in core: the next depth's alive list (ping-pong)
+  uint32_t* d_alive_list2 = nullptr;   // the other depth's alive list (ping-pong)
   uint32_t* d_alive_count2 = nullptr;
-  int32_t* d_alive_idx = nullptr;
   uint32_t* d_alive_count = nullptr;
   uint8_t* d_next_flag = nullptr;
   uint64_t* d_ray_key = nullptr;
@@ -355,7 +354,6 @@ class Tracer {
   uint2* d_sentries = nullptr;     // batched out of core: shadow queues beside the radiance ones
   uint32_t* d_skey_start = nullptr;
   uint32_t* d_snum_entries = nullptr;
-  int32_t* d_alive_idx_prev = nullptr;  // alive index of the depth being retired
   uint32_t* d_live = nullptr;      // live entries per domain (radiance, shadow)
   int32_t* d_live_doms = nullptr;
   uint32_t* h_live = nullptr;      // pinned: domain list (D) + live counts (2 D)
