@@ -1169,9 +1169,9 @@ cudaEvent_t Tracer::poolEvent() {
 //
 // The eye rays are culled by the screen bins: the samples of pixels in bins
 // that no domain box's projection touches have an empty domain list, so they
-// stop here (no record, alive index -1) instead of passing through the
-// depth-0 scheduling, shading and compaction; a compaction of the live flags
-// makes the alive list in sample order.  The debug capture keeps every sample
+// stop here (no record, not in the alive list) instead of passing through
+// the depth-0 scheduling, shading, compaction and retire; a compaction of the
+// live flags makes the alive list in sample order.  The debug capture keeps every sample
 // alive (its ray and hit records cover every eye ray).
 void Tracer::beginWave(const Wave& w) {
   cur = 0;
